@@ -1,0 +1,358 @@
+"""Generate the golden fixtures under ``tests/golden/`` by running the upstream package.
+
+Run in a container that holds the upstream source tree (default ``/root/reference``,
+override with ``TQ_REFERENCE_ROOT``)::
+
+    python tests/golden/make_golden.py
+
+Outputs (all small ``.npz`` files, committed):
+
+* ``gate_matrices.npz`` -- every matrix builder of ``torchquantum.functional.mat_dict``
+  (``functional/__init__.py:97-123``) evaluated in complex128 mode on seeded parameters.
+* ``circuits.npz`` -- seeded random circuits executed gate by gate through
+  ``gate_wrapper`` -> ``apply_unitary_bmm`` (``functional/gate_wrapper.py:96,324``) in
+  complex128 mode: final states, ``expval_joint_analytical`` (``measurement/measurements.py:232``)
+  of random Pauli strings, probabilities, and the autograd gradient of a weighted sum of
+  the expvals with respect to every gate parameter.
+* ``config1.npz`` -- the small plain-method model: ``GeneralEncoder`` (rx,ry,rz,rx per
+  wire) + 2 x (``Op1QAllLayer(U3)`` + ``Op2QAllLayer(CNOT, circular)``) on 4 wires, bsz 32,
+  Z expval per wire, forward and autograd backward, in the upstream default complex64
+  and in complex128.
+* ``known_answers.npz`` -- the upstream known-answer tests (``test/device/test_init.py:32``,
+  ``test/functional/test_controlled_unitary.py:30``, ``test/functional/test_func_mat_exp.py:30``,
+  ``test/operator/test_ControlledU.py:40``, ``test/operator/test_op_hamil_exp.py:32``) and the
+  ``expval_joint_analytical`` docstring example (``measurement/measurements.py:246-256``):
+  the gate applications they make (matrix, wires, state before) and the expected
+  vectors they assert.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refimport  # noqa: E402
+
+tq = refimport.import_reference()
+import torchquantum.functional as tqf  # noqa: E402
+import importlib  # noqa: E402
+
+gw_mod = importlib.import_module("torchquantum.functional.gate_wrapper")
+from torchquantum.measurement import expval_joint_analytical  # noqa: E402
+
+# gates whose builder takes the number of wires instead of / besides params
+VAR_WIRE_NOPARAM = ("multicnot", "multixcnot", "qft")
+VAR_WIRE_PARAM = ("multirz",)
+# upstream builders that fail for a parameter batch > 1 (cu3/cu broadcast bug,
+# xxminyy/xxplusyy scalar indexing); they are exercised with batch 1 only
+BATCH1_ONLY = ("cu3", "cu", "xxminyy", "xxplusyy")
+BATCH1_FAILED = set()
+SKIP = ("qubitunitary", "qubitunitaryfast", "qubitunitarystrict", "globalphase")
+
+
+def gate_table():
+    """name -> (num_params, num_wires) from the upstream operator registry."""
+    table = {}
+    for name in tqf.mat_dict:
+        if name in SKIP:
+            continue
+        cls = tq.op_name_dict.get(name)
+        if cls is None:
+            alias = {"paulix": "x", "pauliy": "y", "pauliz": "z", "hadamard": "h"}.get(name)
+            cls = tq.op_name_dict[alias] if alias else None
+        if cls is None:
+            for c in tq.op_name_dict.values():
+                if getattr(c, "op_name", None) == name:
+                    cls = c
+                    break
+        table[name] = (int(cls.num_params), int(cls.num_wires))
+    return table
+
+
+def ref_matrix(name, params, n_wires=None):
+    mat = tqf.mat_dict[name]
+    if name in VAR_WIRE_NOPARAM:
+        return mat(n_wires)
+    if name in VAR_WIRE_PARAM:
+        return mat(params, n_wires)
+    if callable(mat):
+        return mat(params)
+    return mat
+
+
+def make_gate_matrices(rng):
+    refimport.set_reference_precision(True)
+    out = {}
+    meta = {}
+    for name, (npar, nw) in sorted(gate_table().items()):
+        variants = []
+        if name in VAR_WIRE_NOPARAM + VAR_WIRE_PARAM:
+            for k in (1, 2, 3, 4):
+                if name in VAR_WIRE_NOPARAM and name != "qft" and k < 2:
+                    continue
+                variants.append((k, 1))
+                if npar > 0:
+                    variants.append((k, 3))
+        else:
+            variants.append((nw, 1))
+            if npar > 0 and name not in BATCH1_ONLY:
+                variants.append((nw, 3))
+        for vi, (k, b) in enumerate(variants):
+            params = None
+            if npar > 0:
+                params = torch.tensor(rng.uniform(-np.pi, np.pi, size=(b, npar)), dtype=torch.float64)
+            try:
+                m = ref_matrix(name, params, n_wires=k)
+            except RuntimeError:
+                # upstream builder cannot take a parameter batch > 1 (broadcast bug)
+                BATCH1_FAILED.add(name)
+                continue
+            m = torch.as_tensor(m).to(torch.complex128).detach().numpy()
+            key = f"{name}__{vi}"
+            out[key + "__mat"] = m
+            if params is not None:
+                out[key + "__params"] = params.numpy()
+            meta[key] = {"name": name, "n_wires": k, "batch": b, "num_params": npar}
+    out["__meta__"] = np.array(json.dumps(meta))
+    out["__batch1_only__"] = np.array(json.dumps(sorted(BATCH1_FAILED | set(BATCH1_ONLY))))
+    np.savez_compressed(os.path.join(HERE, "gate_matrices.npz"), **out)
+    print(f"gate_matrices: {len(meta)} variants; batch-1-only builders: {sorted(BATCH1_FAILED)}")
+
+
+def circuit_gate_pool(n):
+    pool = []
+    for name, (npar, nw) in sorted(gate_table().items()):
+        if name in VAR_WIRE_NOPARAM + VAR_WIRE_PARAM:
+            for k in range(1 if name in ("qft", "multirz") else 2, min(n, 4) + 1):
+                pool.append((name, npar, k))
+        elif nw <= n:
+            pool.append((name, npar, nw))
+    return pool
+
+
+def random_unitary(rng, d):
+    z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def run_ref_circuit(n, bsz, gates, double=True):
+    """Execute a gate list through the upstream gate_wrapper; returns (qdev, leaf params)."""
+    refimport.set_reference_precision(double)
+    fdt = torch.float64 if double else torch.float32
+    cdt = torch.complex128 if double else torch.complex64
+    q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+    q.states = q.states.to(cdt)
+    leaves = []
+    for g in gates:
+        name = g["name"]
+        params = None
+        if g["params"] is not None:
+            params = torch.tensor(np.asarray(g["params"]), dtype=cdt if name == "qubitunitaryfast" else fdt,
+                                  requires_grad=name != "qubitunitaryfast")
+            leaves.append(params)
+        gw_mod.gate_wrapper(
+            name=name, mat=tqf.mat_dict[name], method="bmm", q_device=q, wires=g["wires"],
+            params=params, n_wires=g.get("n_wires"), inverse=g["inverse"],
+        )
+    return q, leaves
+
+
+def random_pauli(rng, n):
+    return "".join(rng.choice(list("IXYZ"), size=n))
+
+
+def make_circuits(rng):
+    cases = []
+    arrays = {}
+    specs = [(1, 1, 6), (2, 3, 12), (3, 1, 20), (3, 2, 20), (4, 3, 30), (5, 2, 40), (6, 1, 40), (7, 3, 50), (8, 2, 60)]
+    for ci, (n, bsz, depth) in enumerate(specs):
+        pool = circuit_gate_pool(n)
+        gates = []
+        for _ in range(depth):
+            name, npar, k = pool[rng.integers(len(pool))]
+            wires = [int(w) for w in rng.permutation(n)[:k]]
+            g = {"name": name, "wires": wires, "inverse": bool(rng.random() < 0.3), "params": None,
+                 "n_wires": k if name in VAR_WIRE_NOPARAM + VAR_WIRE_PARAM else None}
+            if npar > 0:
+                b = bsz if (rng.random() < 0.5 and name not in BATCH1_ONLY + tuple(BATCH1_FAILED)) else 1
+                g["params"] = rng.uniform(-np.pi, np.pi, size=(b, npar)).tolist()
+            gates.append(g)
+        # one dense random unitary on 1..3 wires through qubitunitaryfast
+        k = int(min(n, 1 + ci % 3))
+        u = random_unitary(rng, 2 ** k)
+        gates.insert(depth // 2, {"name": "qubitunitaryfast", "wires": [int(w) for w in rng.permutation(n)[:k]],
+                                  "inverse": False, "params": [[[complex(x) for x in row] for row in u]],
+                                  "n_wires": None})
+        paulis = [random_pauli(rng, n) for _ in range(4)] + ["Z" * 1 + "I" * (n - 1)]
+        weights = rng.normal(size=len(paulis))
+        q, leaves = run_ref_circuit(n, bsz, gates, double=True)
+        state = q.get_states_1d()
+        ev = torch.stack([expval_joint_analytical(q, p) for p in paulis], dim=-1)  # [bsz, m]
+        loss = (ev * torch.tensor(weights)).sum()
+        loss.backward()
+        # a builder that leaves the autograd graph (upstream defect) yields no gradient
+        grads = [lf.grad.numpy() if lf.grad is not None else np.full(tuple(lf.shape), np.nan) for lf in leaves]
+        key = f"c{ci}"
+        for g in gates:  # complex params are not JSON: store separately
+            if g["name"] == "qubitunitaryfast":
+                arrays[key + "__unitary"] = np.asarray(g["params"], dtype=np.complex128)
+                g["params"] = "unitary"
+        arrays[key + "__state"] = state.detach().numpy()
+        arrays[key + "__expval"] = ev.detach().numpy()
+        arrays[key + "__probs"] = (state.detach().abs() ** 2).numpy()
+        arrays[key + "__weights"] = weights
+        for gi, gr in enumerate(grads):
+            arrays[f"{key}__grad{gi}"] = gr
+        cases.append({"key": key, "n": n, "bsz": bsz, "gates": gates, "paulis": paulis, "n_grads": len(grads)})
+    arrays["__meta__"] = np.array(json.dumps(cases))
+    np.savez_compressed(os.path.join(HERE, "circuits.npz"), **arrays)
+    print(f"circuits: {len(cases)} cases")
+
+
+def config1_func_list():
+    funcs = ["rx", "ry", "rz", "rx"]
+    return [{"input_idx": [4 * g + w], "func": funcs[g], "wires": [w]} for g in range(4) for w in range(4)]
+
+
+def make_config1(rng):
+    n, bsz = 4, 32
+    x = rng.uniform(0, np.pi, size=(bsz, 16))
+    u3p = rng.uniform(-np.pi, np.pi, size=(2, n, 3))
+    w = rng.normal(size=(bsz, n))
+    out = {"x": x, "u3_params": u3p, "loss_weights": w}
+    for double in (False, True):
+        refimport.set_reference_precision(double)
+        fdt = torch.float64 if double else torch.float32
+        enc = tq.GeneralEncoder(config1_func_list())
+        layers = []
+        for layer in range(2):
+            l1 = tq.layer.Op1QAllLayer(op=tq.U3, n_wires=n, has_params=True, trainable=True)
+            for wi in range(n):
+                l1.ops_all[wi].params.data = torch.tensor(u3p[layer, wi][None, :], dtype=fdt)
+            l2 = tq.layer.Op2QAllLayer(op=tq.CNOT, n_wires=n, circular=True)
+            layers += [l1, l2]
+        xt = torch.tensor(x, dtype=fdt, requires_grad=True)
+        q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+        if double:
+            q.states = q.states.to(torch.complex128)
+        enc(q, xt)
+        for lay in layers:
+            lay(q)
+        obs = ["".join("Z" if i == j else "I" for i in range(n)) for j in range(n)]
+        ev = torch.stack([expval_joint_analytical(q, o) for o in obs], dim=-1)
+        loss = (ev * torch.tensor(w, dtype=fdt)).sum()
+        loss.backward()
+        tag = "c128" if double else "c64"
+        out[f"{tag}__expval"] = ev.detach().numpy()
+        out[f"{tag}__state"] = q.get_states_1d().detach().numpy()
+        out[f"{tag}__grad_x"] = xt.grad.numpy()
+        out[f"{tag}__grad_u3"] = np.stack(
+            [np.stack([layers[2 * l].ops_all[wi].params.grad.numpy()[0] for wi in range(n)]) for l in range(2)])
+    refimport.set_reference_precision(False)
+    np.savez_compressed(os.path.join(HERE, "config1.npz"), **out)
+    print("config1: done")
+
+
+class _Recorder:
+    """Wraps apply_unitary_bmm / check_all_close to capture what a test does."""
+
+    def __init__(self):
+        self.events = []
+        self._orig_apply = gw_mod.apply_unitary_bmm
+
+    def apply(self, state, mat, wires):
+        self.events.append({"kind": "apply", "wires": [int(w) for w in wires],
+                            "mat": mat.detach().to(torch.complex128).numpy().copy(),
+                            "state_in": state.detach().reshape(state.shape[0], -1).to(torch.complex128).numpy().copy()})
+        return self._orig_apply(state, mat, wires)
+
+    def check(self, a, b, rtol=1e-5, atol=1e-4):
+        a = a.detach().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+        b = b.detach().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+        self.events.append({"kind": "expect", "actual": a.astype(np.complex128), "expected": b.astype(np.complex128)})
+        np.testing.assert_allclose(a, b, rtol=rtol, atol=atol)
+
+
+def make_known_answers():
+    refimport.set_reference_precision(False)
+    root = refimport.REFERENCE_ROOT
+    sys.path.insert(0, root)
+    cwd = os.getcwd()
+    os.chdir(root)
+    import importlib
+
+    tests = [
+        ("test.device.test_init", "test_state_init"),
+        ("test.functional.test_controlled_unitary", "test_controlled_unitary"),
+        ("test.functional.test_func_mat_exp", "test_func_mat_exp"),
+        ("test.operator.test_ControlledU", "test_ContorlledU"),
+        ("test.operator.test_op_hamil_exp", "test_op_hamil_exp"),
+    ]
+    arrays = {}
+    index = []
+    try:
+        for modname, fn in tests:
+            mod = importlib.import_module(modname)
+            rec = _Recorder()
+            gw_mod.apply_unitary_bmm = rec.apply
+            if hasattr(mod, "check_all_close"):
+                mod.check_all_close = rec.check
+            orig_eq = np.testing.assert_array_equal
+
+            def eq(a, b, *args, _rec=rec, **kw):
+                _rec.check(a, b, rtol=0, atol=0)
+
+            np.testing.assert_array_equal = eq
+            orig_allclose = np.allclose
+
+            def allclose(a, b, *args, _rec=rec, **kw):
+                _rec.events.append({"kind": "expect", "actual": np.asarray(a).astype(np.complex128),
+                                    "expected": np.asarray(b).astype(np.complex128)})
+                return orig_allclose(a, b, *args, **kw)
+
+            np.allclose = allclose
+            try:
+                getattr(mod, fn)()
+            finally:
+                gw_mod.apply_unitary_bmm = rec._orig_apply
+                np.testing.assert_array_equal = orig_eq
+                np.allclose = orig_allclose
+            key = f"{modname.split('.')[-1]}"
+            ev_meta = []
+            for ei, ev in enumerate(rec.events):
+                if ev["kind"] == "apply":
+                    arrays[f"{key}__{ei}__mat"] = ev["mat"]
+                    arrays[f"{key}__{ei}__state_in"] = ev["state_in"]
+                    ev_meta.append({"kind": "apply", "wires": ev["wires"]})
+                else:
+                    arrays[f"{key}__{ei}__expected"] = ev["expected"]
+                    ev_meta.append({"kind": "expect"})
+            index.append({"key": key, "source": f"{modname.replace('.', '/')}.py::{fn}", "events": ev_meta})
+            print(f"known answer {key}: {len(rec.events)} events")
+    finally:
+        os.chdir(cwd)
+    # expval_joint_analytical docstring example (measurement/measurements.py:246-256)
+    q = tq.QuantumDevice(n_wires=2)
+    tqf.hadamard(q, wires=0)
+    tqf.x(q, wires=1)
+    tqf.cnot(q, wires=[0, 1])
+    arrays["docstring__state"] = q.get_states_1d().detach().to(torch.complex128).numpy()
+    arrays["docstring__expval"] = np.array([float(expval_joint_analytical(q, o)[0]) for o in ("II", "XX", "ZZ")])
+    index.append({"key": "docstring", "source": "torchquantum/measurement/measurements.py:246-256",
+                  "paulis": ["II", "XX", "ZZ"], "expected": [1.0, 1.0, -1.0]})
+    arrays["__meta__"] = np.array(json.dumps(index))
+    np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **arrays)
+
+
+if __name__ == "__main__":
+    torch.manual_seed(0)
+    make_gate_matrices(np.random.default_rng(1))
+    make_circuits(np.random.default_rng(2))
+    make_config1(np.random.default_rng(3))
+    make_known_answers()
