@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark: forward + adjoint backward of a depth-400 random circuit on 24 qubits.
+
+Workload (synthetic, seeded): n_wires=24, bsz=16 (a 2 GiB complex64 state); 400 gates,
+each a U3 on a uniform wire with probability 0.6 (angles ~U[-pi, pi) per sample) or a
+uniform choice of CNOT / CZ / CRX(theta per sample) on a uniform ordered wire pair.
+One step = |0..0> init, the 400 gates, the full probabilities [16, 2^24], the
+expectation values of 8 random 24-site Pauli strings, and the gradient of their sum
+with respect to every gate angle (adjoint method).  ``value`` is circuits/s
+(bsz x steps / device time) with inputs resident in HBM; ``e2e`` is the same through
+the public API with the angles copied from pinned host memory and the expvals and
+gradients copied back every step.  The state (2 GiB) is larger than L2 (129 MB), so no
+flush is needed between steps.
+
+``--impl reference`` times the CPU oracle's restatement of the upstream algorithm
+(torch-autograd-style forward keeping every gate's input state, then the reverse
+sweep) on the host cores, on a bounded sample of the same circuit, extrapolated to
+circuits/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+bwd circuits/s fused+adjoint vs plain at <=1e-5 vs FP64; HBM GB/s per gate"
+UNIT = "circuits/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="plain", choices=["plain", "fused"])
+    ap.add_argument("--n", type=int, default=24)
+    ap.add_argument("--bsz", type=int, default=16)
+    ap.add_argument("--depth", type=int, default=400)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the baseline sample")
+    ap.add_argument("--quick", action="store_true", help="skip e2e/roofline/baseline (profiling runs)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ CPU (oracle) leg
+def cpu_sample(args, seconds: float):
+    """Time the oracle's autograd-style fwd + reverse sweep on one circuit of the
+    workload (bsz 1) over the first G gates, G sized to ~``seconds``; returns
+    (circuits/s extrapolated to the full depth, description, threads)."""
+    from oracle import statevec as O
+    from torchquantum_gb300 import workloads as W
+
+    gates, ncols = W.random_circuit(args.n, args.depth, seed=0)
+    theta = W.random_params(1, ncols, seed=1)
+    og = W.oracle_gates(gates, theta)
+
+    def run(g):
+        t0 = time.perf_counter()
+        s, saved, mats = O.forward_saving(args.n, 1, og[:g], np.complex64)
+        O.backward_sweep(args.n, og[:g], saved, mats, s.copy())
+        return time.perf_counter() - t0
+
+    t1 = run(2) / 2
+    g = int(max(2, min(args.depth, seconds / max(t1, 1e-6))))
+    t = run(g)
+    per_circuit = t / g * args.depth
+    threads = os.cpu_count() or 1
+    desc = (f"oracle (numpy complex64) fwd keeping per-gate states + reverse sweep, n={args.n}, 1 circuit, "
+            f"first {g} of {args.depth} gates in {t:.1f} s, extrapolated to the full depth")
+    return 1.0 / per_circuit, desc, threads, g, t
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = args.warmup
+    from oracle import statevec as O
+    from torchquantum_gb300 import workloads as W
+
+    gates, ncols = W.random_circuit(args.n, args.depth, seed=0)
+    theta = W.random_params(1, ncols, seed=1)
+    og = W.oracle_gates(gates, theta)
+
+    def one(g):
+        s, saved, mats = O.forward_saving(args.n, 1, og[:g], np.complex64)
+        O.backward_sweep(args.n, og[:g], saved, mats, s.copy())
+
+    t0 = time.perf_counter()
+    one(1)
+    t1 = time.perf_counter() - t0
+    # each step is a bounded sample sized so steps+warmup fit in ~3 minutes
+    budget = 180.0 / max(1, args.steps + w)
+    g = int(max(1, min(args.depth, budget / max(t1, 1e-6))))
+    for _ in range(w):
+        one(g)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        one(g)
+        times.append(time.perf_counter() - t0)
+    per_step = sum(times) / len(times)
+    value = 1.0 / (per_step / g * args.depth)
+    threads = os.cpu_count() or 1
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": _config(args, "plain"), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"1 circuit, first {g} of {args.depth} gates fwd+bwd per step, extrapolated"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _config(args, method):
+    return {"workload": f"random circuit n={args.n} bsz={args.bsz} depth={args.depth} "
+                        "(U3 60%, CNOT/CZ/CRX 40%) + probs + 8 Pauli expvals, fwd + adjoint bwd",
+            "n_wires": args.n, "global_batch": args.bsz, "depth": args.depth, "method": method,
+            "l2_flush": "none needed: state 2 GiB > L2 129 MB"}
+
+
+# ------------------------------------------------------------------ GPU leg
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import _lib
+    from torchquantum_gb300 import workloads as W
+
+    n, bsz = args.n, args.bsz
+    gates, ncols = W.random_circuit(n, args.depth, seed=0)
+    theta_host = W.random_params(bsz, ncols, seed=1 + rank)
+    paulis = W.random_paulis(n, 8, seed=2)
+    pw = torch.tensor(np.random.default_rng(3).normal(size=(1, 8)), dtype=torch.float32, device=dev)
+    theta_dev = torch.tensor(theta_host, device=dev)
+
+    def step(theta):
+        q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
+        if args.method == "fused":
+            q.method = "fused"
+        W.apply_circuit(q, gates, theta)
+        pr = tq.probs(q)
+        ev = tq.expval_joint_analytical_batch(q, paulis)
+        (ev * pw).sum().backward()
+        return ev, pr
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    th = theta_dev.clone().requires_grad_(True)
+    for _ in range(args.warmup):
+        th.grad = None
+        step(th)
+    torch.cuda.synchronize()
+    barrier()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _lib.LAUNCHES[0]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            th.grad = None
+            step(th)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = _lib.LAUNCHES[0] - launches0
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t.item())
+    value = bsz * args.steps * world / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": _config(args, args.method),
+            "clocks": clk.summary(), "gpu_launches": launches}
+    if world > 1:
+        line["config"]["parallelism"] = f"replicas x{world} (batch sharding, no collective in the step)"
+
+    if not args.quick:
+        # ---------------- end to end through the public API with host buffers
+        pin_theta = torch.from_numpy(theta_host).pin_memory()
+        out_ev = torch.empty(bsz, 8, dtype=torch.float32).pin_memory()
+        out_g = torch.empty(bsz, ncols, dtype=torch.float32).pin_memory()
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            thd = pin_theta.to(dev, non_blocking=True).requires_grad_(True)
+            ev, _ = step(thd)
+            out_ev.copy_(ev.detach(), non_blocking=True)
+            out_g.copy_(thd.grad, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = e0.elapsed_time(e1)
+        t = torch.tensor([ms_e2e], device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+        line["e2e"] = {"value": bsz * args.steps * world / (ms_e2e / 1e3), "unit": UNIT,
+                       "h2d_bytes_per_step": int(pin_theta.numel() * 4),
+                       "d2h_bytes_per_step": int(out_ev.numel() * 4 + out_g.numel() * 4)}
+        # ---------------- roofline of the dominant kernel (adjoint dense 1-wire step)
+        line["roofline"], line["kernels"] = roofline(args, dev)
+        line["plain_gate_pass"] = line["kernels"]["dense1_fwd"]
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.quick:
+        v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def roofline(args, dev):
+    """Time the engine's hot kernels alone (CUDA events on the launching stream) on the
+    bench's state size; algorithmic bytes per launch from the touched amplitudes."""
+    import torch
+
+    from torchquantum_gb300 import _lib
+
+    n, bsz = args.n, args.bsz
+    S = bsz * (1 << n) * 8
+    psi = torch.zeros(bsz, 1 << n, dtype=torch.complex64, device=dev)
+    psi[:, 0] = 1
+    lam = psi.clone()
+    mat = torch.tensor(np.tile(np.eye(2), (bsz, 1, 1)), dtype=torch.complex64, device=dev)
+    mat4 = torch.tensor(np.tile(np.eye(2), (bsz, 1, 1)), dtype=torch.complex64, device=dev)
+    grad = torch.zeros(bsz * 8, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    peak, peak_kind = _peaks()
+    reps = 24
+    res = {}
+
+    def timeit(fn):
+        for w in range(3):
+            fn(w)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for i in range(reps):
+            fn(i)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps / 1e3
+
+    wires = [int(w) for w in np.random.default_rng(0).integers(0, n, size=reps + 3)]
+    pairs = [tuple(int(x) for x in np.random.default_rng(i).choice(n, 2, replace=False)) for i in range(reps + 3)]
+    kernels = {
+        "dense1_fwd": (lambda i: _lib.apply_matrix(psi, n, [wires[i]], mat, bsz), 2 * S),
+        "dense1_adj": (lambda i: _lib.adjoint_matrix(psi, lam, n, [wires[i]], mat, bsz, grad), 4 * S),
+        "crx_fwd": (lambda i: _lib.apply_controlled(psi, n, [pairs[i][0]], [pairs[i][1]], mat4, bsz), S),
+        "cnot_fwd": (lambda i: _lib.apply_mcx(psi, n, [pairs[i][0]], 1, pairs[i][1]), S),
+        "cz_fwd": (lambda i: _lib.apply_phase(psi, n, list(pairs[i]), mat[:, 0, 0].contiguous(), bsz), S // 2),
+    }
+    for name, (fn, nbytes) in kernels.items():
+        t = timeit(fn)
+        gbs = nbytes / t / 1e9
+        res[name] = {"us": t * 1e6, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak}
+    dom = res["dense1_adj"]
+    roof = {"bound": "hbm", "achieved": dom["GB/s"], "peak": peak, "unit": "GB/s", "frac": dom["GB/s"] / peak,
+            "traffic": None, "kernel": "k_dense_adj<2> (adjoint step of a dense 1-wire gate)",
+            "peak_source": f"{peak_kind} hbm_gbs"}
+    return roof, res
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

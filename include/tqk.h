@@ -1,0 +1,127 @@
+/*
+ * tqk.h -- C ABI of the GB300 statevector engine (libtqk.so).
+ *
+ * Plain pointers and sizes only.  Every entry point:
+ *   - takes device pointers for statevectors / matrices / outputs,
+ *   - takes the CUDA stream to launch on as an opaque handle (cudaStream_t / CUstream),
+ *   - validates its arguments on the host and returns a TQK_* status (0 = OK),
+ *   - never synchronises the stream and never allocates device memory; callers pass
+ *     scratch buffers sized by the matching *_scratch_bytes query.
+ * tqk_last_error() returns the message of the last failing call on this host thread.
+ *
+ * Layout: a statevector is complex64 (interleaved float re, im) of shape [bsz, 2^n];
+ * wire 0 is the MOST significant bit of the in-row index.  A k-wire matrix is
+ * complex64 row-major [mat_batch, 2^k, 2^k] indexed with wires[0] most significant;
+ * mat_batch is 1 (broadcast over the state batch) or bsz (one matrix per row).
+ *
+ * Each declaration cites the upstream torchquantum interface it replaces
+ * (path:line inside the upstream project).
+ */
+#ifndef TQK_H_
+#define TQK_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TQK_OK = 0,
+  TQK_BAD_WIRES = 1,        /* wire out of range, duplicated, or too many */
+  TQK_BAD_SHAPE = 2,        /* bsz / n / batch / size inconsistent */
+  TQK_BAD_POINTER = 3,      /* null or misaligned pointer */
+  TQK_TOO_MANY_QUBITS = 4,  /* n or k beyond the supported maximum */
+  TQK_CUDA_ERROR = 5,       /* a CUDA launch or API call failed */
+  TQK_TIMEOUT = 6,          /* a bounded device-side wait gave up */
+  TQK_SCRATCH_TOO_SMALL = 7,
+  TQK_UNSUPPORTED = 8
+};
+
+#define TQK_MAX_QUBITS 34      /* per batch row */
+#define TQK_MAX_DENSE_WIRES 12 /* generic dense gate width */
+
+const char* tqk_last_error(void);
+int tqk_version(void);
+
+/* ---------------------------------------------------------------- gate application
+ * Replaces functional/gate_wrapper.py:96-140 (apply_unitary_bmm) and :18-93
+ * (apply_unitary_einsum), as dispatched from gate_wrapper (gate_wrapper.py:441-446).
+ * All are in place on `state`. */
+
+/* Dense U (2^k x 2^k) on `wires` (k = 1..TQK_MAX_DENSE_WIRES). */
+int tqk_apply_matrix(void* state, int64_t bsz, int n, const int32_t* wires, int k,
+                     const void* mat, int64_t mat_batch, void* stream);
+
+/* Controlled dense block: the 2^kt x 2^kt block `mat` acts on `targets` (kt = 1 or 2)
+ * where every control wire is 1.  Same operator as the upstream 2^(nc+kt) matrix whose
+ * upper-left block is identity (e.g. crx_matrix, functional/rx.py:87-115). */
+int tqk_apply_controlled(void* state, int64_t bsz, int n, const int32_t* controls, int nc,
+                         const int32_t* targets, int kt, const void* mat, int64_t mat_batch,
+                         void* stream);
+
+/* Multi-controlled X on `target` where every control equals ctrl_val (1: cnot/toffoli/
+ * multicnot, functional/paulix.py; 0: multixcnot).  nc may be 0 (Pauli X). */
+int tqk_apply_mcx(void* state, int64_t bsz, int n, const int32_t* controls, int nc, int ctrl_val,
+                  int target, void* stream);
+
+/* Multiply amplitudes whose `wires` are all 1 by phase[b] (complex64, phase_batch 1|bsz).
+ * k = 0 multiplies every amplitude (globalphase).  cz/ccz/s/t/u1/cu1/... */
+int tqk_apply_phase(void* state, int64_t bsz, int n, const int32_t* wires, int k,
+                    const void* phase, int64_t phase_batch, void* stream);
+
+/* Diagonal gate: amplitude *= diag[b][bits of `wires`] (diag complex64 [batch, 2^k]).
+ * rz/rzz/crz/multirz (functional/rz.py). */
+int tqk_apply_diagonal(void* state, int64_t bsz, int n, const int32_t* wires, int k,
+                       const void* diag, int64_t diag_batch, void* stream);
+
+/* Exchange |..0 1> and |..1 0> on (w0, w1) where every control is 1 (swap, cswap). */
+int tqk_apply_swap(void* state, int64_t bsz, int n, const int32_t* controls, int nc, int w0,
+                   int w1, void* stream);
+
+/* Reset `wires` to |0> and renormalise each row (functional/reset.py). */
+int64_t tqk_reset_scratch_bytes(int64_t bsz, int n);
+int tqk_reset(void* state, int64_t bsz, int n, const int32_t* wires, int k, void* scratch,
+              int64_t scratch_bytes, void* stream);
+
+/* ---------------------------------------------------------------- measurement
+ * |psi|^2 as float32 [bsz, 2^n] (the probabilities read by measurements.py:297-299). */
+int tqk_probs(const void* state, int64_t bsz, int n, float* out, void* stream);
+
+/* Expectation values of m Pauli strings, out[b*m + j] = Re <psi_b| P_j |psi_b> (float64).
+ * P_j is given by bit masks over the in-row index (bit n-1-w <-> wire w):
+ * xmask = X|Y positions, zmask = Z|Y positions; the i^(#Y) factor is applied.
+ * Replaces expval_joint_analytical (measurement/measurements.py:232-279), which
+ * builds a dense 2^n x 2^n kron Hamiltonian.  Deterministic (fixed-order reduction). */
+int64_t tqk_pauli_expval_scratch_bytes(int64_t bsz, int n, int m);
+int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uint64_t* xmask,
+                     const uint64_t* zmask, int m, double* out, void* scratch,
+                     int64_t scratch_bytes, void* stream);
+
+/* out = sum_j coef[b*m + j] * P_j psi  (complex64 [bsz, 2^n]; coef float32 device).
+ * The backward of the expvals above (cotangent of psi). */
+int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const uint64_t* xmask,
+                        const uint64_t* zmask, int m, const float* coef, void* out,
+                        void* stream);
+
+/* ---------------------------------------------------------------- adjoint backward
+ * One reverse step of the adjoint method for a gate applied with the matching forward
+ * entry point above: psi <- U^H psi, lam <- U^H lam, and (if grad != NULL)
+ * grad[g] += sum over the gate's amplitude groups of lam_after * conj(psi_before)^T,
+ * accumulated in float64 (complex128 interleaved), g = batch row if the operand is
+ * per-row else 0.  Replaces the autograd graph of torch.bmm/permute recorded by
+ * apply_unitary_bmm (gate_wrapper.py:127-138).  grad must be zeroed by the caller. */
+int tqk_adjoint_matrix(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
+                       const void* mat, int64_t mat_batch, double* grad, void* stream);
+int tqk_adjoint_controlled(void* psi, void* lam, int64_t bsz, int n, const int32_t* controls,
+                           int nc, const int32_t* targets, int kt, const void* mat,
+                           int64_t mat_batch, double* grad, void* stream);
+int tqk_adjoint_phase(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
+                      const void* phase, int64_t phase_batch, double* grad, void* stream);
+int tqk_adjoint_diagonal(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
+                         const void* diag, int64_t diag_batch, double* grad, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TQK_H_ */

@@ -355,3 +355,38 @@ def fd_grads(n, bsz, gates, paulis, weights, h=1e-3, state=None):
                 gr[idx] += sgn * loss_expvals(n, bsz, gg, paulis, weights, state) / (2 * h)
         out.append(gr)
     return out
+
+
+# ----------------------------------------------------------------------- CPU baseline
+def forward_saving(n: int, bsz: int, gates: List[Dict], dtype=np.complex64):
+    """Forward pass that keeps every gate's input state, as torch autograd does for
+    upstream's apply_unitary_bmm (gate_wrapper.py:127-136); returns (final, saved, mats)."""
+    s = init_state(n, bsz).astype(dtype)
+    saved, mats = [], []
+    for g in gates:
+        wires = list(g["wires"])
+        m = gate_matrix(g["name"], g.get("params"), len(wires), g.get("inverse", False)).astype(dtype)
+        saved.append(s)
+        mats.append(m)
+        s = apply(s, m, wires, n).astype(dtype)
+    return s, saved, mats
+
+
+def backward_sweep(n: int, gates: List[Dict], saved, mats, lam: np.ndarray):
+    """Reverse sweep of the saved-state forward: per gate, the matrix cotangent
+    sum_cols lam psi_in^H (what torch.bmm's backward computes) and lam <- U^H lam."""
+    grads = [None] * len(gates)
+    bsz = lam.shape[0]
+    for i in range(len(gates) - 1, -1, -1):
+        wires = list(gates[i]["wires"])
+        k = len(wires)
+        m = mats[i]
+        axes = [w + 1 for w in wires]
+        rest = [a for a in range(1, n + 1) if a not in axes]
+        perm = [0] + axes + rest
+        lp = np.transpose(lam.reshape([bsz] + [2] * n), perm).reshape(bsz, 1 << k, -1)
+        pp = np.transpose(saved[i].reshape([bsz] + [2] * n), perm).reshape(bsz, 1 << k, -1)
+        g = np.matmul(lp, np.conj(np.swapaxes(pp, -1, -2)))
+        grads[i] = g.sum(0, keepdims=True) if m.shape[0] == 1 else g
+        lam = apply(lam, np.conj(np.swapaxes(m, -1, -2)), wires, n).astype(lam.dtype)
+    return grads, lam

@@ -1,0 +1,48 @@
+"""Host-side logic that needs no GPU: Pauli masks, gate structure table, op construction."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import statevec as O
+from torchquantum_gb300 import gates as G
+from torchquantum_gb300.measurement import pauli_masks
+
+
+@pytest.mark.parametrize("obs", ["ZIII", "IXYZ", "YYYY", "XIZY", "IIII"])
+def test_pauli_masks_match_oracle(obs):
+    x, z, _ = O.pauli_masks(obs, 4)
+    assert pauli_masks(obs, 4) == (x, z)
+
+
+def test_every_upstream_gate_name_present():
+    from tests.golden_data import load
+
+    _, meta = load("gate_matrices")
+    names = {m["name"] for m in meta.values()}
+    for nm in names:
+        assert G.canonical_name(nm) in G.GATES, nm
+
+
+def test_structured_ops_are_consistent_with_matrix():
+    """The block the engine reads for ctrl/phase/diag gates reproduces the full matrix."""
+    for name, gd in G.GATES.items():
+        if gd.num_wires <= 0 or name.startswith("qubitunitary"):
+            continue
+        p = torch.rand(2, gd.num_params, dtype=torch.float64) if gd.num_params > 0 else None
+        m = G.gate_matrix(name, p, gd.num_wires, dtype=torch.complex128)
+        d = m.shape[-1]
+        kind = gd.struct[0]
+        if kind == "ctrl":
+            full = torch.eye(d, dtype=m.dtype).expand_as(m).clone()
+            full[:, -2:, -2:] = m[:, -2:, -2:]
+            assert torch.allclose(full, m), name
+        elif kind == "phase":
+            full = torch.eye(d, dtype=m.dtype).expand_as(m).clone()
+            full[:, -1, -1] = m[:, -1, -1]
+            assert torch.allclose(full, m), name
+        elif kind == "diag":
+            assert torch.allclose(torch.diag_embed(torch.diagonal(m, dim1=-2, dim2=-1)), m), name
+        elif kind == "x":
+            nc = gd.struct[1] if gd.struct[1] >= 0 else gd.num_wires - 1
+            ref = O.gate_matrix(name, None, gd.num_wires)[0]
+            assert np.allclose(m[0].numpy(), ref), name

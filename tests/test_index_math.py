@@ -1,0 +1,183 @@
+"""CPU model of the kernels' thread -> amplitude index mapping (csrc/apply.cu,
+csrc/measure.cu).  For every launch shape the host code picks, checks that each
+access is inside the row, that float4 accesses are 16-byte aligned, and that the
+gate's amplitude groups are covered exactly once."""
+import itertools
+
+import pytest
+
+
+def insert_zero_bits(g, pos):
+    for q in sorted(pos):
+        lo = g & ((1 << q) - 1)
+        g = ((g >> q) << (q + 1)) | lo
+    return g
+
+
+def dense_accesses(n, tbits, cbits):
+    """Addresses touched by k_dense<D, MODE> for targets tbits (matrix MSB first), controls cbits."""
+    kt = len(tbits)
+    D = 1 << kt
+    touched = set(tbits) | set(cbits)
+    groups = 1 << (n - len(touched))
+    setmask = sum(1 << c for c in cbits)
+    off = []
+    for r in range(D):
+        o = 0
+        for j in range(kt):
+            if (r >> (kt - 1 - j)) & 1:
+                o |= 1 << tbits[j]
+        off.append(o)
+    bit0_ctrl = 0 in cbits
+    bit0_tgt = 0 in tbits
+    mode = "scl" if bit0_ctrl else ("low" if bit0_tgt else "vec")
+    pair = [-1] * D
+    if mode == "low":
+        for r in range(D):
+            if off[r] & 1 == 0:
+                for r2 in range(D):
+                    if off[r2] == off[r] | 1:
+                        pair[r] = r2
+    acc = []
+    pairs = (groups + 1) >> 1
+    for t in range(pairs):
+        g0 = 2 * t
+        two = g0 + 1 < groups
+        if mode == "vec":
+            base = insert_zero_bits(g0, touched) | setmask
+            for r in range(D):
+                a = base + off[r]
+                assert a % 2 == 0, "float4 access must be 16-byte aligned"
+                acc += [a, a + 1]
+        else:
+            for j in range(2):
+                if j == 1 and not two:
+                    break
+                base = insert_zero_bits(g0 + j, touched) | setmask
+                for r in range(D):
+                    if mode == "low":
+                        if pair[r] >= 0:
+                            a = base + off[r]
+                            assert a % 2 == 0
+                            acc += [a, a + 1]
+                    else:
+                        acc.append(base + off[r])
+    return acc, setmask, touched
+
+
+def expected_group_amps(n, tbits, cbits):
+    want = []
+    for i in range(1 << n):
+        if all((i >> c) & 1 for c in cbits):
+            want.append(i)
+    return want
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 6])
+def test_dense_1_and_2_target_cover_exactly_once(n):
+    bits = list(range(n))
+    for kt in (1, 2):
+        for tb in itertools.permutations(bits, kt):
+            rest = [b for b in bits if b not in tb]
+            for nc in range(0, min(2, len(rest)) + 1):
+                for cb in itertools.combinations(rest, nc):
+                    acc, _, _ = dense_accesses(n, list(tb), list(cb))
+                    assert all(0 <= a < (1 << n) for a in acc)
+                    assert sorted(acc) == expected_group_amps(n, tb, cb), (n, tb, cb)
+
+
+def mcx_accesses(n, cbits, tbit, ctrl_val):
+    touched = set(cbits) | {tbit}
+    groups = 1 << (n - len(touched))
+    setmask = sum(1 << c for c in cbits) if ctrl_val else 0
+    bit0_ctrl, bit0_tgt = 0 in cbits, tbit == 0
+    mode = "scl" if bit0_ctrl else ("low" if bit0_tgt else "vec")
+    work = groups // 2 if mode == "vec" else groups
+    acc = []
+    for t in range(work):
+        if mode == "vec":
+            i0 = insert_zero_bits(2 * t, touched) | setmask
+            assert i0 % 2 == 0 and (i0 | (1 << tbit)) % 2 == 0
+            acc += [i0, i0 + 1, i0 | (1 << tbit), (i0 | (1 << tbit)) + 1]
+        elif mode == "low":
+            i0 = insert_zero_bits(t, touched) | setmask
+            assert i0 % 2 == 0
+            acc += [i0, i0 + 1]
+        else:
+            i0 = insert_zero_bits(t, touched) | setmask
+            acc += [i0, i0 | (1 << tbit)]
+    return acc
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5])
+def test_mcx_covers_controlled_pairs(n):
+    bits = list(range(n))
+    for tb in bits:
+        rest = [b for b in bits if b != tb]
+        for nc in range(0, min(3, len(rest)) + 1):
+            for cb in itertools.combinations(rest, nc):
+                for cv in (0, 1):
+                    acc = mcx_accesses(n, list(cb), tb, cv)
+                    want = [i for i in range(1 << n) if all(((i >> c) & 1) == cv for c in cb)]
+                    assert sorted(acc) == want, (n, tb, cb, cv)
+
+
+@pytest.mark.parametrize("n", [2, 3, 5])
+def test_swap_and_phase_cover(n):
+    bits = list(range(n))
+    for b0, b1 in itertools.permutations(bits, 2):
+        touched = {b0, b1}
+        groups = 1 << (n - 2)
+        vec = 0 not in touched
+        acc = []
+        for t in range(groups // 2 if vec else groups):
+            if vec:
+                base = insert_zero_bits(2 * t, touched)
+                for a in (base | (1 << b1), base | (1 << b0)):
+                    assert a % 2 == 0
+                    acc += [a, a + 1]
+            else:
+                base = insert_zero_bits(t, touched)
+                acc += [base | (1 << b1), base | (1 << b0)]
+        want = [i for i in range(1 << n) if ((i >> b0) & 1) != ((i >> b1) & 1)]
+        assert sorted(acc) == want
+    for k in range(0, n + 1):
+        for wb in itertools.combinations(bits, k):
+            touched = set(wb)
+            groups = 1 << (n - k)
+            vec = 0 not in touched
+            mask = sum(1 << b for b in wb)
+            acc = []
+            for t in range(groups // 2 if vec else groups):
+                i0 = insert_zero_bits(2 * t if vec else t, touched) | mask
+                acc += [i0, i0 + 1] if vec else [i0]
+            assert sorted(acc) == [i for i in range(1 << n) if i & mask == mask]
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 6])
+def test_expval_pair_iteration_covers_each_pair_once(n):
+    for x in range(1, 1 << n):
+        h = x.bit_length() - 1
+        seen = []
+        if x == 1:
+            for t in range((1 << n) >> 1):
+                i = 2 * t
+                seen += [(i, i + 1)]
+        else:
+            lomask = (1 << h) - 1
+            for t in range((1 << n) >> 2):
+                g = 2 * t
+                i = ((g >> h) << (h + 1)) | (g & lomask)
+                ip = i ^ x
+                assert i % 2 == 0 and 0 <= (ip & ~1) < (1 << n)
+                seen += [(i, ip), (i + 1, ip ^ 1)]
+        want = sorted((i, i ^ x) for i in range(1 << n) if not (i >> h) & 1)
+        assert sorted(seen) == want, x
+
+
+def test_dense_k_groups_per_block_fit_shared_memory():
+    for k in range(1, 13):
+        D = 1 << k
+        gpb = 1 if D >= 256 else 256 // D
+        assert gpb * D <= 16 * 256
+        assert gpb * D * 8 <= 200 * 1024

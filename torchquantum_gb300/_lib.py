@@ -1,0 +1,215 @@
+"""ctypes binding of libtqk.so (C ABI declared in include/tqk.h).
+
+The library is loaded from the package directory; if it is missing the import of
+any engine function raises -- there is no CPU fallback.  Every wrapper raises
+``TQKError`` (a ``RuntimeError``) carrying the library's message when a call
+returns a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from typing import Optional, Sequence
+
+import torch
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libtqk.so")
+HEADER = os.path.join(os.path.dirname(_PKG), "include", "tqk.h")
+
+TQK_STATUS = {
+    0: "OK", 1: "BAD_WIRES", 2: "BAD_SHAPE", 3: "BAD_POINTER", 4: "TOO_MANY_QUBITS",
+    5: "CUDA_ERROR", 6: "TIMEOUT", 7: "SCRATCH_TOO_SMALL", 8: "UNSUPPORTED",
+}
+
+
+class TQKError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{TQK_STATUS.get(code, code)}] {msg}")
+        self.code = code
+
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+
+_SIGS = {
+    "tqk_last_error": (ctypes.c_char_p, []),
+    "tqk_version": (_int, []),
+    "tqk_apply_matrix": (_int, [_vp, _i64, _int, _i32p, _int, _vp, _i64, _vp]),
+    "tqk_apply_controlled": (_int, [_vp, _i64, _int, _i32p, _int, _i32p, _int, _vp, _i64, _vp]),
+    "tqk_apply_mcx": (_int, [_vp, _i64, _int, _i32p, _int, _int, _int, _vp]),
+    "tqk_apply_phase": (_int, [_vp, _i64, _int, _i32p, _int, _vp, _i64, _vp]),
+    "tqk_apply_diagonal": (_int, [_vp, _i64, _int, _i32p, _int, _vp, _i64, _vp]),
+    "tqk_apply_swap": (_int, [_vp, _i64, _int, _i32p, _int, _int, _int, _vp]),
+    "tqk_reset_scratch_bytes": (_i64, [_i64, _int]),
+    "tqk_reset": (_int, [_vp, _i64, _int, _i32p, _int, _vp, _i64, _vp]),
+    "tqk_probs": (_int, [_vp, _i64, _int, _vp, _vp]),
+    "tqk_pauli_expval_scratch_bytes": (_i64, [_i64, _int, _int]),
+    "tqk_pauli_expval": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _i64, _vp]),
+    "tqk_pauli_apply_sum": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _vp]),
+    "tqk_adjoint_matrix": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
+    "tqk_adjoint_controlled": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
+    "tqk_adjoint_phase": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
+    "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+# Kernels launched by this process through the C ABI (bench.py reports the count of
+# its timed region).
+LAUNCHES = [0]
+
+
+def _count(k: int = 1) -> None:
+    LAUNCHES[0] += k
+
+
+def header_symbols() -> list:
+    """Function names declared in include/tqk.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"\b(tqk_[a-z0-9_]+)\s*\(", text)))
+
+
+def load() -> ctypes.CDLL:
+    """Load libtqk.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build the CUDA engine first "
+            "(python -c 'import __graft_entry__ as g; g.build()' or python -m torchquantum_gb300.build)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, launches: int = 1):
+    if rc == 0:
+        LAUNCHES[0] += launches
+    if rc != 0:
+        msg = load().tqk_last_error().decode(errors="replace")
+        raise TQKError(rc, msg)
+
+
+def _i32(vals: Sequence[int]):
+    arr = (ctypes.c_int32 * max(1, len(vals)))(*vals)
+    return arr
+
+
+def _u64(vals: Sequence[int]):
+    return (ctypes.c_uint64 * max(1, len(vals)))(*vals)
+
+
+def _stream(t: torch.Tensor) -> int:
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+# ------------------------------------------------------------------ gate application
+def apply_matrix(state, n, wires, mat, mat_batch):
+    _check(load().tqk_apply_matrix(state.data_ptr(), state.shape[0], n, _i32(wires), len(wires), mat.data_ptr(),
+                                   mat_batch, _stream(state)))
+
+
+def apply_controlled(state, n, controls, targets, mat, mat_batch):
+    _check(load().tqk_apply_controlled(state.data_ptr(), state.shape[0], n, _i32(controls), len(controls),
+                                       _i32(targets), len(targets), mat.data_ptr(), mat_batch, _stream(state)))
+
+
+def apply_mcx(state, n, controls, ctrl_val, target):
+    _check(load().tqk_apply_mcx(state.data_ptr(), state.shape[0], n, _i32(controls), len(controls), ctrl_val, target,
+                                _stream(state)))
+
+
+def apply_phase(state, n, wires, phase, phase_batch):
+    _check(load().tqk_apply_phase(state.data_ptr(), state.shape[0], n, _i32(wires), len(wires), phase.data_ptr(),
+                                  phase_batch, _stream(state)))
+
+
+def apply_diagonal(state, n, wires, diag, diag_batch):
+    _check(load().tqk_apply_diagonal(state.data_ptr(), state.shape[0], n, _i32(wires), len(wires), diag.data_ptr(),
+                                     diag_batch, _stream(state)))
+
+
+def apply_swap(state, n, controls, w0, w1):
+    _check(load().tqk_apply_swap(state.data_ptr(), state.shape[0], n, _i32(controls), len(controls), w0, w1,
+                                 _stream(state)))
+
+
+def reset(state, n, wires):
+    lib = load()
+    nbytes = lib.tqk_reset_scratch_bytes(state.shape[0], n)
+    scratch = torch.empty(max(8, nbytes), dtype=torch.uint8, device=state.device)
+    _check(lib.tqk_reset(state.data_ptr(), state.shape[0], n, _i32(wires), len(wires), scratch.data_ptr(), nbytes,
+                         _stream(state)), launches=2)
+
+
+# ------------------------------------------------------------------ measurement
+def probs(state, n):
+    out = torch.empty(state.shape[0], 1 << n, dtype=torch.float32, device=state.device)
+    _check(load().tqk_probs(state.data_ptr(), state.shape[0], n, out.data_ptr(), _stream(state)))
+    return out
+
+
+def expval_passes(xmasks) -> int:
+    """Passes tqk_pauli_expval makes: strings grouped by xmask, at most 8 per pass."""
+    counts = {}
+    for x in xmasks:
+        counts[x] = counts.get(x, 0) + 1
+    return sum((c + 7) // 8 for c in counts.values())
+
+
+def pauli_expval(state, n, xmasks, zmasks):
+    """[bsz, m] float64 expvals of m Pauli strings given by masks."""
+    lib = load()
+    m = len(xmasks)
+    bsz = state.shape[0]
+    out = torch.empty(bsz, m, dtype=torch.float64, device=state.device)
+    nbytes = lib.tqk_pauli_expval_scratch_bytes(bsz, n, m)
+    scratch = torch.empty(max(8, nbytes), dtype=torch.uint8, device=state.device)
+    _check(lib.tqk_pauli_expval(state.data_ptr(), bsz, n, _u64(xmasks), _u64(zmasks), m, out.data_ptr(),
+                                scratch.data_ptr(), nbytes, _stream(state)), launches=2 * expval_passes(xmasks))
+    return out
+
+
+def pauli_apply_sum(state, n, xmasks, zmasks, coef):
+    """sum_j coef[:, j] * P_j psi; coef float32 [bsz, m] (contiguous, same device)."""
+    out = torch.empty_like(state)
+    _check(load().tqk_pauli_apply_sum(state.data_ptr(), state.shape[0], n, _u64(xmasks), _u64(zmasks), len(xmasks),
+                                      coef.data_ptr(), out.data_ptr(), _stream(state)), launches=(len(xmasks) + 63) // 64)
+    return out
+
+
+# ------------------------------------------------------------------ adjoint
+def adjoint_matrix(psi, lam, n, wires, mat, mat_batch, grad):
+    _check(load().tqk_adjoint_matrix(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), len(wires),
+                                     mat.data_ptr(), mat_batch, _ptr(grad), _stream(psi)))
+
+
+def adjoint_controlled(psi, lam, n, controls, targets, mat, mat_batch, grad):
+    _check(load().tqk_adjoint_controlled(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(controls),
+                                         len(controls), _i32(targets), len(targets), mat.data_ptr(), mat_batch,
+                                         _ptr(grad), _stream(psi)))
+
+
+def adjoint_phase(psi, lam, n, wires, phase, phase_batch, grad):
+    _check(load().tqk_adjoint_phase(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), len(wires),
+                                    phase.data_ptr(), phase_batch, _ptr(grad), _stream(psi)))
+
+
+def adjoint_diagonal(psi, lam, n, wires, diag, diag_batch, grad):
+    _check(load().tqk_adjoint_diagonal(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), len(wires),
+                                       diag.data_ptr(), diag_batch, _ptr(grad), _stream(psi)))

@@ -1,0 +1,330 @@
+// measure.cu -- probabilities and Pauli-string expectation values.
+//
+// <psi|P|psi> for P = (x) sigma_w is evaluated from two bit masks over the in-row
+// index: xmask (X or Y on the wire) and zmask (Z or Y), with
+//   (P psi)_i = i^{#Y} (-1)^{popcount((i ^ x) & z)} psi_{i ^ x}.
+// Strings that share an xmask are evaluated in one pass over the state (each
+// amplitude pair (i, i^x) is read once for all of them).  Each thread accumulates in
+// float32, blocks reduce in float64 and write one partial per (row, block, string) to
+// scratch; a second kernel adds the partials in a fixed order, so results are
+// bitwise reproducible run to run.
+#include <vector>
+
+#include "common.cuh"
+
+namespace tqk {
+
+constexpr int kMaxStringsPerPass = 8;
+constexpr int kMaxApplyStrings = 64;
+
+// Blocks per row for the reduction passes: enough to fill the GPU, bounded so the
+// partials stay small.  Depends only on (bsz, n) so scratch size is a pure function.
+static int64_t reduce_blocks_per_row(int64_t bsz, int n) {
+  const int64_t amps = 1ll << n;
+  const int64_t want = (152 * 8 + bsz - 1) / bsz;        // ~8 blocks of 256 per SM overall
+  const int64_t cap = (amps / 4 + 255) / 256;            // at least one float4 pair per thread
+  int64_t b = want < cap ? want : cap;
+  return b < 1 ? 1 : b;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(float (&v)[NV], double* dst, int count) {
+  __shared__ double red[32][NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) red[warp][j] = (double)v[j];
+  }
+  __syncthreads();
+  if (warp == 0 && lane < count) {
+    double s = 0.0;
+    for (int w = 0; w < nwarps; ++w) s += red[w][lane];
+    dst[lane] = s;
+  }
+}
+
+struct ExpvalParams {
+  const float2* state;
+  int n;
+  uint64_t x;
+  int hbit;                       // highest set bit of x (x != 0)
+  int ns;                         // strings in this pass
+  uint64_t z[kMaxStringsPerPass];
+  int ny[kMaxStringsPerPass];     // number of Y mod 4
+  int col[kMaxStringsPerPass];    // output column of each string
+  int m;                          // total strings (partial row stride)
+  int64_t work;                   // work items per row
+  double* partial;                // [bsz][gridDim.x][m]
+};
+
+__device__ __forceinline__ float sgn_parity(uint64_t v) { return (__popcll(v) & 1) ? -1.f : 1.f; }
+
+__device__ __forceinline__ float pair_term(float2 a, float2 ap, uint64_t i, uint64_t ip, uint64_t z, int ny) {
+  // u = conj(a) * ap
+  const float ur = a.x * ap.x + a.y * ap.y;
+  const float ui = a.x * ap.y - a.y * ap.x;
+  const float sa = sgn_parity(ip & z), sb = sgn_parity(i & z);
+  switch (ny) {
+    case 0: return (sa + sb) * ur;
+    case 1: return (sb - sa) * ui;
+    case 2: return -(sa + sb) * ur;
+    default: return (sa - sb) * ui;
+  }
+}
+
+// x == 0: diagonal strings, contribution |psi_i|^2 * (-1)^{popcount(i & z)}
+__global__ void __launch_bounds__(256) k_expval_diag(const ExpvalParams p) {
+  const int64_t b = blockIdx.y;
+  const float2* row = p.state + (b << p.n);
+  float acc[kMaxStringsPerPass];
+#pragma unroll
+  for (int s = 0; s < kMaxStringsPerPass; ++s) acc[s] = 0.f;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < p.work; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = (uint64_t)t * 2;
+    const float4 v = ld4(row + i);
+    const float p0 = v.x * v.x + v.y * v.y, p1 = v.z * v.z + v.w * v.w;
+#pragma unroll
+    for (int s = 0; s < kMaxStringsPerPass; ++s)
+      if (s < p.ns) acc[s] += sgn_parity(i & p.z[s]) * p0 + sgn_parity((i + 1) & p.z[s]) * p1;
+  }
+  block_reduce_store<kMaxStringsPerPass>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
+}
+
+// x != 0: pairs (i, i^x) with bit hbit of i clear.
+template <bool LOWX>  // LOWX: x == 1 (the pair is one float4)
+__global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
+  const int64_t b = blockIdx.y;
+  const float2* row = p.state + (b << p.n);
+  float acc[kMaxStringsPerPass];
+#pragma unroll
+  for (int s = 0; s < kMaxStringsPerPass; ++s) acc[s] = 0.f;
+  const uint64_t lomask = (1ull << p.hbit) - 1ull;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < p.work; t += (int64_t)gridDim.x * blockDim.x) {
+    if (LOWX) {
+      const uint64_t i = (uint64_t)t * 2;  // i has bit 0 clear, partner i+1
+      const float4 v = ld4(row + i);
+#pragma unroll
+      for (int s = 0; s < kMaxStringsPerPass; ++s)
+        if (s < p.ns) acc[s] += pair_term(lo2(v), hi2(v), i, i + 1, p.z[s], p.ny[s]);
+    } else {
+      const uint64_t g = (uint64_t)t * 2;  // two consecutive groups: i, i+1 (hbit >= 1)
+      const uint64_t i = ((g >> p.hbit) << (p.hbit + 1)) | (g & lomask);
+      const uint64_t ip = i ^ p.x;
+      const float4 v = ld4(row + i);
+      const float4 w = ld4(row + (ip & ~1ull));
+      const bool sw = (p.x & 1ull) != 0;
+      const float2 a0 = lo2(v), a1 = hi2(v);
+      const float2 b0 = sw ? hi2(w) : lo2(w), b1 = sw ? lo2(w) : hi2(w);
+#pragma unroll
+      for (int s = 0; s < kMaxStringsPerPass; ++s)
+        if (s < p.ns)
+          acc[s] += pair_term(a0, b0, i, ip, p.z[s], p.ny[s]) + pair_term(a1, b1, i + 1, ip ^ 1ull, p.z[s], p.ny[s]);
+    }
+  }
+  block_reduce_store<kMaxStringsPerPass>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
+}
+
+// The two kernels above store block partials contiguously as [row][block][slot];
+// this kernel reduces them in block order into out[row*m + col].
+struct FinishCols {
+  int c[kMaxStringsPerPass];
+};
+
+__global__ void k_expval_finish(const double* partial, int64_t nblk, int ns, int slot_stride, const FinishCols cols,
+                                int m, double* out, int64_t bsz) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= bsz * ns) return;
+  const int64_t b = idx / ns;
+  const int s = (int)(idx % ns);
+  double acc = 0.0;
+  for (int64_t k = 0; k < nblk; ++k) acc += partial[(b * nblk + k) * slot_stride + s];
+  out[b * m + cols.c[s]] = acc;
+}
+
+struct ApplySumParams {
+  const float2* state;
+  float2* out;
+  int n;
+  int ns;
+  uint64_t x[kMaxApplyStrings], z[kMaxApplyStrings];
+  int ny[kMaxApplyStrings];
+  const float* coef;  // [bsz][m] + col0
+  int m, col0;
+  int accumulate;
+};
+
+__device__ __forceinline__ float2 ipow_mul(int ny, float2 v) {  // i^ny * v
+  switch (ny) {
+    case 0: return v;
+    case 1: return make_float2(-v.y, v.x);
+    case 2: return make_float2(-v.x, -v.y);
+    default: return make_float2(v.y, -v.x);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_pauli_apply_sum(const ApplySumParams p) {
+  const int64_t b = blockIdx.y;
+  const int64_t half = (1ll << p.n) >> 1;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= half) return;
+  const float2* row = p.state + (b << p.n);
+  float2* orow = p.out + (b << p.n);
+  const uint64_t i = (uint64_t)t * 2;
+  float2 o0 = make_float2(0.f, 0.f), o1 = make_float2(0.f, 0.f);
+  if (p.accumulate) {
+    const float4 v = ld4(orow + i);
+    o0 = lo2(v);
+    o1 = hi2(v);
+  }
+  for (int s = 0; s < p.ns; ++s) {
+    const float c = __ldg(p.coef + b * p.m + p.col0 + s);
+    const uint64_t x = p.x[s];
+    const float4 w = ld4(row + ((i ^ x) & ~1ull));
+    const bool sw = (x & 1ull) != 0;
+    const float2 src0 = sw ? hi2(w) : lo2(w), src1 = sw ? lo2(w) : hi2(w);
+    const float f0 = c * sgn_parity((i ^ x) & p.z[s]);
+    const float f1 = c * sgn_parity(((i + 1) ^ x) & p.z[s]);
+    const float2 v0 = ipow_mul(p.ny[s], src0), v1 = ipow_mul(p.ny[s], src1);
+    o0.x = fmaf(f0, v0.x, o0.x);
+    o0.y = fmaf(f0, v0.y, o0.y);
+    o1.x = fmaf(f1, v1.x, o1.x);
+    o1.y = fmaf(f1, v1.y, o1.y);
+  }
+  st4(orow + i, pack4(o0, o1));
+}
+
+__global__ void __launch_bounds__(256) k_probs(const float2* state, float* out, int64_t total_half) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total_half) return;
+  const float4 v = ld4(state + t * 2);
+  reinterpret_cast<float2*>(out)[t] = make_float2(v.x * v.x + v.y * v.y, v.z * v.z + v.w * v.w);
+}
+
+}  // namespace tqk
+
+using namespace tqk;
+
+extern "C" int tqk_probs(const void* state, int64_t bsz, int n, float* out, void* stream) {
+  int rc = check_state(state, bsz, n, "tqk_probs");
+  if (rc) return rc;
+  if (out == nullptr || (reinterpret_cast<uintptr_t>(out) & 7u))
+    return fail(TQK_BAD_POINTER, "tqk_probs: out must be non-null and 8-byte aligned");
+  const int64_t total_half = (bsz << n) >> 1;
+  const int threads = 256;
+  k_probs<<<(unsigned)((total_half + threads - 1) / threads), threads, 0, as_stream(stream)>>>(
+      static_cast<const float2*>(state), out, total_half);
+  return launch_status("tqk_probs");
+}
+
+extern "C" int64_t tqk_pauli_expval_scratch_bytes(int64_t bsz, int n, int m) {
+  // partials [bsz][nblk][kMaxStringsPerPass] per pass (passes reuse the region; the
+  // stream orders them)
+  const int64_t nblk = reduce_blocks_per_row(bsz, n);
+  (void)m;
+  return bsz * nblk * kMaxStringsPerPass * (int64_t)sizeof(double);
+}
+
+extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uint64_t* xmask, const uint64_t* zmask,
+                                int m, double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+  const char* what = "tqk_pauli_expval";
+  int rc = check_state(state, bsz, n, what);
+  if (rc) return rc;
+  if (m <= 0) return TQK_OK;
+  if (!xmask || !zmask || !out) return fail(TQK_BAD_POINTER, "%s: null mask/output pointer", what);
+  if (scratch == nullptr || scratch_bytes < tqk_pauli_expval_scratch_bytes(bsz, n, m))
+    return fail(TQK_SCRATCH_TOO_SMALL, "%s: scratch of %lld bytes needed", what,
+                (long long)tqk_pauli_expval_scratch_bytes(bsz, n, m));
+  const uint64_t lim = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+  for (int j = 0; j < m; ++j)
+    if ((xmask[j] | zmask[j]) & ~lim) return fail(TQK_BAD_WIRES, "%s: string %d has bits beyond n_wires=%d", what, j, n);
+  cudaStream_t st = as_stream(stream);
+  const int64_t nblk = reduce_blocks_per_row(bsz, n);
+  double* partial = static_cast<double*>(scratch);
+  std::vector<int> done(m, 0);
+  for (int j0 = 0; j0 < m; ++j0) {
+    if (done[j0]) continue;
+    ExpvalParams p;
+    p.state = static_cast<const float2*>(state);
+    p.n = n;
+    p.x = xmask[j0];
+    p.ns = 0;
+    p.m = kMaxStringsPerPass;
+    p.partial = partial;
+    FinishCols cols;
+    for (int j = j0; j < m && p.ns < kMaxStringsPerPass; ++j) {
+      if (done[j] || xmask[j] != p.x) continue;
+      done[j] = 1;
+      p.z[p.ns] = zmask[j];
+      p.ny[p.ns] = __builtin_popcountll(xmask[j] & zmask[j]) & 3;
+      cols.c[p.ns] = j;
+      p.col[p.ns] = j;
+      p.ns++;
+    }
+    for (int s = p.ns; s < kMaxStringsPerPass; ++s) {
+      p.z[s] = 0;
+      p.ny[s] = 0;
+      p.col[s] = 0;
+      cols.c[s] = 0;
+    }
+    dim3 grid((unsigned)nblk, (unsigned)bsz, 1);
+    const int threads = 256;
+    if (p.x == 0) {
+      p.work = (1ll << n) >> 1;
+      // block partials land at partial[(b*nblk + blk)*kMax + s]
+      k_expval_diag<<<grid, threads, 0, st>>>(p);
+    } else {
+      p.hbit = 63 - __builtin_clzll(p.x);
+      if (p.x == 1ull) {
+        p.work = (1ll << n) >> 1;
+        k_expval_pair<true><<<grid, threads, 0, st>>>(p);
+      } else {
+        p.work = (1ll << n) >> 2;
+        k_expval_pair<false><<<grid, threads, 0, st>>>(p);
+      }
+    }
+    if ((rc = launch_status(what))) return rc;
+    const int64_t nout = bsz * p.ns;
+    k_expval_finish<<<(unsigned)((nout + 127) / 128), 128, 0, st>>>(partial, nblk, p.ns, kMaxStringsPerPass,
+                                                                      cols, m, out, bsz);
+    if ((rc = launch_status(what))) return rc;
+  }
+  return TQK_OK;
+}
+
+extern "C" int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const uint64_t* xmask,
+                                   const uint64_t* zmask, int m, const float* coef, void* out, void* stream) {
+  const char* what = "tqk_pauli_apply_sum";
+  int rc = check_state(state, bsz, n, what);
+  if (rc) return rc;
+  if ((rc = check_state(out, bsz, n, what))) return rc;
+  if (m <= 0) return fail(TQK_BAD_SHAPE, "%s: need at least one string", what);
+  if (!xmask || !zmask || !coef) return fail(TQK_BAD_POINTER, "%s: null pointer", what);
+  cudaStream_t st = as_stream(stream);
+  const int64_t half = (1ll << n) >> 1;
+  for (int j0 = 0; j0 < m; j0 += kMaxApplyStrings) {
+    ApplySumParams p;
+    p.state = static_cast<const float2*>(state);
+    p.out = static_cast<float2*>(out);
+    p.n = n;
+    p.ns = (m - j0) < kMaxApplyStrings ? (m - j0) : kMaxApplyStrings;
+    for (int s = 0; s < p.ns; ++s) {
+      p.x[s] = xmask[j0 + s];
+      p.z[s] = zmask[j0 + s];
+      p.ny[s] = __builtin_popcountll(xmask[j0 + s] & zmask[j0 + s]) & 3;
+    }
+    p.coef = coef;
+    p.m = m;
+    p.col0 = j0;
+    p.accumulate = j0 > 0;
+    const int threads = threads_for(half);
+    dim3 grid((unsigned)((half + threads - 1) / threads), (unsigned)bsz, 1);
+    k_pauli_apply_sum<<<grid, threads, 0, st>>>(p);
+    if ((rc = launch_status(what))) return rc;
+  }
+  return TQK_OK;
+}

@@ -1,0 +1,187 @@
+"""QuantumDevice: the statevector container, backed by one engine-owned device buffer.
+
+Mirrors upstream ``torchquantum/device/devices.py:37-136``: same constructor, same
+``states`` shape ``[bsz, 2, ..., 2]`` (complex64, |0...0> initially, wire 0 the most
+significant bit), ``get_states_1d``, ``set_states``, ``clone_states``,
+``reset_states``, ``reset_identity_states``, ``reset_all_eq_states``, op history and
+every functional gate bound as a method.  Differences by design:
+
+* the state lives in one contiguous ``[bsz, 2^n]`` buffer updated in place by the
+  CUDA kernels (upstream rebuilds a permuted view per gate);
+* reading ``states`` returns a tensor connected to autograd through
+  ``engine.CircuitFunction`` (adjoint-method backward) instead of a per-gate graph;
+* CUDA devices only: there is no CPU path.
+"""
+from __future__ import annotations
+
+from typing import List, Optional, Union
+
+import numpy as np
+import torch
+import torch.nn as nn
+
+from . import engine
+
+__all__ = ["QuantumDevice"]
+
+
+class QuantumDevice(nn.Module):
+    def __init__(self, n_wires: int, device_name: str = "default", bsz: int = 1,
+                 device: Union[torch.device, str] = "cuda", record_op: bool = False):
+        super().__init__()
+        dev = torch.device(device)
+        if dev.type != "cuda":
+            raise RuntimeError(
+                f"torchquantum_gb300.QuantumDevice runs on CUDA devices only (got device={device!r})")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.n_wires = int(n_wires)
+        self.device_name = device_name
+        self.bsz = int(bsz)
+        self.device = dev
+        self.record_op = record_op
+        self.op_history: List[dict] = []
+        self.method = "plain"          # "plain" | "fused" (see fusion.py)
+        self.fuse_wires = 5
+        self._tape: List[engine.TapeOp] = []
+        self._pending: List[engine.TapeOp] = []   # fused method: recorded, not yet applied
+        self._init: Optional[torch.Tensor] = None
+        self._exported = False
+        self._out: Optional[torch.Tensor] = None
+        self._buf = self._zero_state(self.bsz)
+
+    # ------------------------------------------------------------------ buffers
+    def _zero_state(self, bsz: int) -> torch.Tensor:
+        s = torch.zeros(bsz, 1 << self.n_wires, dtype=torch.complex64, device=self.device)
+        s[:, 0] = 1
+        return s
+
+    def _anchor(self, states: Optional[torch.Tensor], bsz: Optional[int] = None):
+        """Start a new tape from ``states`` ([bsz, 2^n]) or from |0..0>."""
+        self._tape = []
+        self._pending = []
+        self._out = None
+        self._exported = False
+        if states is None:
+            self._init = None
+            self._buf = self._zero_state(bsz if bsz is not None else self.bsz)
+        else:
+            st = states.reshape(states.shape[0], 1 << self.n_wires)
+            if st.device != self.device:
+                st = st.to(self.device)
+            st = st.to(torch.complex64)
+            self._init = st if st.requires_grad else None
+            self._buf = st.detach().clone().contiguous()
+        self.bsz = int(self._buf.shape[0])
+
+    @property
+    def state(self) -> torch.Tensor:
+        """The |0...0> single state [2]*n (upstream registers it as a buffer)."""
+        s = torch.zeros(1 << self.n_wires, dtype=torch.complex64, device=self.device)
+        s[0] = 1
+        return s.reshape([2] * self.n_wires)
+
+    # ------------------------------------------------------------------ gate path
+    def _apply(self, op: engine.TapeOp) -> None:
+        if op.operand is not None and op.batch not in (1, self.bsz):
+            raise ValueError(f"gate operand batch {op.batch} does not match QuantumDevice bsz {self.bsz}")
+        if self.method == "fused":
+            self._pending.append(op)
+            self._out = None
+            return
+        if self._exported:  # the buffer is referenced by an exported tensor: copy on write
+            self._buf = self._buf.clone()
+            self._exported = False
+        engine.apply_op(self._buf, self.n_wires, op)
+        self._tape.append(op)
+        self._out = None
+
+    def _flush(self) -> None:
+        if self._pending:
+            from . import fusion
+
+            ops, self._pending = self._pending, []
+            if self._exported:
+                self._buf = self._buf.clone()
+                self._exported = False
+            self._tape.extend(fusion.apply_fused(self, ops))
+            self._out = None
+
+    def _output(self) -> torch.Tensor:
+        """[bsz, 2^n] state as an autograd-connected tensor (cached until the next gate)."""
+        self._flush()
+        if self._out is not None:
+            return self._out
+        sources = [op.source for op in self._tape if op.needs_grad]
+        needs = bool(sources) or (self._init is not None and self._init.requires_grad)
+        if needs and torch.is_grad_enabled():
+            out = engine.CircuitFunction.apply(self._buf, self.n_wires, list(self._tape), self._init, *sources)
+        else:
+            out = self._buf
+        self._exported = True
+        self._out = out
+        return out
+
+    def reset_wires(self, wires: List[int]) -> None:
+        """Project ``wires`` onto |0> and renormalise (functional/reset.py); anchors the tape."""
+        from . import _lib
+
+        self._flush()
+        cur = self._output().detach().clone()
+        _lib.reset(cur, self.n_wires, wires)
+        self._anchor(cur)
+
+    # ------------------------------------------------------------------ upstream API
+    @property
+    def states(self) -> torch.Tensor:
+        return self._output().view([self.bsz] + [2] * self.n_wires)
+
+    @states.setter
+    def states(self, value: torch.Tensor) -> None:
+        self._anchor(value)
+
+    def reset_op_history(self):
+        self.op_history = []
+
+    def clone_states(self, existing_states: torch.Tensor):
+        self._anchor(existing_states.clone())
+
+    def set_states(self, states: torch.Tensor):
+        self._anchor(states)
+
+    def reset_states(self, bsz: int):
+        self._anchor(None, bsz)
+
+    def reset_identity_states(self):
+        """Batch of 2^n basis states (one per row); useful for unitary extraction."""
+        dim = 1 << self.n_wires
+        self._anchor(torch.eye(dim, dtype=torch.complex64, device=self.device))
+
+    def reset_all_eq_states(self, bsz: int):
+        energy = np.sqrt(1 / (2 ** self.n_wires) / 2)
+        s = torch.full((bsz, 1 << self.n_wires), complex(energy, energy), dtype=torch.complex64, device=self.device)
+        self._anchor(s)
+
+    def get_states_1d(self) -> torch.Tensor:
+        return self._output()
+
+    def get_state_1d(self) -> torch.Tensor:
+        return self.state.reshape(1 << self.n_wires)
+
+    @property
+    def name(self):
+        return self.__class__.__name__
+
+    def __repr__(self):
+        return (f" class: {self.name} \n device name: {self.device_name} \n number of qubits: {self.n_wires} \n"
+                f" batch size: {self.bsz} \n current computing device: {self.device} \n"
+                f" recording op history: {self.record_op} \n method: {self.method}")
+
+
+def _bind_gate_methods():
+    from .functional import func_name_dict, func_name_dict_collect
+
+    for fname, fn in func_name_dict.items():
+        setattr(QuantumDevice, fname, fn)
+    for fname, fn in func_name_dict_collect.items():
+        setattr(QuantumDevice, fname, fn)

@@ -1,0 +1,47 @@
+"""Encoders (upstream ``torchquantum/encoding/encodings.py``).
+
+``GeneralEncoder`` (``encodings.py:50-102``) applies ``func_name_dict[f](qdev, wires,
+params=x[:, input_idx])`` per entry of its ``func_list``; the per-sample parameters
+make every batch row's matrix different, which the engine handles with per-row
+operands (``mat_batch == bsz``).
+"""
+from __future__ import annotations
+
+from .functional import func_name_dict
+from .module import QuantumModule, static_support
+from .operators import op_name_dict
+
+__all__ = ["Encoder", "GeneralEncoder", "StateEncoder"]
+
+
+class Encoder(QuantumModule):
+    def __init__(self):
+        super().__init__()
+        self.q_device = None
+
+    def forward(self, qdev, x):
+        raise NotImplementedError
+
+
+class GeneralEncoder(Encoder):
+    def __init__(self, func_list):
+        super().__init__()
+        self.func_list = func_list
+
+    @static_support
+    def forward(self, qdev, x):
+        for info in self.func_list:
+            params = x[:, info["input_idx"]] if op_name_dict[info["func"]].num_params > 0 else None
+            func_name_dict[info["func"]](qdev, wires=info["wires"], params=params)
+
+
+class StateEncoder(Encoder):
+    """Load a (zero-padded, normalised) state from ``x`` (upstream encodings.py StateEncoder)."""
+
+    def forward(self, qdev, x):
+        import torch
+
+        pad = (1 << qdev.n_wires) - x.shape[1]
+        state = torch.cat([x, torch.zeros(x.shape[0], pad, device=x.device, dtype=x.dtype)], dim=-1)
+        state = state / state.abs().pow(2).sum(-1, keepdim=True).sqrt()
+        qdev.set_states(state.to(torch.complex64))

@@ -1,0 +1,157 @@
+"""Gate tape, kernel dispatch and the adjoint-method autograd Function.
+
+A ``QuantumDevice`` owns one contiguous ``[bsz, 2^n]`` complex64 device buffer and a
+tape of ``TapeOp`` records.  Gates are applied to the buffer in place by the CUDA
+kernels of ``libtqk.so`` as they are called (the plain method).  Nothing per gate is
+kept for autograd except the small gate operand (a 2x2 / 4x4 matrix, a phase or a
+diagonal); when the state is read by a measurement, ``CircuitFunction`` exposes it
+to torch autograd as a function of every operand that requires grad.  Its backward
+is the adjoint method: starting from the final state psi and the incoming cotangent
+lam it walks the tape in reverse, uncomputing psi <- U^H psi and lam <- U^H lam and
+accumulating each operand's cotangent ``sum lam_after conj(psi_before)^T`` in float64
+-- two state buffers instead of one saved state per gate.  Torch autograd then
+carries the operand cotangents through the differentiable matrix builders
+(``gates.py``) to the gate parameters.
+
+Replaces the per-gate ``torch.bmm``/``permute`` graph that upstream
+``apply_unitary_bmm`` records (``torchquantum/functional/gate_wrapper.py:96-140``).
+"""
+from __future__ import annotations
+
+from typing import List, Optional
+
+import torch
+
+from . import _lib
+
+KIND_DENSE, KIND_CTRL, KIND_X, KIND_PHASE, KIND_DIAG, KIND_SWAP = "dense", "ctrl", "x", "phase", "diag", "swap"
+
+
+class TapeOp:
+    """One applied gate.
+
+    ``operand`` is the detached complex64 tensor the kernel reads (``[B, D, D]``
+    matrix, ``[B]`` phase or ``[B, 2^k]`` diagonal, ``B`` in {1, bsz});
+    ``source`` is the autograd-tracked tensor it was taken from (or None).
+    """
+
+    __slots__ = ("kind", "wires", "controls", "targets", "ctrl_val", "operand", "source", "batch")
+
+    def __init__(self, kind, wires, controls=(), targets=(), ctrl_val=1, operand=None, source=None):
+        self.kind = kind
+        self.wires = list(wires)
+        self.controls = list(controls)
+        self.targets = list(targets)
+        self.ctrl_val = int(ctrl_val)
+        self.operand = operand
+        self.source = source
+        self.batch = 0 if operand is None else int(operand.shape[0])
+
+    @property
+    def needs_grad(self) -> bool:
+        return self.source is not None and self.source.requires_grad
+
+    def grad_numel(self) -> int:
+        """float64 values of this op's operand cotangent (complex128 interleaved)."""
+        if self.operand is None:
+            return 0
+        return 2 * self.operand.numel()
+
+    def __repr__(self):
+        return f"TapeOp({self.kind}, wires={self.wires}, batch={self.batch})"
+
+
+def apply_op(buf: torch.Tensor, n: int, op: TapeOp) -> None:
+    """Launch the forward kernel of ``op`` on ``buf`` (in place, current stream)."""
+    k = op.kind
+    if k == KIND_DENSE:
+        _lib.apply_matrix(buf, n, op.wires, op.operand, op.batch)
+    elif k == KIND_CTRL:
+        _lib.apply_controlled(buf, n, op.controls, op.targets, op.operand, op.batch)
+    elif k == KIND_X:
+        _lib.apply_mcx(buf, n, op.controls, op.ctrl_val, op.targets[0])
+    elif k == KIND_PHASE:
+        _lib.apply_phase(buf, n, op.wires, op.operand, op.batch)
+    elif k == KIND_DIAG:
+        _lib.apply_diagonal(buf, n, op.wires, op.operand, op.batch)
+    elif k == KIND_SWAP:
+        _lib.apply_swap(buf, n, op.controls, op.targets[0], op.targets[1])
+    else:
+        raise ValueError(f"unknown op kind {k}")
+
+
+def _conj_t(m: torch.Tensor) -> torch.Tensor:
+    return m.conj().transpose(-1, -2).contiguous()
+
+
+def adjoint_op(psi: torch.Tensor, lam: torch.Tensor, n: int, op: TapeOp, grad: Optional[torch.Tensor]) -> None:
+    """One reverse step: psi <- U^H psi, lam <- U^H lam, grad += lam conj(psi_before)^T."""
+    k = op.kind
+    if k == KIND_DENSE:
+        if len(op.wires) <= 2:
+            _lib.adjoint_matrix(psi, lam, n, op.wires, op.operand, op.batch, grad)
+        else:
+            if grad is not None:
+                raise NotImplementedError("gradient of a dense gate on more than 2 wires is not supported yet")
+            uh = _conj_t(op.operand)
+            _lib.apply_matrix(psi, n, op.wires, uh, op.batch)
+            _lib.apply_matrix(lam, n, op.wires, uh, op.batch)
+    elif k == KIND_CTRL:
+        _lib.adjoint_controlled(psi, lam, n, op.controls, op.targets, op.operand, op.batch, grad)
+    elif k == KIND_X:
+        _lib.apply_mcx(psi, n, op.controls, op.ctrl_val, op.targets[0])
+        _lib.apply_mcx(lam, n, op.controls, op.ctrl_val, op.targets[0])
+    elif k == KIND_PHASE:
+        _lib.adjoint_phase(psi, lam, n, op.wires, op.operand, op.batch, grad)
+    elif k == KIND_DIAG:
+        _lib.adjoint_diagonal(psi, lam, n, op.wires, op.operand, op.batch, grad)
+    elif k == KIND_SWAP:
+        _lib.apply_swap(psi, n, op.controls, op.targets[0], op.targets[1])
+        _lib.apply_swap(lam, n, op.controls, op.targets[0], op.targets[1])
+    else:
+        raise ValueError(f"unknown op kind {k}")
+
+
+class CircuitFunction(torch.autograd.Function):
+    """final_state = circuit(init_state, operands...) with an adjoint-method backward.
+
+    forward receives the already-computed final state (the device buffer) and returns
+    it; backward walks ``tape`` in reverse.  Inputs: ``init`` (the anchored initial
+    state, possibly requiring grad) followed by the operand sources that require grad.
+    """
+
+    @staticmethod
+    def forward(ctx, final: torch.Tensor, n: int, tape: List[TapeOp], init: Optional[torch.Tensor], *sources):
+        ctx.n = n
+        ctx.tape = tape
+        ctx.has_init = init is not None
+        ctx.save_for_backward(final)
+        return final
+
+    @staticmethod
+    def backward(ctx, grad_out: torch.Tensor):
+        (final,) = ctx.saved_tensors
+        n, tape = ctx.n, ctx.tape
+        psi = final.detach().clone()
+        lam = grad_out.detach().to(torch.complex64).contiguous().clone()
+        grad_ops = [op for op in tape if op.needs_grad]
+        total = sum(op.grad_numel() for op in grad_ops)
+        gbuf = torch.zeros(max(1, total), dtype=torch.float64, device=psi.device)
+        offsets = {}
+        off = 0
+        for op in grad_ops:
+            offsets[id(op)] = off
+            off += op.grad_numel()
+        for op in reversed(tape):
+            g = None
+            if op.needs_grad:
+                o = offsets[id(op)]
+                g = gbuf[o:o + op.grad_numel()]
+            adjoint_op(psi, lam, n, op, g)
+        grads = []
+        for op in grad_ops:
+            o = offsets[id(op)]
+            g = torch.view_as_complex(gbuf[o:o + op.grad_numel()].view(-1, 2)).view(op.operand.shape)
+            grads.append(g.to(op.source.dtype))
+        g_init = lam if ctx.has_init else None
+        return (None, None, None, g_init, *grads)
