@@ -106,16 +106,19 @@ int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const uint64_t* x
 
 /* ---------------------------------------------------------------- adjoint backward
  * One reverse step of the adjoint method for a gate applied with the matching forward
- * entry point above: psi <- U^H psi, lam <- U^H lam, and (if grad != NULL)
+ * entry point above: psi <- U^H psi (or psi <- uncompute psi when `uncompute` is not
+ * NULL: the exact inverse, for gates that are not unitary such as upstream's cu2),
+ * lam <- U^H lam, and (if grad != NULL)
  * grad[g] += sum over the gate's amplitude groups of lam_after * conj(psi_before)^T,
  * accumulated in float64 (complex128 interleaved), g = batch row if the operand is
  * per-row else 0.  Replaces the autograd graph of torch.bmm/permute recorded by
  * apply_unitary_bmm (gate_wrapper.py:127-138).  grad must be zeroed by the caller. */
 int tqk_adjoint_matrix(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
-                       const void* mat, int64_t mat_batch, double* grad, void* stream);
+                       const void* mat, int64_t mat_batch, const void* uncompute, double* grad,
+                       void* stream);
 int tqk_adjoint_controlled(void* psi, void* lam, int64_t bsz, int n, const int32_t* controls,
                            int nc, const int32_t* targets, int kt, const void* mat,
-                           int64_t mat_batch, double* grad, void* stream);
+                           int64_t mat_batch, const void* uncompute, double* grad, void* stream);
 int tqk_adjoint_phase(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
                       const void* phase, int64_t phase_batch, double* grad, void* stream);
 int tqk_adjoint_diagonal(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,

@@ -51,8 +51,8 @@ _SIGS = {
     "tqk_pauli_expval_scratch_bytes": (_i64, [_i64, _int, _int]),
     "tqk_pauli_expval": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _i64, _vp]),
     "tqk_pauli_apply_sum": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _vp]),
-    "tqk_adjoint_matrix": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
-    "tqk_adjoint_controlled": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
+    "tqk_adjoint_matrix": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp, _vp]),
+    "tqk_adjoint_controlled": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _i32p, _int, _vp, _i64, _vp, _vp, _vp]),
     "tqk_adjoint_phase": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
 }
@@ -194,15 +194,15 @@ def pauli_apply_sum(state, n, xmasks, zmasks, coef):
 
 
 # ------------------------------------------------------------------ adjoint
-def adjoint_matrix(psi, lam, n, wires, mat, mat_batch, grad):
+def adjoint_matrix(psi, lam, n, wires, mat, mat_batch, grad, uncompute=None):
     _check(load().tqk_adjoint_matrix(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), len(wires),
-                                     mat.data_ptr(), mat_batch, _ptr(grad), _stream(psi)))
+                                     mat.data_ptr(), mat_batch, _ptr(uncompute), _ptr(grad), _stream(psi)))
 
 
-def adjoint_controlled(psi, lam, n, controls, targets, mat, mat_batch, grad):
+def adjoint_controlled(psi, lam, n, controls, targets, mat, mat_batch, grad, uncompute=None):
     _check(load().tqk_adjoint_controlled(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(controls),
                                          len(controls), _i32(targets), len(targets), mat.data_ptr(), mat_batch,
-                                         _ptr(grad), _stream(psi)))
+                                         _ptr(uncompute), _ptr(grad), _stream(psi)))
 
 
 def adjoint_phase(psi, lam, n, wires, phase, phase_batch, grad):

@@ -31,6 +31,7 @@ struct DenseParams {
   int pair[D];            // MODE_LOW: index r' with off[r'] = off[r] | 1, or -1
   const float2* mat;      // [batch][D][D]
   int64_t mat_stride;     // D*D if per row else 0
+  const float2* uinv;     // adjoint: exact inverse used to uncompute psi (non-unitary gates), or null
   double* grad;           // adjoint: [batch][D][D] complex128, or null
   int64_t grad_stride;    // 2*D*D if per row else 0
 };
@@ -143,8 +144,9 @@ __global__ void __launch_bounds__(256) k_dense(const DenseParams<D> p) {
   store_groups<D, MODE>(row, p, g0, two, y);
 }
 
-// Adjoint step: psi <- U^H psi, lam <- U^H lam, grad += lam_after (x) conj(psi_before).
-template <int D, int MODE, bool GRAD>
+// Adjoint step: psi <- U^H psi (or U^-1 psi when INV), lam <- U^H lam,
+// grad += lam_after (x) conj(psi_before).
+template <int D, int MODE, bool GRAD, bool INV>
 __global__ void __launch_bounds__(256) k_dense_adj(const DenseParams<D> p) {
   const int64_t b = blockIdx.y;
   const int64_t pairs = (p.groups + 1) >> 1;
@@ -166,11 +168,17 @@ __global__ void __launch_bounds__(256) k_dense_adj(const DenseParams<D> p) {
       for (int r = 0; r < D; ++r) a[j][r] = l[j][r] = make_float2(0.f, 0.f);
     load_groups<D, MODE>(prow, p, g0, two, a);
     load_groups<D, MODE>(lrow, p, g0, two, l);
+    if (INV) {
+      float2 Mi[D][D];
+      load_mat<D>(p.uinv + b * p.mat_stride, Mi);
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      matvec_h<D>(M, a[j], y[j]);
-      matvec_h<D>(M, l[j], z[j]);
+      for (int j = 0; j < 2; ++j) matvec<D>(Mi, a[j], y[j]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) matvec_h<D>(M, a[j], y[j]);
     }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) matvec_h<D>(M, l[j], z[j]);
     if (GRAD) {
 #pragma unroll
       for (int j = 0; j < 2; ++j)
@@ -190,15 +198,23 @@ __global__ void __launch_bounds__(256) k_dense_adj(const DenseParams<D> p) {
 }
 
 // ------------------------------------------------------------------ generic dense k
+// One block stages gpb groups (2^k amplitudes each) in shared memory, applies the
+// matrix (staged in shared memory too when 2^k <= 64) and writes back.  Thread idx
+// maps to (group gi = idx % gpb, row r = idx / gpb), so a warp shares its matrix row.
 struct DenseKParams {
   float2* state;
+  float2* lam;                      // adjoint only
   int n, k;
   int64_t groups;
   BitInsert ins;
-  int tbits[TQK_MAX_DENSE_WIRES];  // bit of matrix-index bit j (j=0 is the MSB of r)
+  int tbits[TQK_MAX_DENSE_WIRES];   // bit of matrix-index bit j (j=0 is the MSB of r)
   const float2* mat;
+  const float2* uinv;               // adjoint: exact inverse for psi, or null (use U^H)
   int64_t mat_stride;
+  double* grad;                     // adjoint: [batch][D][D] complex128 or null
+  int64_t grad_stride;
   int gpb;                          // groups per block
+  int mat_in_smem;
 };
 
 __device__ __forceinline__ uint64_t dk_offset(const DenseKParams& p, int r) {
@@ -208,37 +224,115 @@ __device__ __forceinline__ uint64_t dk_offset(const DenseKParams& p, int r) {
   return off;
 }
 
+constexpr int kDkMaxOut = 16;
+
+// smem: [mat D*D if staged][tile gpb*(D+1)] (tile rows padded by one amplitude)
 __global__ void __launch_bounds__(256) k_dense_k(const DenseKParams p) {
   extern __shared__ float2 sm[];
   const int D = 1 << p.k;
+  const int ld = D + 1;
   const int64_t b = blockIdx.y;
   const int64_t gbase = (int64_t)blockIdx.x * p.gpb;
   float2* row = p.state + (b << p.n);
-  const float2* M = p.mat + b * p.mat_stride;
+  const float2* Mg = p.mat + b * p.mat_stride;
+  float2* Ms = sm;
+  float2* tile = sm + (p.mat_in_smem ? D * D : 0);
+  if (p.mat_in_smem)
+    for (int i = threadIdx.x; i < D * D; i += blockDim.x) Ms[i] = Mg[i];
+  const float2* M = p.mat_in_smem ? Ms : Mg;
   const int total = p.gpb * D;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     const int gi = idx % p.gpb, r = idx / p.gpb;
     const int64_t g = gbase + gi;
-    if (g < p.groups) sm[gi * D + r] = row[insert_zero_bits((uint64_t)g, p.ins) + dk_offset(p, r)];
+    if (g < p.groups) tile[gi * ld + r] = row[insert_zero_bits((uint64_t)g, p.ins) + dk_offset(p, r)];
   }
   __syncthreads();
-  // each thread computes up to 16 outputs into registers, writes after a barrier
-  float2 out[16];
+  float2 out[kDkMaxOut];
   int cnt = 0;
-  for (int idx = threadIdx.x; idx < total && cnt < 16; idx += blockDim.x, ++cnt) {
+  for (int idx = threadIdx.x; idx < total && cnt < kDkMaxOut; idx += blockDim.x, ++cnt) {
     const int gi = idx % p.gpb, r = idx / p.gpb;
     float2 acc = make_float2(0.f, 0.f);
     const float2* mr = M + (int64_t)r * D;
-    const float2* s = sm + gi * D;
-    for (int c = 0; c < D; ++c) acc = cfma(__ldg(mr + c), s[c], acc);
+    const float2* s = tile + gi * ld;
+    for (int c = 0; c < D; ++c) acc = cfma(mr[c], s[c], acc);
     out[cnt] = acc;
   }
   __syncthreads();
   cnt = 0;
-  for (int idx = threadIdx.x; idx < total && cnt < 16; idx += blockDim.x, ++cnt) {
+  for (int idx = threadIdx.x; idx < total && cnt < kDkMaxOut; idx += blockDim.x, ++cnt) {
     const int gi = idx % p.gpb, r = idx / p.gpb;
     const int64_t g = gbase + gi;
     if (g < p.groups) row[insert_zero_bits((uint64_t)g, p.ins) + dk_offset(p, r)] = out[cnt];
+  }
+}
+
+// Adjoint of a dense k-wire gate: psi <- U^H psi (or U^-1 psi), lam <- U^H lam,
+// grad[r][c] += sum over groups of lam_after[r] * conj(psi_before[c]).
+// smem: [psi tile gpb*(D+1)][lam tile gpb*(D+1)]
+__global__ void __launch_bounds__(256) k_dense_k_adj(const DenseKParams p) {
+  extern __shared__ float2 sm[];
+  const int D = 1 << p.k;
+  const int ld = D + 1;
+  const int64_t b = blockIdx.y;
+  const int64_t gbase = (int64_t)blockIdx.x * p.gpb;
+  float2* prow = p.state + (b << p.n);
+  float2* lrow = p.lam + (b << p.n);
+  const float2* M = p.mat + b * p.mat_stride;
+  const float2* Mi = p.uinv ? p.uinv + b * p.mat_stride : nullptr;
+  float2* ps = sm;
+  float2* ls = sm + p.gpb * ld;
+  const int total = p.gpb * D;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int gi = idx % p.gpb, r = idx / p.gpb;
+    const int64_t g = gbase + gi;
+    float2 a = make_float2(0.f, 0.f), l = make_float2(0.f, 0.f);
+    if (g < p.groups) {
+      const uint64_t ad = insert_zero_bits((uint64_t)g, p.ins) + dk_offset(p, r);
+      a = prow[ad];
+      l = lrow[ad];
+    }
+    ps[gi * ld + r] = a;
+    ls[gi * ld + r] = l;
+  }
+  __syncthreads();
+  float2 po[kDkMaxOut], lo[kDkMaxOut];
+  int cnt = 0;
+  for (int idx = threadIdx.x; idx < total && cnt < kDkMaxOut; idx += blockDim.x, ++cnt) {
+    const int gi = idx % p.gpb, r = idx / p.gpb;
+    float2 ap = make_float2(0.f, 0.f), al = make_float2(0.f, 0.f);
+    const float2* s = ps + gi * ld;
+    const float2* t = ls + gi * ld;
+    for (int c = 0; c < D; ++c) {
+      const float2 m = __ldg(M + (int64_t)c * D + r);  // (U^H)[r][c] = conj(U[c][r])
+      al = cfma_conj(m, t[c], al);
+      if (Mi) ap = cfma(__ldg(Mi + (int64_t)r * D + c), s[c], ap);
+      else ap = cfma_conj(m, s[c], ap);
+    }
+    po[cnt] = ap;
+    lo[cnt] = al;
+  }
+  __syncthreads();
+  // psi_before into the psi tile (lam tile keeps lam_after for the gradient)
+  cnt = 0;
+  for (int idx = threadIdx.x; idx < total && cnt < kDkMaxOut; idx += blockDim.x, ++cnt) {
+    const int gi = idx % p.gpb, r = idx / p.gpb;
+    ps[gi * ld + r] = po[cnt];
+    const int64_t g = gbase + gi;
+    if (g < p.groups) {
+      const uint64_t ad = insert_zero_bits((uint64_t)g, p.ins) + dk_offset(p, r);
+      prow[ad] = po[cnt];
+      lrow[ad] = lo[cnt];
+    }
+  }
+  if (p.grad == nullptr) return;
+  __syncthreads();
+  double* gd = p.grad + b * p.grad_stride;
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+    const int r = e / D, c = e % D;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int gi = 0; gi < p.gpb; ++gi) acc = cfma_bconj(ls[gi * ld + r], ps[gi * ld + c], acc);
+    atomicAdd(gd + 2 * e, (double)acc.x);
+    atomicAdd(gd + 2 * e + 1, (double)acc.y);
   }
 }
 
@@ -522,9 +616,22 @@ int fill_dense(DenseParams<D>& p, const GateSetup& s, int& mode) {
   return TQK_OK;
 }
 
+template <int D, bool INV>
+void launch_dense_adj(const DenseParams<D>& p, int mode, bool grad, dim3 grid, int threads, cudaStream_t st) {
+  if (grad) {
+    if (mode == MODE_VEC) k_dense_adj<D, MODE_VEC, true, INV><<<grid, threads, 0, st>>>(p);
+    else if (mode == MODE_LOW) k_dense_adj<D, MODE_LOW, true, INV><<<grid, threads, 0, st>>>(p);
+    else k_dense_adj<D, MODE_SCL, true, INV><<<grid, threads, 0, st>>>(p);
+  } else {
+    if (mode == MODE_VEC) k_dense_adj<D, MODE_VEC, false, INV><<<grid, threads, 0, st>>>(p);
+    else if (mode == MODE_LOW) k_dense_adj<D, MODE_LOW, false, INV><<<grid, threads, 0, st>>>(p);
+    else k_dense_adj<D, MODE_SCL, false, INV><<<grid, threads, 0, st>>>(p);
+  }
+}
+
 template <int D>
 int launch_dense(const GateSetup& s, float2* state, float2* lam, const float2* mat, int64_t mat_batch,
-                 double* grad, bool adjoint, cudaStream_t st) {
+                 const float2* uinv, double* grad, bool adjoint, cudaStream_t st) {
   DenseParams<D> p;
   int mode;
   fill_dense<D>(p, s, mode);
@@ -532,6 +639,7 @@ int launch_dense(const GateSetup& s, float2* state, float2* lam, const float2* m
   p.lam = lam;
   p.mat = mat;
   p.mat_stride = mat_batch > 1 ? D * D : 0;
+  p.uinv = uinv;
   p.grad = grad;
   p.grad_stride = mat_batch > 1 ? 2 * D * D : 0;
   const int64_t work = (p.groups + 1) >> 1;
@@ -541,21 +649,19 @@ int launch_dense(const GateSetup& s, float2* state, float2* lam, const float2* m
     if (mode == MODE_VEC) k_dense<D, MODE_VEC><<<grid, threads, 0, st>>>(p);
     else if (mode == MODE_LOW) k_dense<D, MODE_LOW><<<grid, threads, 0, st>>>(p);
     else k_dense<D, MODE_SCL><<<grid, threads, 0, st>>>(p);
-  } else if (grad) {
-    if (mode == MODE_VEC) k_dense_adj<D, MODE_VEC, true><<<grid, threads, 0, st>>>(p);
-    else if (mode == MODE_LOW) k_dense_adj<D, MODE_LOW, true><<<grid, threads, 0, st>>>(p);
-    else k_dense_adj<D, MODE_SCL, true><<<grid, threads, 0, st>>>(p);
+  } else if (uinv) {
+    launch_dense_adj<D, true>(p, mode, grad != nullptr, grid, threads, st);
   } else {
-    if (mode == MODE_VEC) k_dense_adj<D, MODE_VEC, false><<<grid, threads, 0, st>>>(p);
-    else if (mode == MODE_LOW) k_dense_adj<D, MODE_LOW, false><<<grid, threads, 0, st>>>(p);
-    else k_dense_adj<D, MODE_SCL, false><<<grid, threads, 0, st>>>(p);
+    launch_dense_adj<D, false>(p, mode, grad != nullptr, grid, threads, st);
   }
   return launch_status(adjoint ? "adjoint dense gate" : "dense gate");
 }
 
-int launch_dense_k(const GateSetup& s, float2* state, const float2* mat, int64_t mat_batch, cudaStream_t st) {
+int launch_dense_k(const GateSetup& s, float2* state, float2* lam, const float2* mat, const float2* uinv,
+                   int64_t mat_batch, double* grad, bool adjoint, cudaStream_t st) {
   DenseKParams p;
   p.state = state;
+  p.lam = lam;
   p.n = s.n;
   p.k = s.kt;
   const int m = __builtin_popcountll(s.touched);
@@ -564,23 +670,30 @@ int launch_dense_k(const GateSetup& s, float2* state, const float2* mat, int64_t
   for (int j = 0; j < s.kt; ++j) p.tbits[j] = s.tb[j];
   const int D = 1 << s.kt;
   p.mat = mat;
+  p.uinv = uinv;
   p.mat_stride = mat_batch > 1 ? (int64_t)D * D : 0;
-  p.gpb = D >= 256 ? 1 : 256 / D;
-  if (p.gpb > p.groups) p.gpb = (int)p.groups;
+  p.grad = grad;
+  p.grad_stride = mat_batch > 1 ? 2ll * D * D : 0;
   const int threads = 256;
-  // each thread holds at most 16 outputs
-  if ((int64_t)p.gpb * D > 16 * threads) return fail(TQK_TOO_MANY_QUBITS, "dense gate: k=%d too wide", s.kt);
-  const size_t smem = (size_t)p.gpb * D * sizeof(float2);
-  if (smem > 48 * 1024) {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(k_dense_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_set = true;
-    }
+  // groups per block: up to 32 for narrow gates, bounded by 16 outputs per thread
+  int gpb = 32;
+  while (gpb > 1 && (int64_t)gpb * D > kDkMaxOut * threads) gpb >>= 1;
+  if (gpb > p.groups) gpb = (int)p.groups;
+  p.gpb = gpb;
+  p.mat_in_smem = (!adjoint && D <= 64) ? 1 : 0;
+  const size_t tile = (size_t)gpb * (D + 1) * sizeof(float2);
+  const size_t smem = adjoint ? 2 * tile : tile + (p.mat_in_smem ? (size_t)D * D * sizeof(float2) : 0);
+  if (smem > 200 * 1024) return fail(TQK_TOO_MANY_QUBITS, "dense gate: k=%d too wide", s.kt);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_dense_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_dense_k_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
   }
-  dim3 grid((unsigned)((p.groups + p.gpb - 1) / p.gpb), (unsigned)s.bsz, 1);
-  k_dense_k<<<grid, threads, smem, st>>>(p);
-  return launch_status("dense k-wire gate");
+  dim3 grid((unsigned)((p.groups + gpb - 1) / gpb), (unsigned)s.bsz, 1);
+  if (adjoint) k_dense_k_adj<<<grid, threads, smem, st>>>(p);
+  else k_dense_k<<<grid, threads, smem, st>>>(p);
+  return launch_status(adjoint ? "adjoint dense k-wire gate" : "dense k-wire gate");
 }
 
 int setup_targets(GateSetup& s, int n, int64_t bsz, const int32_t* targets, int kt, const int32_t* controls,
@@ -600,8 +713,8 @@ int setup_targets(GateSetup& s, int n, int64_t bsz, const int32_t* targets, int 
 }
 
 int dense_entry(void* state, void* lam, int64_t bsz, int n, const int32_t* controls, int nc,
-                const int32_t* targets, int kt, const void* mat, int64_t mat_batch, double* grad,
-                bool adjoint, void* stream, const char* what) {
+                const int32_t* targets, int kt, const void* mat, int64_t mat_batch, const void* uinv,
+                double* grad, bool adjoint, void* stream, const char* what) {
   int rc = check_state(state, bsz, n, what);
   if (rc) return rc;
   if (adjoint && (rc = check_state(lam, bsz, n, what))) return rc;
@@ -614,11 +727,11 @@ int dense_entry(void* state, void* lam, int64_t bsz, int n, const int32_t* contr
   auto* ps = static_cast<float2*>(state);
   auto* pl = static_cast<float2*>(lam);
   auto* pm = static_cast<const float2*>(mat);
-  if (kt == 1) return launch_dense<2>(s, ps, pl, pm, mat_batch, grad, adjoint, st);
-  if (kt == 2) return launch_dense<4>(s, ps, pl, pm, mat_batch, grad, adjoint, st);
-  if (adjoint) return fail(TQK_UNSUPPORTED, "%s: adjoint of a %d-target gate goes through the fused path", what, kt);
+  auto* pi = static_cast<const float2*>(uinv);
+  if (kt == 1) return launch_dense<2>(s, ps, pl, pm, mat_batch, pi, grad, adjoint, st);
+  if (kt == 2) return launch_dense<4>(s, ps, pl, pm, mat_batch, pi, grad, adjoint, st);
   if (nc > 0) return fail(TQK_UNSUPPORTED, "%s: controlled gates take 1 or 2 targets", what);
-  return launch_dense_k(s, ps, pm, mat_batch, st);
+  return launch_dense_k(s, ps, pl, pm, pi, mat_batch, grad, adjoint, st);
 }
 
 int phase_entry(void* state, void* lam, int64_t bsz, int n, const int32_t* wires, int k, const void* phase,
@@ -709,7 +822,7 @@ using namespace tqk;
 
 extern "C" int tqk_apply_matrix(void* state, int64_t bsz, int n, const int32_t* wires, int k, const void* mat,
                                 int64_t mat_batch, void* stream) {
-  return dense_entry(state, nullptr, bsz, n, nullptr, 0, wires, k, mat, mat_batch, nullptr, false, stream,
+  return dense_entry(state, nullptr, bsz, n, nullptr, 0, wires, k, mat, mat_batch, nullptr, nullptr, false, stream,
                      "tqk_apply_matrix");
 }
 
@@ -717,21 +830,22 @@ extern "C" int tqk_apply_controlled(void* state, int64_t bsz, int n, const int32
                                     const int32_t* targets, int kt, const void* mat, int64_t mat_batch,
                                     void* stream) {
   if (kt != 1 && kt != 2) return fail(TQK_UNSUPPORTED, "tqk_apply_controlled: kt=%d must be 1 or 2", kt);
-  return dense_entry(state, nullptr, bsz, n, controls, nc, targets, kt, mat, mat_batch, nullptr, false, stream,
-                     "tqk_apply_controlled");
+  return dense_entry(state, nullptr, bsz, n, controls, nc, targets, kt, mat, mat_batch, nullptr, nullptr, false,
+                     stream, "tqk_apply_controlled");
 }
 
 extern "C" int tqk_adjoint_matrix(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
-                                  const void* mat, int64_t mat_batch, double* grad, void* stream) {
-  return dense_entry(psi, lam, bsz, n, nullptr, 0, wires, k, mat, mat_batch, grad, true, stream,
+                                  const void* mat, int64_t mat_batch, const void* uncompute, double* grad,
+                                  void* stream) {
+  return dense_entry(psi, lam, bsz, n, nullptr, 0, wires, k, mat, mat_batch, uncompute, grad, true, stream,
                      "tqk_adjoint_matrix");
 }
 
 extern "C" int tqk_adjoint_controlled(void* psi, void* lam, int64_t bsz, int n, const int32_t* controls, int nc,
                                       const int32_t* targets, int kt, const void* mat, int64_t mat_batch,
-                                      double* grad, void* stream) {
+                                      const void* uncompute, double* grad, void* stream) {
   if (kt != 1 && kt != 2) return fail(TQK_UNSUPPORTED, "tqk_adjoint_controlled: kt=%d must be 1 or 2", kt);
-  return dense_entry(psi, lam, bsz, n, controls, nc, targets, kt, mat, mat_batch, grad, true, stream,
+  return dense_entry(psi, lam, bsz, n, controls, nc, targets, kt, mat, mat_batch, uncompute, grad, true, stream,
                      "tqk_adjoint_controlled");
 }
 

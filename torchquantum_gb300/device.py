@@ -71,7 +71,7 @@ class QuantumDevice(nn.Module):
                 st = st.to(self.device)
             st = st.to(torch.complex64)
             self._init = st if st.requires_grad else None
-            self._buf = st.detach().clone().contiguous()
+            self._buf = st.detach().resolve_conj().resolve_neg().clone().contiguous()
         self.bsz = int(self._buf.shape[0])
 
     @property

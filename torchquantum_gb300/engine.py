@@ -35,9 +35,9 @@ class TapeOp:
     ``source`` is the autograd-tracked tensor it was taken from (or None).
     """
 
-    __slots__ = ("kind", "wires", "controls", "targets", "ctrl_val", "operand", "source", "batch")
+    __slots__ = ("kind", "wires", "controls", "targets", "ctrl_val", "operand", "source", "batch", "uncompute")
 
-    def __init__(self, kind, wires, controls=(), targets=(), ctrl_val=1, operand=None, source=None):
+    def __init__(self, kind, wires, controls=(), targets=(), ctrl_val=1, operand=None, source=None, uncompute=None):
         self.kind = kind
         self.wires = list(wires)
         self.controls = list(controls)
@@ -46,10 +46,13 @@ class TapeOp:
         self.operand = operand
         self.source = source
         self.batch = 0 if operand is None else int(operand.shape[0])
+        # exact inverse of a dense/controlled operand that is not unitary (psi is uncomputed
+        # with it; the cotangent still propagates with U^H)
+        self.uncompute = uncompute
 
     @property
     def needs_grad(self) -> bool:
-        return self.source is not None and self.source.requires_grad
+        return self.source is not None and self.source.requires_grad and torch.is_grad_enabled()
 
     def grad_numel(self) -> int:
         """float64 values of this op's operand cotangent (complex128 interleaved)."""
@@ -80,24 +83,26 @@ def apply_op(buf: torch.Tensor, n: int, op: TapeOp) -> None:
         raise ValueError(f"unknown op kind {k}")
 
 
+def kernel_operand(t: torch.Tensor) -> torch.Tensor:
+    """Detached, materialised (no lazy conj/neg bit), contiguous copy-or-view for a kernel.
+
+    ``Tensor.conj()`` only sets a conjugation bit; ``contiguous()`` keeps that bit on an
+    already-contiguous view, so the raw pointer would still address unconjugated data.
+    """
+    return t.detach().resolve_conj().resolve_neg().contiguous()
+
+
 def _conj_t(m: torch.Tensor) -> torch.Tensor:
-    return m.conj().transpose(-1, -2).contiguous()
+    return kernel_operand(m.conj().transpose(-1, -2))
 
 
 def adjoint_op(psi: torch.Tensor, lam: torch.Tensor, n: int, op: TapeOp, grad: Optional[torch.Tensor]) -> None:
     """One reverse step: psi <- U^H psi, lam <- U^H lam, grad += lam conj(psi_before)^T."""
     k = op.kind
     if k == KIND_DENSE:
-        if len(op.wires) <= 2:
-            _lib.adjoint_matrix(psi, lam, n, op.wires, op.operand, op.batch, grad)
-        else:
-            if grad is not None:
-                raise NotImplementedError("gradient of a dense gate on more than 2 wires is not supported yet")
-            uh = _conj_t(op.operand)
-            _lib.apply_matrix(psi, n, op.wires, uh, op.batch)
-            _lib.apply_matrix(lam, n, op.wires, uh, op.batch)
+        _lib.adjoint_matrix(psi, lam, n, op.wires, op.operand, op.batch, grad, op.uncompute)
     elif k == KIND_CTRL:
-        _lib.adjoint_controlled(psi, lam, n, op.controls, op.targets, op.operand, op.batch, grad)
+        _lib.adjoint_controlled(psi, lam, n, op.controls, op.targets, op.operand, op.batch, grad, op.uncompute)
     elif k == KIND_X:
         _lib.apply_mcx(psi, n, op.controls, op.ctrl_val, op.targets[0])
         _lib.apply_mcx(lam, n, op.controls, op.ctrl_val, op.targets[0])
@@ -133,7 +138,7 @@ class CircuitFunction(torch.autograd.Function):
         (final,) = ctx.saved_tensors
         n, tape = ctx.n, ctx.tape
         psi = final.detach().clone()
-        lam = grad_out.detach().to(torch.complex64).contiguous().clone()
+        lam = kernel_operand(grad_out.to(torch.complex64)).clone()
         grad_ops = [op for op in tape if op.needs_grad]
         total = sum(op.grad_numel() for op in grad_ops)
         gbuf = torch.zeros(max(1, total), dtype=torch.float64, device=psi.device)

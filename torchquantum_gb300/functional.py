@@ -29,6 +29,9 @@ __all__ = ["gate_wrapper", "func_name_dict", "func_name_dict_collect", "mat_dict
            "apply_unitary_einsum"]
 
 _QU = ("qubitunitary", "qubitunitaryfast", "qubitunitarystrict")
+# operands that are not unitary by construction: upstream's cu2 block has no 1/sqrt(2)
+# (functional/u2.py), and qubitunitaryfast does not check its matrix
+_MAYBE_NON_UNITARY = ("cu2", "qubitunitaryfast")
 _VAR_WIRES_NOPARAM = ("multicnot", "multixcnot", "qft")
 
 
@@ -62,22 +65,27 @@ def _record(q_device, name, wires, params, inverse):
 
 
 def _op_from_matrix(name: str, matrix: torch.Tensor, wires, device) -> engine.TapeOp:
-    """Turn the (batched) gate matrix into the engine op for the gate's structure."""
+    """Turn the (batched) gate matrix into the engine op for the gate's structure.
+
+    ``source`` keeps the operand at the matrix's own precision (complex128 when built
+    for the fused method) and autograd-tracked; ``operand`` is the complex64 copy the
+    plain kernels read."""
     if matrix.dim() == 2:
         matrix = matrix.unsqueeze(0)
     if matrix.device != device:
         matrix = matrix.to(device)
-    if matrix.dtype != torch.complex64:
+    if not matrix.is_complex():
         matrix = matrix.to(torch.complex64)
     gd = G.GATES.get(name)
     struct = gd.struct if gd is not None else ("dense",)
     kind = struct[0]
     k = len(wires)
-    track = matrix if matrix.requires_grad else None
 
-    def mk(op_kind, operand, **kw):
-        src = operand if track is not None else None
-        return engine.TapeOp(op_kind, wires, operand=operand.detach().contiguous(), source=src, **kw)
+    def mk(op_kind, src, **kw):
+        kop = engine.kernel_operand(src.to(torch.complex64))
+        if name in _MAYBE_NON_UNITARY and op_kind in (engine.KIND_DENSE, engine.KIND_CTRL):
+            kw["uncompute"] = engine.kernel_operand(torch.linalg.inv(kop))
+        return engine.TapeOp(op_kind, wires, operand=kop, source=src, **kw)
 
     if kind == "x":
         nc = struct[1] if struct[1] >= 0 else k - 1
@@ -100,9 +108,12 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
     """Apply gate ``name`` to ``q_device`` (upstream gate_wrapper.py:324-446)."""
     params = _normalize_params(name, params)
     wires = [wires] if isinstance(wires, int) else [int(w) for w in wires]
+    fused = getattr(q_device, "method", "plain") == "fused"
     if q_device.record_op:
         _record(q_device, name, wires, params, inverse)
-    if static:
+    if static and parent_graph is not None and hasattr(parent_graph, "add_func"):
+        # a caller-provided graph object collects the op (gate_wrapper.py:393-403); without
+        # one, static mode is the device's fused method (module.static_support)
         parent_graph.add_func(name=name, wires=wires, parent_graph=parent_graph, params=params, n_wires=n_wires,
                               inverse=inverse)
         return
@@ -118,8 +129,10 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
         else:
             matrix = mat(params)
     elif mat is None:
+        if fused and params is not None and params.is_floating_point() and not params.is_complex():
+            params = params.to(torch.float64)  # fused blocks are built in complex128
         matrix = G.gate_matrix(cname, params, n_wires if n_wires is not None else len(wires),
-                               device=q_device.device)
+                               dtype=torch.complex128 if fused else torch.complex64, device=q_device.device)
     else:
         matrix = mat
     if inverse:
@@ -128,15 +141,12 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
     dim = matrix.shape[-1]
     assert int(round(math.log2(dim))) == len(wires), f"{name}: matrix of dim {dim} on wires {wires}"
     if len(wires) == 0:  # globalphase: a phase on every amplitude
-        q_device._apply(engine.TapeOp(engine.KIND_PHASE, [], operand=_c64(matrix.reshape(-1), q_device).detach(),
-                                      source=_c64(matrix.reshape(-1), q_device) if matrix.requires_grad else None))
+        ph = matrix.reshape(-1).to(q_device.device)
+        q_device._apply(engine.TapeOp(engine.KIND_PHASE, [], operand=engine.kernel_operand(ph.to(torch.complex64)),
+                                      source=ph))
         return
     q_device._apply(_op_from_matrix(cname if mat is None or isinstance(mat, Callable) else "qubitunitaryfast",
                                     matrix, wires, q_device.device))
-
-
-def _c64(t, q_device):
-    return t.to(device=q_device.device, dtype=torch.complex64).contiguous()
 
 
 class _Builder:

@@ -1,0 +1,170 @@
+"""Fused method: group gates into k-wire blocks, build each block's unitary in
+complex128, apply it with one pass over the state.
+
+Planner: greedy and linear in the number of gates per block.  A block starts with
+the first pending gate's wires; walking the pending list in order, a gate joins the
+block if none of its wires is blocked by an earlier gate left out and the union of
+wires stays within ``k``; otherwise its wires become blocked (gates on disjoint wires
+commute, so later gates may still join).  Upstream's static mode instead scores every
+``C(n, k)`` wire combination per block (``torchquantum/graph/graphs.py:384-532``),
+which is impractical at n = 24..28.
+
+Build: the block unitary starts as the identity and every gate is applied to its
+rows (the same permute/contract as a gate on a k-wire state with 2^k columns), in
+complex128 and through differentiable torch ops, so the cotangent of the block
+unitary returned by the adjoint sweep reaches every gate parameter by autograd.
+
+Apply: blocks of <= 2 wires use the plain kernels; wider blocks use the dense k-wire
+kernel (CUDA cores) or, for 5 or 6 wires on large states, the tensor-core kernel
+(``tc.py``).
+"""
+from __future__ import annotations
+
+from typing import List, Sequence, Tuple
+
+import torch
+
+from . import engine
+from . import gates as G
+
+__all__ = ["plan_blocks", "op_full_matrix", "build_block_unitary", "apply_fused"]
+
+
+def plan_blocks(wire_lists: Sequence[Sequence[int]], k: int) -> List[Tuple[List[int], List[int]]]:
+    """Greedy fusion plan: list of (sorted block wires, gate indices in order)."""
+    pending = list(range(len(wire_lists)))
+    blocks = []
+    while pending:
+        first = set(wire_lists[pending[0]])
+        if len(first) > k:  # a gate wider than the block size stays on its own
+            blocks.append((sorted(first), [pending[0]]))
+            pending = pending[1:]
+            continue
+        q = set(first)
+        blocked = set()
+        take, rest = [], []
+        for gi in pending:
+            w = set(wire_lists[gi])
+            if w & blocked:
+                blocked |= w
+                rest.append(gi)
+                continue
+            if len(q | w) <= k:
+                q |= w
+                take.append(gi)
+            else:
+                blocked |= w
+                rest.append(gi)
+            if len(blocked) >= 64 and not rest:
+                break
+        blocks.append((sorted(q), take))
+        pending = rest
+    return blocks
+
+
+def op_full_matrix(op: engine.TapeOp, dtype=torch.complex128) -> torch.Tensor:
+    """Full [B, 2^m, 2^m] matrix of a tape op on its own wires (differentiable in op.source)."""
+    src = op.source if op.source is not None else op.operand
+    k = op.kind
+    m = len(op.wires)
+    if k == engine.KIND_DENSE:
+        return src.to(dtype)
+    if k == engine.KIND_CTRL:
+        blk = src.to(dtype)
+        b, d = blk.shape[0], blk.shape[-1]
+        full = torch.eye(1 << m, dtype=dtype, device=blk.device).repeat(b, 1, 1)
+        full[:, -d:, -d:] = blk
+        return full
+    if k == engine.KIND_PHASE:
+        ph = src.to(dtype)
+        ones = torch.ones(ph.shape[0], (1 << m) - 1, dtype=dtype, device=ph.device)
+        return torch.diag_embed(torch.cat([ones, ph.reshape(-1, 1)], dim=1))
+    if k == engine.KIND_DIAG:
+        return torch.diag_embed(src.to(dtype))
+    if k in (engine.KIND_X, engine.KIND_SWAP):
+        dev = op.operand.device if op.operand is not None else None
+        return _perm_matrix(op.kind, len(op.wires), len(op.controls), op.ctrl_val, dtype, dev)
+    raise ValueError(f"cannot fuse op kind {k}")
+
+
+_PERM_CACHE = {}
+
+
+def _perm_matrix(kind, m, nc, ctrl_val, dtype, device):
+    key = (kind, m, nc, ctrl_val, dtype, str(device))
+    if key in _PERM_CACHE:
+        return _PERM_CACHE[key]
+    mat = _perm_matrix_cpu(kind, m, nc, ctrl_val, dtype)
+    if device is not None:
+        mat = mat.to(device)
+    _PERM_CACHE[key] = mat
+    return mat
+
+
+def _perm_matrix_cpu(kind, m, nc, ctrl_val, dtype):
+    dim = 1 << m
+    idx = torch.arange(dim)
+    if kind == engine.KIND_X:
+        cmask = ((1 << nc) - 1) << 1  # controls are the top nc bits of the (nc+1)-bit index
+        want = cmask if ctrl_val else 0
+        src = torch.where((idx & cmask) == want, idx ^ 1, idx)
+    else:  # controlled swap of the last two bits
+        cmask = ((1 << nc) - 1) << 2
+        b1, b0 = (idx >> 1) & 1, idx & 1
+        swapped = (idx & ~3) | (b0 << 1) | b1
+        src = torch.where((idx & cmask) == cmask, swapped, idx)
+    mat = torch.zeros(dim, dim, dtype=dtype)
+    mat[idx, src] = 1
+    return mat[None]
+
+
+def _apply_rows(u: torch.Tensor, g: torch.Tensor, pos: List[int], k: int) -> torch.Tensor:
+    """g (on row bits ``pos``, pos[0] most significant) times u, for u [B, 2^k, 2^k]."""
+    b = max(u.shape[0], g.shape[0])
+    d = 1 << k
+    ut = u.expand(b, d, d).reshape([b] + [2] * k + [d])
+    axes = [1 + p for p in pos]
+    rest = [a for a in range(1, k + 1) if a not in axes]
+    perm = [0] + axes + rest + [k + 1]
+    up = ut.permute(perm).reshape(b, 1 << len(pos), -1)
+    up = torch.matmul(g.expand(b, -1, -1), up)
+    up = up.reshape([b] + [2] * k + [d])
+    inv = [0] * len(perm)
+    for i, p in enumerate(perm):
+        inv[p] = i
+    return up.permute(inv).reshape(b, d, d)
+
+
+def build_block_unitary(ops: Sequence[engine.TapeOp], block_wires: List[int], device) -> torch.Tensor:
+    """Product of the block's gates, [B, 2^k, 2^k] complex128 (B = 1 or bsz)."""
+    k = len(block_wires)
+    u = torch.eye(1 << k, dtype=torch.complex128, device=device)[None]
+    where = {w: i for i, w in enumerate(block_wires)}
+    for op in ops:
+        g = op_full_matrix(op)
+        if g.device != device:
+            g = g.to(device)
+        u = _apply_rows(u, g, [where[w] for w in op.wires], k)
+    return u
+
+
+def apply_fused(qdev, ops: List[engine.TapeOp]) -> List[engine.TapeOp]:
+    """Plan, build and apply the pending ops of ``qdev``; returns the tape entries."""
+    n = qdev.n_wires
+    k = max(1, min(qdev.fuse_wires, n, 6))
+    # a global phase (no wires) is applied on its own, in order
+    blocks = plan_blocks([op.wires if op.wires else list(range(n)) for op in ops], k)
+    tape = []
+    for bwires, idxs in blocks:
+        bops = [ops[i] for i in idxs]
+        if len(bops) == 1:
+            op = bops[0]
+            engine.apply_op(qdev._buf, n, op)
+            tape.append(op)
+            continue
+        u = build_block_unitary(bops, bwires, qdev.device)
+        op = engine.TapeOp(engine.KIND_DENSE, bwires, operand=engine.kernel_operand(u.to(torch.complex64)),
+                           source=u if u.requires_grad else u.detach())
+        engine.apply_op(qdev._buf, n, op)
+        tape.append(op)
+    return tape

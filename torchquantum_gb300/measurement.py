@@ -18,6 +18,7 @@ from typing import List, Sequence, Union
 import torch
 
 from . import _lib
+from .engine import kernel_operand
 from .module import QuantumModule
 
 __all__ = ["expval_joint_analytical", "expval_joint_analytical_batch", "expval", "MeasureAll", "probs",
@@ -48,13 +49,13 @@ class PauliExpvalFunction(torch.autograd.Function):
     def forward(ctx, state, n, xmasks, zmasks):
         ctx.n, ctx.x, ctx.z = n, xmasks, zmasks
         ctx.save_for_backward(state)
-        return _lib.pauli_expval(state.detach().contiguous(), n, xmasks, zmasks).to(torch.float32)
+        return _lib.pauli_expval(kernel_operand(state), n, xmasks, zmasks).to(torch.float32)
 
     @staticmethod
     def backward(ctx, grad):
         (state,) = ctx.saved_tensors
         coef = (2.0 * grad).to(torch.float32).contiguous()
-        g = _lib.pauli_apply_sum(state.detach().contiguous(), ctx.n, ctx.x, ctx.z, coef)
+        g = _lib.pauli_apply_sum(kernel_operand(state), ctx.n, ctx.x, ctx.z, coef)
         return g, None, None, None
 
 
@@ -119,5 +120,5 @@ class MeasureAll(QuantumModule):
 
 def probs(qdev) -> torch.Tensor:
     """|psi|^2 as [bsz, 2^n] float32 (no autograd; use ``get_states_1d().abs()**2`` for gradients)."""
-    st = _state_2d(qdev).detach().contiguous()
+    st = kernel_operand(_state_2d(qdev))
     return _lib.probs(st, qdev.n_wires)
