@@ -124,6 +124,22 @@ int tqk_adjoint_phase(void* psi, void* lam, int64_t bsz, int n, const int32_t* w
 int tqk_adjoint_diagonal(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires, int k,
                          const void* diag, int64_t diag_batch, double* grad, void* stream);
 
+/* ---------------------------------------------------------------- fused blocks (tensor cores)
+ * A fused 6-wire block (64x64 complex U) applied to every column of the state as one
+ * tcgen05 GEMM with split-BF16 operands (hi.hi + hi.lo + lo.hi, fp32 accumulate).
+ * Replaces the per-block dense bmm of upstream static mode: QuantumGraph.apply_unitary
+ * (graph/graphs.py:836-860) -> qubitunitaryfast (functional/qubit_unitary.py:143).
+ *
+ * tqk_fused_prepare converts U (complex128 [u_batch, 64, 64], row-major, rows = output
+ * pattern, wires[0] the most significant bit) into the operand image the kernel reads
+ * (tqk_fused_image_bytes(u_batch) bytes, 16-byte aligned).  tqk_fused_apply needs
+ * n >= 13; u_batch is 1 or bsz.  `status` is a device int: the kernel writes
+ * TQK_TIMEOUT there if one of its bounded waits gives up (it then stops early). */
+int64_t tqk_fused_image_bytes(int64_t u_batch);
+int tqk_fused_prepare(const void* u, int64_t u_batch, void* image, void* stream);
+int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
+                    int64_t u_batch, int* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,3 +112,45 @@ def test_dense_k_wire_adjoint_vs_fd(kw):
                 d = (vals[0] - vals[1]) / (2 * eps)
                 gnum[i, j] += d * unit
     assert np.abs(ut.grad.cpu().numpy()[0] - gnum).max() < 1e-4
+
+
+@pytest.mark.parametrize("n,bsz,per_row", [(13, 1, False), (14, 3, True), (16, 2, False), (14, 2, True)])
+def test_tensor_core_block_vs_cuda_cores(n, bsz, per_row):
+    """The tcgen05 split-BF16 kernel against the CUDA-core dense kernel on random 6-wire unitaries."""
+    from torchquantum_gb300 import _lib
+
+    rng = np.random.default_rng(n * 10 + bsz)
+    for trial in range(4):
+        wires = [int(w) for w in rng.permutation(n)[:6]]
+        if trial == 1:
+            wires = list(range(n - 6, n))  # the lowest bits
+        b = bsz if per_row else 1
+        us = []
+        for _ in range(b):
+            z = rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64))
+            q_, r_ = np.linalg.qr(z)
+            us.append(q_ * (np.diag(r_) / np.abs(np.diag(r_))))
+        u128 = torch.tensor(np.stack(us), dtype=torch.complex128, device="cuda")
+        s = rng.normal(size=(bsz, 1 << n)) + 1j * rng.normal(size=(bsz, 1 << n))
+        s /= np.linalg.norm(s, axis=1, keepdims=True)
+        st = torch.tensor(s, dtype=torch.complex64, device="cuda")
+        ref = st.clone()
+        _lib.apply_matrix(ref, n, wires, u128.to(torch.complex64).contiguous(), b)
+        img = _lib.fused_prepare(u128)
+        _lib.fused_apply(st, n, wires, img, b)
+        torch.cuda.synchronize()
+        _lib.check_status(st.device)
+        err = (st - ref).abs().max().item()
+        scale = ref.abs().max().item()
+        assert err < 2e-5 * scale, (trial, wires, err, scale)
+
+
+def test_fused_tensor_core_circuit_vs_oracle():
+    rng = np.random.default_rng(21)
+    n, bsz = 14, 2
+    gates = _circuit(rng, n, bsz, 150)
+    q, _ = _run(n, bsz, gates, "fused", 6, grad=False)
+    assert any(op.image is not None for op in q._tape) or q._pending
+    got = q.get_states_1d().detach().cpu().numpy()
+    assert any(op.image is not None for op in q._tape)
+    assert np.abs(got - O.run(n, bsz, gates)).max() < 1e-5

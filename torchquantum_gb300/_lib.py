@@ -55,6 +55,9 @@ _SIGS = {
     "tqk_adjoint_controlled": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _i32p, _int, _vp, _i64, _vp, _vp, _vp]),
     "tqk_adjoint_phase": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
+    "tqk_fused_image_bytes": (_i64, [_i64]),
+    "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp]),
+    "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -213,3 +216,40 @@ def adjoint_phase(psi, lam, n, wires, phase, phase_batch, grad):
 def adjoint_diagonal(psi, lam, n, wires, diag, diag_batch, grad):
     _check(load().tqk_adjoint_diagonal(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), len(wires),
                                        diag.data_ptr(), diag_batch, _ptr(grad), _stream(psi)))
+
+
+# ------------------------------------------------------------------ fused (tensor cores)
+_STATUS = {}
+
+
+def status_word(device) -> torch.Tensor:
+    """Per-device int32 the tensor-core kernels write TQK_TIMEOUT into on a bounded-wait timeout."""
+    key = str(device)
+    t = _STATUS.get(key)
+    if t is None:
+        t = torch.zeros(1, dtype=torch.int32, device=device)
+        _STATUS[key] = t
+    return t
+
+
+def check_status(device) -> None:
+    """Raise if a kernel on ``device`` reported a timeout (synchronises); clears the word."""
+    t = status_word(device)
+    v = int(t.item())
+    if v != 0:
+        t.zero_()
+        raise TQKError(v, "a tensor-core kernel gave up waiting on its pipeline (bounded wait timed out)")
+
+
+def fused_prepare(u128: torch.Tensor) -> torch.Tensor:
+    """complex128 [B, 64, 64] -> operand image (uint8 tensor) for fused_apply."""
+    lib = load()
+    b = int(u128.shape[0])
+    img = torch.empty(lib.tqk_fused_image_bytes(b), dtype=torch.uint8, device=u128.device)
+    _check(lib.tqk_fused_prepare(u128.data_ptr(), b, img.data_ptr(), _stream(u128)))
+    return img
+
+
+def fused_apply(state, n, wires, image, u_batch):
+    _check(load().tqk_fused_apply(state.data_ptr(), state.shape[0], n, _i32(wires), image.data_ptr(), u_batch,
+                                  status_word(state.device).data_ptr(), _stream(state)))

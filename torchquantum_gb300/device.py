@@ -42,7 +42,8 @@ class QuantumDevice(nn.Module):
         self.record_op = record_op
         self.op_history: List[dict] = []
         self.method = "plain"          # "plain" | "fused" (see fusion.py)
-        self.fuse_wires = 5
+        self.fuse_wires = 6
+        self.fused_backend = "auto"    # "auto" | "tc" (tensor cores) | "cuda" (CUDA cores)
         self._tape: List[engine.TapeOp] = []
         self._pending: List[engine.TapeOp] = []   # fused method: recorded, not yet applied
         self._init: Optional[torch.Tensor] = None

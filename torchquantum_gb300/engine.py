@@ -35,7 +35,8 @@ class TapeOp:
     ``source`` is the autograd-tracked tensor it was taken from (or None).
     """
 
-    __slots__ = ("kind", "wires", "controls", "targets", "ctrl_val", "operand", "source", "batch", "uncompute")
+    __slots__ = ("kind", "wires", "controls", "targets", "ctrl_val", "operand", "source", "batch", "uncompute",
+                 "image")
 
     def __init__(self, kind, wires, controls=(), targets=(), ctrl_val=1, operand=None, source=None, uncompute=None):
         self.kind = kind
@@ -49,10 +50,12 @@ class TapeOp:
         # exact inverse of a dense/controlled operand that is not unitary (psi is uncomputed
         # with it; the cotangent still propagates with U^H)
         self.uncompute = uncompute
+        # tensor-core operand image of a fused 6-wire block (forward uses the tcgen05 kernel)
+        self.image = None
 
     @property
     def needs_grad(self) -> bool:
-        return self.source is not None and self.source.requires_grad and torch.is_grad_enabled()
+        return self.source is not None and self.source.requires_grad
 
     def grad_numel(self) -> int:
         """float64 values of this op's operand cotangent (complex128 interleaved)."""
@@ -68,7 +71,10 @@ def apply_op(buf: torch.Tensor, n: int, op: TapeOp) -> None:
     """Launch the forward kernel of ``op`` on ``buf`` (in place, current stream)."""
     k = op.kind
     if k == KIND_DENSE:
-        _lib.apply_matrix(buf, n, op.wires, op.operand, op.batch)
+        if op.image is not None:
+            _lib.fused_apply(buf, n, op.wires, op.image, op.batch)
+        else:
+            _lib.apply_matrix(buf, n, op.wires, op.operand, op.batch)
     elif k == KIND_CTRL:
         _lib.apply_controlled(buf, n, op.controls, op.targets, op.operand, op.batch)
     elif k == KIND_X:
@@ -129,6 +135,7 @@ class CircuitFunction(torch.autograd.Function):
     def forward(ctx, final: torch.Tensor, n: int, tape: List[TapeOp], init: Optional[torch.Tensor], *sources):
         ctx.n = n
         ctx.tape = tape
+        ctx.grad_ops = [op for op in tape if op.needs_grad]  # the order of ``sources``
         ctx.has_init = init is not None
         ctx.save_for_backward(final)
         return final
@@ -139,7 +146,7 @@ class CircuitFunction(torch.autograd.Function):
         n, tape = ctx.n, ctx.tape
         psi = final.detach().clone()
         lam = kernel_operand(grad_out.to(torch.complex64)).clone()
-        grad_ops = [op for op in tape if op.needs_grad]
+        grad_ops = ctx.grad_ops
         total = sum(op.grad_numel() for op in grad_ops)
         gbuf = torch.zeros(max(1, total), dtype=torch.float64, device=psi.device)
         offsets = {}
@@ -149,7 +156,7 @@ class CircuitFunction(torch.autograd.Function):
             off += op.grad_numel()
         for op in reversed(tape):
             g = None
-            if op.needs_grad:
+            if id(op) in offsets:
                 o = offsets[id(op)]
                 g = gbuf[o:o + op.grad_numel()]
             adjoint_op(psi, lam, n, op, g)

@@ -24,8 +24,8 @@ from typing import List, Sequence, Tuple
 
 import torch
 
+from . import _lib
 from . import engine
-from . import gates as G
 
 __all__ = ["plan_blocks", "op_full_matrix", "build_block_unitary", "apply_fused"]
 
@@ -148,23 +148,47 @@ def build_block_unitary(ops: Sequence[engine.TapeOp], block_wires: List[int], de
     return u
 
 
+TC_MIN_WIRES = 13     # the tensor-core kernel tiles 128 columns of 2^(n-6)
+TC_MIN_BLOCK = 4      # narrower blocks are cheaper on the CUDA-core kernels
+
+
+def use_tensor_cores(qdev, width: int) -> bool:
+    backend = getattr(qdev, "fused_backend", "auto")
+    if backend == "cuda" or qdev.n_wires < TC_MIN_WIRES:
+        return False
+    return width >= (1 if backend == "tc" else TC_MIN_BLOCK)
+
+
+def _pad_wires(bwires: List[int], n: int) -> List[int]:
+    """Extend a block to 6 wires with identity wires (lowest-numbered free wires)."""
+    extra = [w for w in range(n) if w not in bwires][:6 - len(bwires)]
+    return sorted(bwires + extra)
+
+
 def apply_fused(qdev, ops: List[engine.TapeOp]) -> List[engine.TapeOp]:
     """Plan, build and apply the pending ops of ``qdev``; returns the tape entries."""
     n = qdev.n_wires
     k = max(1, min(qdev.fuse_wires, n, 6))
-    # a global phase (no wires) is applied on its own, in order
-    blocks = plan_blocks([op.wires if op.wires else list(range(n)) for op in ops], k)
+    # a global phase (no wires) and gates with an exact-inverse operand (not unitary)
+    # are applied on their own, in order
+    wl = [op.wires if (op.wires and op.uncompute is None) else list(range(n)) for op in ops]
+    blocks = plan_blocks(wl, k)
     tape = []
     for bwires, idxs in blocks:
         bops = [ops[i] for i in idxs]
-        if len(bops) == 1:
+        if len(bops) == 1 and not (len(bops[0].wires) >= TC_MIN_BLOCK and use_tensor_cores(qdev, 6)):
             op = bops[0]
             engine.apply_op(qdev._buf, n, op)
             tape.append(op)
             continue
+        tc = use_tensor_cores(qdev, len(bwires))
+        if tc:
+            bwires = _pad_wires(bwires, n)
         u = build_block_unitary(bops, bwires, qdev.device)
         op = engine.TapeOp(engine.KIND_DENSE, bwires, operand=engine.kernel_operand(u.to(torch.complex64)),
                            source=u if u.requires_grad else u.detach())
+        if tc:
+            op.image = _lib.fused_prepare(engine.kernel_operand(u))
         engine.apply_op(qdev._buf, n, op)
         tape.append(op)
     return tape
