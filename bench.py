@@ -42,7 +42,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--method", default="plain", choices=["plain", "fused"])
+    ap.add_argument("--method", default="fused", choices=["plain", "fused"])
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain method for comparison")
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--bsz", type=int, default=16)
     ap.add_argument("--depth", type=int, default=400)
@@ -211,10 +212,11 @@ def run_ours(args):
     pw = torch.tensor(np.random.default_rng(3).normal(size=(1, 8)), dtype=torch.float32, device=dev)
     theta_dev = torch.tensor(theta_host, device=dev)
 
-    def step(theta):
+    def step(theta, method=args.method):
         q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
-        if args.method == "fused":
+        if method == "fused":
             q.method = "fused"
+            q.fuse_wires = 6
         W.apply_circuit(q, gates, theta)
         pr = tq.probs(q)
         ev = tq.expval_joint_analytical_batch(q, paulis)
@@ -256,6 +258,28 @@ def run_ours(args):
     if world > 1:
         line["config"]["parallelism"] = f"replicas x{world} (batch sharding, no collective in the step)"
 
+    _lib.check_status(dev)
+    if args.method == "fused" and not args.quick and not args.no_plain:
+        # ---------------- the plain gate-by-gate method on the same workload
+        for _ in range(2):
+            th.grad = None
+            step(th, "plain")
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            th.grad = None
+            step(th, "plain")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_plain = e0.elapsed_time(e1)
+        t = torch.tensor([ms_plain], device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_plain = float(t.item())
+        v_plain = bsz * args.steps * world / (ms_plain / 1e3)
+        line["plain_method"] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps}
+        line["fused_speedup_vs_plain"] = value / v_plain
     if not args.quick:
         # ---------------- end to end through the public API with host buffers
         pin_theta = torch.from_numpy(theta_host).pin_memory()
@@ -346,10 +370,35 @@ def roofline(args, dev):
         t = timeit(fn)
         gbs = nbytes / t / 1e9
         res[name] = {"us": t * 1e6, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak}
-    dom = res["dense1_adj"]
+    if n >= 13:
+        # fused 6-wire block on the tensor cores: forward (2S) and adjoint step (4S) per launch
+        rng = np.random.default_rng(0)
+        z = rng.normal(size=(bsz, 64, 64)) + 1j * rng.normal(size=(bsz, 64, 64))
+        u = torch.tensor(np.linalg.qr(z)[0], dtype=torch.complex128, device=dev)
+        img = _lib.fused_prepare(u)
+        imgh = _lib.fused_prepare(u.conj().transpose(-1, -2).contiguous())
+        mr = torch.zeros(bsz, 128, 128, dtype=torch.float64, device=dev)
+        wsets = [[int(x) for x in np.random.default_rng(i).choice(n, 6, replace=False)] for i in range(reps + 3)]
+        tiles = bsz * (1 << (n - 6)) // 128
+        fl_apply = tiles * 24 * 128 * 128 * 16 * 2
+        extra = {
+            "fused6_tc_fwd": (lambda i: _lib.fused_apply(psi, n, wsets[i], img, bsz), 2 * S, fl_apply),
+            "fused6_tc_adj": (lambda i: _lib.fused_adjoint(psi, lam, n, wsets[i], imgh, bsz, mr), 4 * S, 3 * fl_apply),
+        }
+        for name, (fn, nbytes, flops) in extra.items():
+            t = timeit(fn)
+            gbs = nbytes / t / 1e9
+            res[name] = {"us": t * 1e6, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak,
+                         "tensor_TFLOP/s": flops / t / 1e12}
+        _lib.check_status(dev)
+    if args.method == "fused" and "fused6_tc_adj" in res:
+        dom = res["fused6_tc_adj"]
+        kname = "tqk::tc::k_tc_adjoint (adjoint step of a fused 6-wire block, tcgen05 split-BF16)"
+    else:
+        dom = res["dense1_adj"]
+        kname = "k_dense_adj<2> (adjoint step of a dense 1-wire gate)"
     roof = {"bound": "hbm", "achieved": dom["GB/s"], "peak": peak, "unit": "GB/s", "frac": dom["GB/s"] / peak,
-            "traffic": None, "kernel": "k_dense_adj<2> (adjoint step of a dense 1-wire gate)",
-            "peak_source": f"{peak_kind} hbm_gbs"}
+            "traffic": None, "kernel": kname, "peak_source": f"{peak_kind} hbm_gbs"}
     return roof, res
 
 

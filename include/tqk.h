@@ -140,6 +140,80 @@ int tqk_fused_prepare(const void* u, int64_t u_batch, void* image, void* stream)
 int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
                     int64_t u_batch, int* status, void* stream);
 
+/* Adjoint step of a fused block on the tensor cores: psi <- U^H psi, lam <- U^H lam
+ * (image_h = tqk_fused_prepare of U^H), and, if mr_out != NULL, the real cross term
+ * mr_out[g][2j+p][2j'+q] += sum over columns of Re/Im parts lam_{j,p} * psi_{j',q}
+ * (float64, g = batch row if u_batch == bsz > 1 else 0; zeroed by the caller), from
+ * which M[j][j'] = sum lam[j] conj(psi[j']) and the cotangent of U, M U, follow.
+ * Replaces the autograd graph upstream records for the block's bmm. */
+int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires,
+                      const void* image_h, int64_t u_batch, double* mr_out, int* status,
+                      void* stream);
+
+/* ---------------------------------------------------------------- gate programs
+ * Parameterised gates whose operand the GPU builds from the parameters in place.
+ * Replaces the per-gate torch matrix builders (functional/u3.py:52-77, rx.py:19-46,
+ * ry.py:50-67, rz.py:150-172, ...) and their autograd graphs: operands and the analytic
+ * derivatives of every operand entry are evaluated in float64. */
+enum {
+  TQK_G_U3 = 0, TQK_G_RX = 1, TQK_G_RY = 2, TQK_G_RZ = 3, TQK_G_PHASE = 4, TQK_G_ROT = 5,
+  TQK_G_U2 = 6, TQK_G_R = 7, TQK_G_CRX = 8, TQK_G_CRY = 9, TQK_G_CRZ = 10, TQK_G_CU3 = 11,
+  TQK_G_CU1 = 12, TQK_G_CROT = 13, TQK_G_CU = 14, TQK_G_RZZ = 15, TQK_G_RXX = 16,
+  TQK_G_RYY = 17, TQK_G_RZX = 18, TQK_G_SINGLEEXC = 19
+};
+/* op kinds (operand shapes) inside fused blocks */
+enum { TQK_K_DENSE = 0, TQK_K_CTRL = 1, TQK_K_X = 2, TQK_K_PHASE = 3, TQK_K_DIAG = 4, TQK_K_SWAP = 5 };
+
+typedef struct {
+  int32_t type;          /* TQK_G_* */
+  int32_t inverse;       /* operand is the conjugate transpose (conjugate for diagonals) */
+  int32_t batch;         /* operand rows: 1 (broadcast) or bsz */
+  int32_t nparam;
+  const void* p;         /* parameter (row 0, column 0), float32 or float64, read in place */
+  int64_t p_row_stride;  /* elements between rows (0 when batch == 1) */
+  int64_t p_col_stride;  /* elements between parameters of a row */
+  int32_t p_is_double;
+  int32_t pad0;
+  void* op128;           /* out: complex128 operand [batch][size], or NULL */
+  void* op64;            /* out: complex64 operand [batch][size], or NULL */
+  const void* op_grad;   /* in (tqk_param_grads): complex128 operand cotangent [batch][size] */
+  double* grad;          /* float64 buffer laid out like the parameters (same strides), or NULL */
+} tqk_gate_desc;
+
+typedef struct {
+  int32_t kind;          /* TQK_K_* */
+  int32_t nw;            /* wires of the op (controls first, then targets) */
+  int32_t pos[6];        /* row-index bit of each op wire inside the block */
+  int32_t nctrl;
+  int32_t ctrl_val;
+  int32_t batch;         /* operand rows: 1 or bsz */
+  int32_t op_size;       /* complex entries per operand row */
+  const void* operand;   /* complex128 [batch][op_size] */
+  void* grad;            /* complex128 operand cotangent (atomically accumulated), or NULL */
+} tqk_block_op;
+
+typedef struct {
+  int32_t first_op, num_ops;
+  int32_t k;             /* block width (<= 6): U is 2^k x 2^k, block wire i <-> row bit k-1-i */
+  int32_t batch;         /* 1 or bsz */
+  void* u;               /* complex128 [batch][2^k][2^k] */
+  const void* gu;        /* complex128 dL/dU, same layout, or NULL */
+} tqk_block_desc;
+
+int tqk_gate_operand_size(int type);
+/* gates[ngates] (device array): write every gate's operand (op128 and/or op64). */
+int tqk_gate_operands(const tqk_gate_desc* gates, int ngates, void* stream);
+/* grad[...] += d loss / d param for every gate with grad != NULL, from op_grad. */
+int tqk_param_grads(const tqk_gate_desc* gates, int ngates, void* stream);
+/* U = G_m ... G_1 per (block, batch row) in float64; replaces upstream static mode's
+ * block unitary construction (graph/graphs.py:712-792). */
+int tqk_block_build(const tqk_block_desc* blocks, int nblocks, int max_batch, const tqk_block_op* ops,
+                    void* stream);
+/* From dL/dU (desc.gu) and U (desc.u): every op's operand cotangent, atomically added
+ * into op.grad (ops with grad == NULL are skipped). */
+int tqk_block_unbuild(const tqk_block_desc* blocks, int nblocks, int max_batch,
+                      const tqk_block_op* ops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,12 @@ _SIGS = {
     "tqk_fused_image_bytes": (_i64, [_i64]),
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp]),
     "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
+    "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
+    "tqk_gate_operand_size": (_int, [_int]),
+    "tqk_gate_operands": (_int, [_vp, _int, _vp]),
+    "tqk_param_grads": (_int, [_vp, _int, _vp]),
+    "tqk_block_build": (_int, [_vp, _int, _int, _vp, _vp]),
+    "tqk_block_unbuild": (_int, [_vp, _int, _int, _vp, _vp]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -253,3 +259,37 @@ def fused_prepare(u128: torch.Tensor) -> torch.Tensor:
 def fused_apply(state, n, wires, image, u_batch):
     _check(load().tqk_fused_apply(state.data_ptr(), state.shape[0], n, _i32(wires), image.data_ptr(), u_batch,
                                   status_word(state.device).data_ptr(), _stream(state)))
+
+
+def fused_adjoint(psi, lam, n, wires, image_h, u_batch, mr_out):
+    _check(load().tqk_fused_adjoint(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), image_h.data_ptr(),
+                                    u_batch, _ptr(mr_out), status_word(psi.device).data_ptr(), _stream(psi)))
+
+
+def cross_to_complex(mr: torch.Tensor) -> torch.Tensor:
+    """[B, 128, 128] real cross term -> M [B, 64, 64] complex128, M[j][j'] = sum lam[j] conj(psi[j'])."""
+    d = mr.view(-1, 64, 2, 64, 2)
+    re = d[:, :, 0, :, 0] + d[:, :, 1, :, 1]
+    im = d[:, :, 1, :, 0] - d[:, :, 0, :, 1]
+    return torch.complex(re, im)
+
+
+# ------------------------------------------------------------------ gate programs
+def _dstream(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def gate_operands(table, ngates, device):
+    _check(load().tqk_gate_operands(table.data_ptr(), ngates, _dstream(device)))
+
+
+def param_grads(table, ngates, device):
+    _check(load().tqk_param_grads(table.data_ptr(), ngates, _dstream(device)))
+
+
+def block_build(blocks, nblocks, max_batch, ops, device):
+    _check(load().tqk_block_build(blocks.data_ptr(), nblocks, max_batch, ops.data_ptr(), _dstream(device)))
+
+
+def block_unbuild(blocks, nblocks, max_batch, ops, device):
+    _check(load().tqk_block_unbuild(blocks.data_ptr(), nblocks, max_batch, ops.data_ptr(), _dstream(device)))

@@ -324,6 +324,213 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_apply(const ApplyParams p) {
   }
 }
 
+// ------------------------------------------------------------------ adjoint step
+// One reverse step of the adjoint method for a fused block, per tile of 128 columns:
+//   psi <- U^H psi, lam <- U^H lam   (two K-major GEMMs against the image of U^H)
+//   Mr += Lam~^T Psi~                 (the cross term, reduced over the tile's columns)
+// where Lam~ / Psi~ are the tiles' real embeddings [column][2j+p].  The cross GEMM
+// reads the same swizzled tiles as MN-major operands (M = N = 128 = (j, p), K = the
+// tile's columns, 16 per instruction: start address + 2048 B per K step, LBO = 16 KB
+// between the two 64-element (j, p) halves, SBO = 1024 B between 8-column groups).
+// Mr is flushed to float64 (atomicAdd into mr_out[row or 0][128][128]) at the end and
+// whenever a per-row U changes with the batch row; the host forms
+//   M[j][j'] = sum lam[j] conj(psi[j'])  from Mr, and the cotangent of U as M U.
+// Single-buffered: shared memory holds U^H (64 KB) and the psi and lam tiles (64 KB each).
+struct AdjParams {
+  float2* psi;
+  float2* lam;
+  int n;
+  BitInsert ins;
+  uint64_t off[64];
+  const uint8_t* uimg;   // image of U^H
+  int64_t u_batch;
+  int64_t tiles_per_row;
+  int64_t tiles;
+  double* mr_out;        // [u_batch][128][128] or null (no gradient)
+  int* status;
+};
+
+__device__ __forceinline__ void produce_rows(const float2* row, int64_t c0, const BitInsert& ins, uint8_t* abuf,
+                                             const uint64_t* offs) {
+#pragma unroll
+  for (int e = threadIdx.x; e < kTileCols * 16; e += kThreads) {
+    const int i = e & (kTileCols - 1);
+    const int q = e >> 7;
+    const uint64_t base = insert_zero_bits(static_cast<uint64_t>(c0 + i), ins);
+    float2 a[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a[r] = row[base + offs[4 * q + r]];
+    uint4 hi, lo;
+    split4(a, hi, lo);
+    const uint32_t o = sw128_off(i, q);
+    *reinterpret_cast<uint4*>(abuf + o) = hi;
+    *reinterpret_cast<uint4*>(abuf + kImgBytes + o) = lo;
+  }
+}
+
+__device__ __forceinline__ void epilogue_rows(float2* row, int64_t c0, const BitInsert& ins, uint32_t d_tmem,
+                                              const uint64_t* offs) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = warp & 3, half = warp >> 2;
+  const int i = sub * 32 + lane;
+  const uint64_t base = insert_zero_bits(static_cast<uint64_t>(c0 + i), ins);
+#pragma unroll
+  for (int part = 0; part < 2; ++part) {
+    const int col = half * 64 + part * 32;
+    uint32_t r[32];
+    tmem_ld32(d_tmem + (static_cast<uint32_t>(sub * 32) << 16) + col, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int v = 0; v < 16; ++v) {
+      const int j = (col >> 1) + v;
+      row[base + offs[j]] = make_float2(__uint_as_float(r[2 * v]), __uint_as_float(r[2 * v + 1]));
+    }
+  }
+}
+
+// MN-major SWIZZLE_128B descriptor over a [column][128 (j,p)] tile image.
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>(kKBlockBytes >> 4) << 16;
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;
+  d |= static_cast<uint64_t>(1) << 46;
+  d |= static_cast<uint64_t>(2) << 61;
+  return d;
+}
+
+__device__ __forceinline__ void issue_cross(uint32_t d_tmem, uint32_t lam_s, uint32_t psi_s, bool first) {
+  // kind::f16, D fp32, bf16 A/B, A and B MN-major (bits 15, 16), M = N = 128
+  constexpr uint32_t idesc = idesc_bf16(128, 128) | (1u << 15) | (1u << 16);
+  const uint32_t ao[3] = {0u, 0u, static_cast<uint32_t>(kImgBytes)};
+  const uint32_t bo[3] = {0u, static_cast<uint32_t>(kImgBytes), 0u};
+#pragma unroll
+  for (int prod = 0; prod < 3; ++prod) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const uint32_t koff = s * 2048;
+      mma_bf16(d_tmem, desc_sw128_mn(lam_s + ao[prod] + koff), desc_sw128_mn(psi_s + bo[prod] + koff), idesc,
+               (first && prod == 0 && s == 0) ? 0u : 1u);
+    }
+  }
+}
+
+__device__ __forceinline__ void flush_cross(double* dst, uint32_t d_tmem) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = warp & 3, half = warp >> 2;
+  const int m = sub * 32 + lane;
+#pragma unroll
+  for (int part = 0; part < 2; ++part) {
+    const int col = half * 64 + part * 32;
+    uint32_t r[32];
+    tmem_ld32(d_tmem + (static_cast<uint32_t>(sub * 32) << 16) + col, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int v = 0; v < 32; ++v) atomicAdd(dst + m * 128 + col + v, static_cast<double>(__uint_as_float(r[v])));
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const AdjParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  uint8_t* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+  uint8_t* bimg = smem;                        // U^H hi, lo
+  uint8_t* apsi = smem + 2 * kImgBytes;        // psi tile hi, lo
+  uint8_t* alam = apsi + 2 * kImgBytes;        // lam tile hi, lo
+  uint64_t* offs = reinterpret_cast<uint64_t*>(alam + 2 * kImgBytes);
+  uint64_t* bar = offs + 64;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+
+  const int64_t per = (p.tiles + gridDim.x - 1) / gridDim.x;
+  const int64_t t_begin = blockIdx.x * per;
+  const int64_t t_end = min(p.tiles, t_begin + per);
+  if (t_begin >= t_end) return;
+
+  if (threadIdx.x < 64) offs[threadIdx.x] = p.off[threadIdx.x];
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512u)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc_fence_before();
+  }
+  int64_t cur_b = t_begin / p.tiles_per_row;
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? cur_b : 0) * 2 * kImgBytes);
+    uint4* dst = reinterpret_cast<uint4*>(bimg);
+    for (int i = threadIdx.x; i < 2 * kImgBytes / 16; i += kThreads) dst[i] = src[i];
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t d_psi = tmem, d_lam = tmem + 128, d_m = tmem + 256;
+  const uint32_t b_s = smem_u32(bimg), psi_s = smem_u32(apsi), lam_s = smem_u32(alam);
+  uint32_t phase = 0;
+  int aborted = 0, inflight = 0;
+  bool first_cross = true;
+
+  for (int64_t t = t_begin; t < t_end && !aborted; ++t) {
+    const int64_t b = t / p.tiles_per_row;
+    const int64_t c0 = (t % p.tiles_per_row) * kTileCols;
+    if (p.u_batch > 1 && b != cur_b) {
+      // per-row U: flush the cross term of the previous row, reload U^H
+      if (p.mr_out && !first_cross) {
+        tc_fence_after();
+        flush_cross(p.mr_out + cur_b * 128 * 128, d_m);
+        first_cross = true;
+      }
+      const uint4* src = reinterpret_cast<const uint4*>(p.uimg + b * 2 * kImgBytes);
+      uint4* dst = reinterpret_cast<uint4*>(bimg);
+      for (int i = threadIdx.x; i < 2 * kImgBytes / 16; i += kThreads) dst[i] = src[i];
+      cur_b = b;
+    }
+    float2* prow = p.psi + (b << p.n);
+    float2* lrow = p.lam + (b << p.n);
+    produce_rows(prow, c0, p.ins, apsi, offs);
+    produce_rows(lrow, c0, p.ins, alam, offs);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      issue_mma(d_psi, psi_s, b_s);
+      issue_mma(d_lam, lam_s, b_s);
+      if (p.mr_out) issue_cross(d_m, lam_s, psi_s, first_cross);
+      mma_commit(bar);
+    }
+    inflight = 1;
+    first_cross = false;
+    const int timed_out = mbar_wait(bar, phase) ? 0 : 1;
+    if (__syncthreads_or(timed_out)) {
+      if (threadIdx.x == 0) atomicExch(p.status, TQK_TIMEOUT);
+      aborted = 1;
+      break;
+    }
+    phase ^= 1u;
+    inflight = 0;
+    tc_fence_after();
+    epilogue_rows(prow, c0, p.ins, d_psi, offs);
+    epilogue_rows(lrow, c0, p.ins, d_lam, offs);
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (aborted && inflight) mbar_wait(bar, phase);
+  if (!aborted && p.mr_out && !first_cross) {
+    tc_fence_after();
+    flush_cross(p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, d_m);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+  }
+}
+
 // U (complex128 [u_batch][64][64], row-major) -> hi/lo bf16 images of the real
 // embedding in the SWIZZLE_128B K-major layout expected by k_tc_apply (B operand:
 // row n = 2j'+p', K = 2j+p).  One thread per (batch, row n, 16-byte chunk).
@@ -373,6 +580,49 @@ extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, void* image, vo
   tc::k_tc_prep<<<static_cast<unsigned>((work + 255) / 256), 256, 0, as_stream(stream)>>>(
       static_cast<const double2*>(u), u_batch, static_cast<uint8_t*>(image));
   return launch_status("tqk_fused_prepare");
+}
+
+extern "C" int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires,
+                                 const void* image_h, int64_t u_batch, double* mr_out, int* status, void* stream) {
+  const char* what = "tqk_fused_adjoint";
+  int rc = check_state(psi, bsz, n, what);
+  if (rc) return rc;
+  if ((rc = check_state(lam, bsz, n, what))) return rc;
+  if ((rc = check_batch(u_batch, bsz, what))) return rc;
+  if (!image_h || !status) return fail(TQK_BAD_POINTER, "%s: null image/status", what);
+  if (n < 13) return fail(TQK_UNSUPPORTED, "%s: needs n_wires >= 13 (got %d)", what, n);
+  int tb[6];
+  uint64_t used = 0;
+  if ((rc = wires_to_bits(n, wires, 6, tb, &used, what))) return rc;
+  tc::AdjParams p;
+  p.psi = static_cast<float2*>(psi);
+  p.lam = static_cast<float2*>(lam);
+  p.n = n;
+  p.ins = make_insert(used);
+  for (int j = 0; j < 64; ++j) {
+    uint64_t o = 0;
+    for (int jb = 0; jb < 6; ++jb)
+      if ((j >> (5 - jb)) & 1) o |= 1ull << tb[jb];
+    p.off[j] = o;
+  }
+  p.uimg = static_cast<const uint8_t*>(image_h);
+  p.u_batch = u_batch;
+  p.tiles_per_row = (1ll << (n - 6)) / tc::kTileCols;
+  p.tiles = p.tiles_per_row * bsz;
+  p.mr_out = mr_out;
+  p.status = status;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = 1024 + 6 * tc::kImgBytes + 64 * 8 + 8 + 16;
+  static int attr_dev = -1;
+  if (attr_dev != dev) {
+    cudaFuncSetAttribute(tc::k_tc_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    attr_dev = dev;
+  }
+  const int64_t grid = p.tiles < sms ? p.tiles : sms;
+  tc::k_tc_adjoint<<<static_cast<unsigned>(grid), tc::kThreads, smem, as_stream(stream)>>>(p);
+  return launch_status(what);
 }
 
 extern "C" int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,

@@ -20,6 +20,7 @@ import numpy as np
 import torch
 import torch.nn as nn
 
+from . import _lib
 from . import engine
 
 __all__ = ["QuantumDevice"]
@@ -83,29 +84,34 @@ class QuantumDevice(nn.Module):
         return s.reshape([2] * self.n_wires)
 
     # ------------------------------------------------------------------ gate path
-    def _apply(self, op: engine.TapeOp) -> None:
-        if op.operand is not None and op.batch not in (1, self.bsz):
-            raise ValueError(f"gate operand batch {op.batch} does not match QuantumDevice bsz {self.bsz}")
-        if self.method == "fused":
-            self._pending.append(op)
-            self._out = None
-            return
-        if self._exported:  # the buffer is referenced by an exported tensor: copy on write
-            self._buf = self._buf.clone()
-            self._exported = False
-        engine.apply_op(self._buf, self.n_wires, op)
-        self._tape.append(op)
+    def _apply(self, op) -> None:
+        """Record a gate (``engine.TapeOp`` or ``program.NativeGate``); it runs at the next read."""
+        b = op.batch
+        if b and b not in (1, self.bsz):
+            raise ValueError(f"gate operand batch {b} does not match QuantumDevice bsz {self.bsz}")
+        n = self.n_wires
+        seen = set()
+        for w in op.wires:  # same checks (and messages) as the kernels' host validation
+            if w < 0 or w >= n:
+                raise _lib.TQKError(1, f"wire {w} out of range for n_wires={n}")
+            if w in seen:
+                raise _lib.TQKError(1, f"wire {w} used twice")
+            seen.add(w)
+        self._pending.append(op)
         self._out = None
 
     def _flush(self) -> None:
+        """Compile the recorded gates into a segment and apply it to the state buffer."""
         if self._pending:
-            from . import fusion
+            from . import program
 
             ops, self._pending = self._pending, []
-            if self._exported:
+            if self._exported:  # the buffer is referenced by an exported tensor: copy on write
                 self._buf = self._buf.clone()
                 self._exported = False
-            self._tape.extend(fusion.apply_fused(self, ops))
+            seg = program.Segment(self, ops, self.method)
+            seg.apply(self._buf)
+            self._tape.append(seg)
             self._out = None
 
     def _output(self) -> torch.Tensor:
@@ -113,7 +119,7 @@ class QuantumDevice(nn.Module):
         self._flush()
         if self._out is not None:
             return self._out
-        sources = [op.source for op in self._tape if op.needs_grad]
+        sources = [t for sg in self._tape for t in sg.diff_inputs]
         needs = bool(sources) or (self._init is not None and self._init.requires_grad)
         if needs and torch.is_grad_enabled():
             out = engine.CircuitFunction.apply(self._buf, self.n_wires, list(self._tape), self._init, *sources)

@@ -35,9 +35,6 @@ class TapeOp:
     ``source`` is the autograd-tracked tensor it was taken from (or None).
     """
 
-    __slots__ = ("kind", "wires", "controls", "targets", "ctrl_val", "operand", "source", "batch", "uncompute",
-                 "image")
-
     def __init__(self, kind, wires, controls=(), targets=(), ctrl_val=1, operand=None, source=None, uncompute=None):
         self.kind = kind
         self.wires = list(wires)
@@ -123,19 +120,36 @@ def adjoint_op(psi: torch.Tensor, lam: torch.Tensor, n: int, op: TapeOp, grad: O
         raise ValueError(f"unknown op kind {k}")
 
 
-class CircuitFunction(torch.autograd.Function):
-    """final_state = circuit(init_state, operands...) with an adjoint-method backward.
+def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: Optional[torch.Tensor]) -> None:
+    """Tensor-core adjoint step of a fused 6-wire block: psi, lam <- U^H (.), and the
+    cotangent of U as M U with M = sum over columns of lam conj(psi)^T (U unitary),
+    added into ``grad`` (float64 interleaved view of a complex128 [batch, 64, 64])."""
+    u = u128.detach()
+    img_h = _lib.fused_prepare(kernel_operand(u.conj().transpose(-1, -2)))
+    mr = None
+    if grad is not None:
+        mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=psi.device)
+    _lib.fused_adjoint(psi, lam, n, wires, img_h, batch, mr)
+    if grad is not None:
+        gu = torch.matmul(_lib.cross_to_complex(mr), u)
+        torch.view_as_complex(grad.view(-1, 2)).view(u.shape).add_(gu)
 
-    forward receives the already-computed final state (the device buffer) and returns
-    it; backward walks ``tape`` in reverse.  Inputs: ``init`` (the anchored initial
-    state, possibly requiring grad) followed by the operand sources that require grad.
+
+class CircuitFunction(torch.autograd.Function):
+    """final_state = circuit(init_state, differentiable inputs...) with an adjoint backward.
+
+    ``segments`` are the compiled gate runs (``program.Segment``) applied since the
+    state was anchored; forward receives the already-computed final state (the device
+    buffer) and returns it.  Inputs after ``init`` are every segment's
+    ``diff_inputs`` in order (parameter base tensors, generic operand sources).
+    backward walks the segments in reverse, each returning its inputs' gradients.
     """
 
     @staticmethod
-    def forward(ctx, final: torch.Tensor, n: int, tape: List[TapeOp], init: Optional[torch.Tensor], *sources):
+    def forward(ctx, final: torch.Tensor, n: int, segments: list, init: Optional[torch.Tensor], *inputs):
         ctx.n = n
-        ctx.tape = tape
-        ctx.grad_ops = [op for op in tape if op.needs_grad]  # the order of ``sources``
+        ctx.segments = segments
+        ctx.counts = [len(sg.diff_inputs) for sg in segments]
         ctx.has_init = init is not None
         ctx.save_for_backward(final)
         return final
@@ -143,27 +157,11 @@ class CircuitFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out: torch.Tensor):
         (final,) = ctx.saved_tensors
-        n, tape = ctx.n, ctx.tape
         psi = final.detach().clone()
         lam = kernel_operand(grad_out.to(torch.complex64)).clone()
-        grad_ops = ctx.grad_ops
-        total = sum(op.grad_numel() for op in grad_ops)
-        gbuf = torch.zeros(max(1, total), dtype=torch.float64, device=psi.device)
-        offsets = {}
-        off = 0
-        for op in grad_ops:
-            offsets[id(op)] = off
-            off += op.grad_numel()
-        for op in reversed(tape):
-            g = None
-            if id(op) in offsets:
-                o = offsets[id(op)]
-                g = gbuf[o:o + op.grad_numel()]
-            adjoint_op(psi, lam, n, op, g)
-        grads = []
-        for op in grad_ops:
-            o = offsets[id(op)]
-            g = torch.view_as_complex(gbuf[o:o + op.grad_numel()].view(-1, 2)).view(op.operand.shape)
-            grads.append(g.to(op.source.dtype))
+        per_seg = []
+        for sg, cnt in zip(reversed(ctx.segments), reversed(ctx.counts)):
+            per_seg.append(sg.backward(psi, lam, cnt > 0))
+        grads = [g for gl in reversed(per_seg) for g in gl]
         g_init = lam if ctx.has_init else None
         return (None, None, None, g_init, *grads)

@@ -24,6 +24,7 @@ import torch
 
 from . import engine
 from . import gates as G
+from . import program
 
 __all__ = ["gate_wrapper", "func_name_dict", "func_name_dict_collect", "mat_dict", "apply_unitary_bmm",
            "apply_unitary_einsum"]
@@ -103,6 +104,26 @@ def _op_from_matrix(name: str, matrix: torch.Tensor, wires, device) -> engine.Ta
     return mk(engine.KIND_DENSE, matrix)
 
 
+_STRUCT_NCTRL = {"dense": 0, "diag": 0, "phase": 0}
+
+
+def _native_record(cname, wires, params, inverse, q_device):
+    """A NativeGate for a supported parameterised gate (operand built on the GPU)."""
+    gd = G.GATES[cname]
+    ntype, npar = program.NATIVE[cname]
+    if params.dim() != 2 or params.shape[1] != npar or len(wires) != gd.num_wires:
+        return None
+    if params.device != q_device.device:
+        params = params.to(q_device.device)
+    if params.dtype not in (torch.float32, torch.float64):
+        params = params.to(torch.float32)
+    kind_name = gd.struct[0]
+    kind = {"dense": engine.KIND_DENSE, "ctrl": engine.KIND_CTRL, "diag": engine.KIND_DIAG,
+            "phase": engine.KIND_PHASE}[kind_name]
+    nctrl = gd.struct[1] if kind_name == "ctrl" else 0
+    return program.NativeGate(cname, wires, params, inverse, kind, nctrl)
+
+
 def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, static=False, parent_graph=None,
                  inverse=False):
     """Apply gate ``name`` to ``q_device`` (upstream gate_wrapper.py:324-446)."""
@@ -118,6 +139,11 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
                               inverse=inverse)
         return
     cname = G.canonical_name(name)
+    if mat is None and cname in program.NATIVE and isinstance(params, torch.Tensor) and not params.is_complex():
+        nat = _native_record(cname, wires, params, inverse, q_device)
+        if nat is not None:
+            q_device._apply(nat)
+            return
     if isinstance(mat, Callable):
         # upstream calling convention of the builder (gate_wrapper.py:406-423)
         if n_wires is None or name in _QU:

@@ -9,14 +9,12 @@ commute, so later gates may still join).  Upstream's static mode instead scores 
 ``C(n, k)`` wire combination per block (``torchquantum/graph/graphs.py:384-532``),
 which is impractical at n = 24..28.
 
-Build: the block unitary starts as the identity and every gate is applied to its
-rows (the same permute/contract as a gate on a k-wire state with 2^k columns), in
-complex128 and through differentiable torch ops, so the cotangent of the block
-unitary returned by the adjoint sweep reaches every gate parameter by autograd.
+Build: ``program.Segment`` builds every block unitary on the GPU in float64
+(``tqk_block_build``); ``build_block_unitary`` here is the same product written with
+torch ops, used to check it.
 
-Apply: blocks of <= 2 wires use the plain kernels; wider blocks use the dense k-wire
-kernel (CUDA cores) or, for 5 or 6 wires on large states, the tensor-core kernel
-(``tc.py``).
+Apply: wide blocks on states of >= 13 wires run on the tensor-core kernel, padded to
+6 wires with identity wires; otherwise the dense k-wire kernel (CUDA cores).
 """
 from __future__ import annotations
 
@@ -27,7 +25,7 @@ import torch
 from . import _lib
 from . import engine
 
-__all__ = ["plan_blocks", "op_full_matrix", "build_block_unitary", "apply_fused"]
+__all__ = ["plan_blocks", "op_full_matrix", "build_block_unitary", "use_tensor_cores"]
 
 
 def plan_blocks(wire_lists: Sequence[Sequence[int]], k: int) -> List[Tuple[List[int], List[int]]]:
@@ -62,7 +60,7 @@ def plan_blocks(wire_lists: Sequence[Sequence[int]], k: int) -> List[Tuple[List[
     return blocks
 
 
-def op_full_matrix(op: engine.TapeOp, dtype=torch.complex128) -> torch.Tensor:
+def op_full_matrix(op: engine.TapeOp, dtype=torch.complex128, device=None) -> torch.Tensor:
     """Full [B, 2^m, 2^m] matrix of a tape op on its own wires (differentiable in op.source)."""
     src = op.source if op.source is not None else op.operand
     k = op.kind
@@ -82,8 +80,7 @@ def op_full_matrix(op: engine.TapeOp, dtype=torch.complex128) -> torch.Tensor:
     if k == engine.KIND_DIAG:
         return torch.diag_embed(src.to(dtype))
     if k in (engine.KIND_X, engine.KIND_SWAP):
-        dev = op.operand.device if op.operand is not None else None
-        return _perm_matrix(op.kind, len(op.wires), len(op.controls), op.ctrl_val, dtype, dev)
+        return _perm_matrix(op.kind, len(op.wires), len(op.controls), op.ctrl_val, dtype, device)
     raise ValueError(f"cannot fuse op kind {k}")
 
 
@@ -141,7 +138,7 @@ def build_block_unitary(ops: Sequence[engine.TapeOp], block_wires: List[int], de
     u = torch.eye(1 << k, dtype=torch.complex128, device=device)[None]
     where = {w: i for i, w in enumerate(block_wires)}
     for op in ops:
-        g = op_full_matrix(op)
+        g = op_full_matrix(op, device=device)
         if g.device != device:
             g = g.to(device)
         u = _apply_rows(u, g, [where[w] for w in op.wires], k)
@@ -163,32 +160,3 @@ def _pad_wires(bwires: List[int], n: int) -> List[int]:
     """Extend a block to 6 wires with identity wires (lowest-numbered free wires)."""
     extra = [w for w in range(n) if w not in bwires][:6 - len(bwires)]
     return sorted(bwires + extra)
-
-
-def apply_fused(qdev, ops: List[engine.TapeOp]) -> List[engine.TapeOp]:
-    """Plan, build and apply the pending ops of ``qdev``; returns the tape entries."""
-    n = qdev.n_wires
-    k = max(1, min(qdev.fuse_wires, n, 6))
-    # a global phase (no wires) and gates with an exact-inverse operand (not unitary)
-    # are applied on their own, in order
-    wl = [op.wires if (op.wires and op.uncompute is None) else list(range(n)) for op in ops]
-    blocks = plan_blocks(wl, k)
-    tape = []
-    for bwires, idxs in blocks:
-        bops = [ops[i] for i in idxs]
-        if len(bops) == 1 and not (len(bops[0].wires) >= TC_MIN_BLOCK and use_tensor_cores(qdev, 6)):
-            op = bops[0]
-            engine.apply_op(qdev._buf, n, op)
-            tape.append(op)
-            continue
-        tc = use_tensor_cores(qdev, len(bwires))
-        if tc:
-            bwires = _pad_wires(bwires, n)
-        u = build_block_unitary(bops, bwires, qdev.device)
-        op = engine.TapeOp(engine.KIND_DENSE, bwires, operand=engine.kernel_operand(u.to(torch.complex64)),
-                           source=u if u.requires_grad else u.detach())
-        if tc:
-            op.image = _lib.fused_prepare(engine.kernel_operand(u))
-        engine.apply_op(qdev._buf, n, op)
-        tape.append(op)
-    return tape

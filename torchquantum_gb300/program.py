@@ -1,0 +1,406 @@
+"""Gate programs: how a recorded sequence of gates becomes GPU work.
+
+Gates are recorded cheaply by ``gate_wrapper`` and compiled into a ``Segment`` when
+the state is read:
+
+* every parameterised gate of a supported type (``NATIVE``) gets its operand built
+  on the GPU by one ``tqk_gate_operands`` launch for the whole segment, reading its
+  parameters in place through their strides (no per-gate torch ops);
+* the plain method then applies each op with its kernel; the fused method plans
+  blocks of up to 6 wires (``fusion.plan_blocks``), builds every block unitary in
+  float64 with one ``tqk_block_build`` launch, and applies each block with the
+  tensor-core kernel (or the CUDA-core dense kernel on small states);
+* the backward walks the segment in reverse with the adjoint kernels, turns block
+  cotangents into gate-operand cotangents with ``tqk_block_unbuild``, and gate-operand
+  cotangents into parameter gradients with ``tqk_param_grads`` (analytic
+  derivatives), accumulated in float64 into one buffer per parameter base tensor.
+
+Gates with no native type (qubitunitary, multirz, qft, user matrices, ...) keep the
+torch-built operand and its autograd graph (``generic`` ops).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import engine
+
+# canonical gate name -> (TQK_G_* type id, number of parameters)
+NATIVE = {
+    "u3": (0, 3), "rx": (1, 1), "ry": (2, 1), "rz": (3, 1), "phaseshift": (4, 1), "u1": (4, 1), "rot": (5, 3),
+    "u2": (6, 2), "r": (7, 2), "crx": (8, 1), "cry": (9, 1), "crz": (10, 1), "cu3": (11, 3), "cu1": (12, 1),
+    "crot": (13, 3), "cu": (14, 4), "rzz": (15, 1), "rxx": (16, 1), "ryy": (17, 1), "rzx": (18, 1),
+    "singleexcitation": (19, 1),
+}
+_DIAG_TYPES = {3: 2, 4: 1, 12: 1, 10: 4, 15: 4}  # type -> operand size for diagonal / phase operands
+_WIDE_TYPES = {16, 17, 18, 19}                    # 4x4 dense operands
+
+KIND_ID = {engine.KIND_DENSE: 0, engine.KIND_CTRL: 1, engine.KIND_X: 2, engine.KIND_PHASE: 3,
+           engine.KIND_DIAG: 4, engine.KIND_SWAP: 5}
+
+
+def operand_size(type_id: int) -> int:
+    if type_id in _DIAG_TYPES:
+        return _DIAG_TYPES[type_id]
+    return 16 if type_id in _WIDE_TYPES else 4
+
+
+# ---------------------------------------------------------------- ctypes descriptor layouts
+class GateDesc(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("inverse", ctypes.c_int32), ("batch", ctypes.c_int32),
+                ("nparam", ctypes.c_int32), ("p", ctypes.c_void_p), ("p_row_stride", ctypes.c_int64),
+                ("p_col_stride", ctypes.c_int64), ("p_is_double", ctypes.c_int32), ("pad0", ctypes.c_int32),
+                ("op128", ctypes.c_void_p), ("op64", ctypes.c_void_p), ("op_grad", ctypes.c_void_p),
+                ("grad", ctypes.c_void_p)]
+
+
+class BlockOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("nw", ctypes.c_int32), ("pos", ctypes.c_int32 * 6),
+                ("nctrl", ctypes.c_int32), ("ctrl_val", ctypes.c_int32), ("batch", ctypes.c_int32),
+                ("op_size", ctypes.c_int32), ("operand", ctypes.c_void_p), ("grad", ctypes.c_void_p)]
+
+
+class BlockDesc(ctypes.Structure):
+    _fields_ = [("first_op", ctypes.c_int32), ("num_ops", ctypes.c_int32), ("k", ctypes.c_int32),
+                ("batch", ctypes.c_int32), ("u", ctypes.c_void_p), ("gu", ctypes.c_void_p)]
+
+
+assert ctypes.sizeof(GateDesc) == 80 and ctypes.sizeof(BlockOp) == 64 and ctypes.sizeof(BlockDesc) == 32
+
+
+def _to_device_table(structs, device) -> torch.Tensor:
+    """Array of ctypes structures -> device uint8 tensor (via a pinned staging copy)."""
+    n = len(structs)
+    size = ctypes.sizeof(structs[0]) * n if n else 0
+    host = torch.empty(max(size, 1), dtype=torch.uint8, pin_memory=True)
+    arr = (type(structs[0]) * n)(*structs)
+    ctypes.memmove(host.data_ptr(), ctypes.addressof(arr), size)
+    dev = host.to(device, non_blocking=True)
+    return dev, host  # keep the staging buffer alive until the copy has run
+
+
+# ---------------------------------------------------------------- recorded native gate
+class NativeGate:
+    """A parameterised gate whose operand the GPU builds from ``params`` in place."""
+
+    __slots__ = ("name", "type_id", "nparam", "wires", "params", "inverse", "kind", "nctrl", "batch")
+
+    def __init__(self, name, wires, params, inverse, kind, nctrl):
+        self.name = name
+        self.type_id, self.nparam = NATIVE[name]
+        self.wires = list(wires)
+        self.params = params          # [B, P] float32/float64 on the device (may require grad)
+        self.inverse = bool(inverse)
+        self.kind = kind              # engine.KIND_*
+        self.nctrl = nctrl
+        self.batch = int(params.shape[0])
+
+
+def _param_base(p: torch.Tensor):
+    """(base tensor to differentiate, element offset of p[0, 0] inside base's storage)."""
+    base = p._base if p._base is not None else p
+    if base.dtype not in (torch.float32, torch.float64) or not _dense(base):
+        return p, 0
+    return base, p.storage_offset() - base.storage_offset()
+
+
+def _dense(t: torch.Tensor) -> bool:
+    try:
+        return t.is_contiguous() or t.is_non_overlapping_and_dense()
+    except AttributeError:
+        return t.is_contiguous()
+
+
+# ---------------------------------------------------------------- segment
+class Segment:
+    """A compiled run of gates: forward applied at construction, ``backward`` on demand."""
+
+    def __init__(self, qdev, records: List, method: str):
+        from . import fusion
+
+        self.n = qdev.n_wires
+        self.bsz = qdev.bsz
+        self.device = qdev.device
+        dev = self.device
+        n = self.n
+        # ---- native gate operands (one launch)
+        natives = [r for r in records if isinstance(r, NativeGate)]
+        self.natives = natives
+        sizes = [operand_size(g.type_id) * g.batch for g in natives]
+        total = sum(sizes)
+        self.op128 = torch.empty(max(total, 1), dtype=torch.complex128, device=dev)
+        self.op64 = torch.empty(max(total, 1), dtype=torch.complex64, device=dev)
+        self.gate_offsets = []
+        descs = []
+        off = 0
+        self._keep = []
+        for g, sz in zip(natives, sizes):
+            p = g.params
+            d = GateDesc()
+            d.type, d.inverse, d.batch, d.nparam = g.type_id, int(g.inverse), g.batch, g.nparam
+            d.p = p.data_ptr()
+            d.p_row_stride = p.stride(0) if g.batch > 1 else 0
+            d.p_col_stride = p.stride(1)
+            d.p_is_double = int(p.dtype == torch.float64)
+            d.op128 = self.op128.data_ptr() + 16 * off
+            d.op64 = self.op64.data_ptr() + 8 * off
+            self.gate_offsets.append(off)
+            descs.append(d)
+            off += sz
+        self.gate_descs = descs
+        if descs:
+            table, host = _to_device_table(descs, dev)
+            self._keep += [table, host]
+            _lib.gate_operands(table, len(descs), dev)
+        # ---- exec ops: one TapeOp per record (operands point into op64 / op128)
+        ops = []
+        gi = 0
+        for r in records:
+            if isinstance(r, NativeGate):
+                o = self.gate_offsets[gi]
+                sz = operand_size(r.type_id)
+                shape = _operand_shape(r, sz)
+                op = engine.TapeOp(r.kind, r.wires, controls=r.wires[:r.nctrl], targets=r.wires[r.nctrl:],
+                                   operand=self.op64[o:o + sz * r.batch].view(shape))
+                op.native = r
+                op.op128 = self.op128[o:o + sz * r.batch].view(shape)
+                gi += 1
+            else:
+                op = r
+            ops.append(op)
+        self.records = ops
+        # ---- plan
+        self.blocks = []
+        if method == "fused":
+            k = max(1, min(qdev.fuse_wires, n, 6))
+            wl = [op.wires if fusable(op) else list(range(n)) for op in ops]
+            plan = fusion.plan_blocks(wl, k)
+            exec_ops = []
+            for bwires, idxs in plan:
+                members = [ops[i] for i in idxs]
+                if len(members) == 1:  # a lone gate is cheapest on its own kernel
+                    exec_ops.append(members[0])
+                    continue
+                exec_ops.append(self._make_block(qdev, members, bwires))
+            self.exec_ops = exec_ops
+            self._build_blocks()
+        else:
+            self.exec_ops = ops
+        # ---- differentiable inputs
+        self.bases: Dict[int, tuple] = {}
+        for g in natives:
+            if g.params.requires_grad:
+                base, _ = _param_base(g.params)
+                self.bases.setdefault(id(base), (base, None))
+        self.generic_sources = [op for op in ops if not hasattr(op, "native") and op.needs_grad]
+        self.diff_inputs = [b for b, _ in self.bases.values()] + [op.source for op in self.generic_sources]
+
+    # -------------------------------------------------------------- blocks
+    def _make_block(self, qdev, members, bwires):
+        from . import fusion
+
+        tc = fusion.use_tensor_cores(qdev, len(bwires))
+        if tc:
+            bwires = fusion._pad_wires(bwires, self.n)
+        k = len(bwires)
+        batch = max(m.batch if m.batch else 1 for m in members)
+        blk = engine.TapeOp(engine.KIND_DENSE, bwires)
+        blk.members = members
+        blk.block_batch = batch
+        blk.tc = tc
+        blk.batch = batch
+        blk.k = k
+        self.blocks.append(blk)
+        return blk
+
+    def _build_blocks(self):
+        if not self.blocks:
+            return
+        dev = self.device
+        sizes = [b.block_batch * (1 << (2 * b.k)) for b in self.blocks]
+        self.u128 = torch.empty(max(sum(sizes), 1), dtype=torch.complex128, device=dev)
+        off = 0
+        bdescs, bops = [], []
+        for blk, sz in zip(self.blocks, sizes):
+            d = 1 << blk.k
+            blk.u128 = self.u128[off:off + sz].view(blk.block_batch, d, d)
+            off += sz
+            where = {w: blk.k - 1 - i for i, w in enumerate(blk.wires)}
+            bd = BlockDesc()
+            bd.first_op, bd.num_ops, bd.k, bd.batch = len(bops), len(blk.members), blk.k, blk.block_batch
+            bd.u = blk.u128.data_ptr()
+            bd.gu = None
+            bdescs.append(bd)
+            for m in blk.members:
+                bops.append(self._block_op(m, where))
+        self.block_descs, self.block_ops = bdescs, bops
+        bt, bh = _to_device_table(bdescs, dev)
+        ot, oh = _to_device_table(bops, dev)
+        self._keep += [bt, bh, ot, oh]
+        maxb = max(b.block_batch for b in self.blocks)
+        _lib.block_build(bt, len(bdescs), maxb, ot, dev)
+        for blk in self.blocks:
+            if blk.tc:
+                blk.image = _lib.fused_prepare(blk.u128)
+            else:
+                blk.operand = blk.u128.to(torch.complex64)
+        # keep operands of non-native members alive in complex128
+        self._member128 = [getattr(m, "_op128_keep", None) for b in self.blocks for m in b.members]
+
+    def _block_op(self, m, where):
+        bo = BlockOp()
+        bo.kind = KIND_ID[m.kind]
+        wires = m.wires
+        bo.nw = len(wires)
+        for j, w in enumerate(wires):
+            bo.pos[j] = where[w]
+        bo.nctrl = len(m.controls) if m.kind in (engine.KIND_CTRL, engine.KIND_X, engine.KIND_SWAP) else 0
+        bo.ctrl_val = m.ctrl_val
+        if m.kind in (engine.KIND_X, engine.KIND_SWAP):
+            bo.batch, bo.op_size, bo.operand = 1, 1, self._dummy_ptr()
+            return bo
+        o128 = m.op128 if hasattr(m, "op128") else _generic128(m)
+        bo.batch = int(o128.shape[0])
+        bo.op_size = int(o128[0].numel())
+        bo.operand = o128.data_ptr()
+        bo.grad = None
+        return bo
+
+    def _dummy_ptr(self):
+        if not hasattr(self, "_dummy"):
+            self._dummy = torch.zeros(1, dtype=torch.complex128, device=self.device)
+        return self._dummy.data_ptr()
+
+    # -------------------------------------------------------------- forward
+    def apply(self, buf: torch.Tensor) -> None:
+        for op in self.exec_ops:
+            if getattr(op, "members", None) is not None:
+                if op.tc:
+                    _lib.fused_apply(buf, self.n, op.wires, op.image, op.block_batch)
+                else:
+                    _lib.apply_matrix(buf, self.n, op.wires, op.operand, op.block_batch)
+            else:
+                engine.apply_op(buf, self.n, op)
+
+    # -------------------------------------------------------------- backward
+    def backward(self, psi: torch.Tensor, lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
+        """Reverse sweep over this segment; returns grads for ``self.diff_inputs``."""
+        dev = self.device
+        n = self.n
+        opg = torch.zeros_like(self.op128) if (need_grads and self.natives) else None
+        gslots = {}
+        for op in self.generic_sources:
+            gslots[id(op)] = torch.zeros(op.operand.shape, dtype=torch.complex128, device=dev)
+        gu = torch.zeros_like(self.u128) if (need_grads and self.blocks) else None
+        for op in reversed(self.exec_ops):
+            if getattr(op, "members", None) is not None:
+                slot = None
+                if gu is not None and _block_needs_grad(op):
+                    slot = _as_real(gu, op.u128, self.u128)
+                if op.tc:
+                    engine.adjoint_fused_tc(psi, lam, n, op.wires, op.u128, op.block_batch, slot)
+                else:
+                    _lib.adjoint_matrix(psi, lam, n, op.wires, op.operand, op.block_batch, slot)
+                continue
+            slot = None
+            if need_grads:
+                if hasattr(op, "native") and op.native.params.requires_grad:
+                    slot = _as_real(opg, op.op128, self.op128)
+                elif id(op) in gslots:
+                    slot = torch.view_as_real(gslots[id(op)]).view(-1)
+            engine.adjoint_op(psi, lam, n, op, slot)
+        if not need_grads:
+            return [None] * len(self.diff_inputs)
+        # block cotangents -> member operand cotangents
+        if self.blocks and gu is not None:
+            bops = []
+            bdescs = []
+            for bi, blk in enumerate(self.blocks):
+                bd = BlockDesc()
+                src = self.block_descs[bi]
+                bd.first_op, bd.num_ops, bd.k, bd.batch = src.first_op, src.num_ops, src.k, src.batch
+                bd.u = blk.u128.data_ptr()
+                bd.gu = gu.data_ptr() + (blk.u128.data_ptr() - self.u128.data_ptr()) \
+                    if _block_needs_grad(blk) else None
+                bdescs.append(bd)
+                for m, src_op in zip(blk.members, self.block_ops[src.first_op:src.first_op + src.num_ops]):
+                    bo = BlockOp.from_buffer_copy(src_op)
+                    bo.grad = None
+                    if hasattr(m, "native") and m.native.params.requires_grad:
+                        bo.grad = opg.data_ptr() + (m.op128.data_ptr() - self.op128.data_ptr())
+                    elif id(m) in gslots:
+                        bo.grad = gslots[id(m)].data_ptr()
+                    bops.append(bo)
+            bt, bh = _to_device_table(bdescs, dev)
+            ot, oh = _to_device_table(bops, dev)
+            maxb = max(b.block_batch for b in self.blocks)
+            _lib.block_unbuild(bt, len(bdescs), maxb, ot, dev)
+            self._keep_bw = [bt, bh, ot, oh]
+        # operand cotangents -> parameter gradients
+        grads = []
+        if self.natives and self.bases:
+            gbufs = {k: torch.zeros_like(b, dtype=torch.float64) for k, (b, _) in self.bases.items()}
+            descs = []
+            for g, d, off in zip(self.natives, self.gate_descs, self.gate_offsets):
+                if not g.params.requires_grad:
+                    continue
+                base, eoff = _param_base(g.params)
+                nd = GateDesc.from_buffer_copy(d)
+                nd.op128 = None
+                nd.op64 = None
+                nd.op_grad = opg.data_ptr() + 16 * off
+                nd.grad = gbufs[id(base)].data_ptr() + 8 * eoff
+                descs.append(nd)
+            if descs:
+                table, host = _to_device_table(descs, dev)
+                _lib.param_grads(table, len(descs), dev)
+                self._keep_pg = [table, host]
+            for key, (base, _) in self.bases.items():
+                grads.append(gbufs[key].to(base.dtype))
+        else:
+            grads += [None] * len(self.bases)
+        for op in self.generic_sources:
+            grads.append(gslots[id(op)].to(op.source.dtype).view(op.source.shape))
+        return grads
+
+
+def _operand_shape(r: NativeGate, sz: int):
+    if r.type_id in _DIAG_TYPES:
+        return (r.batch,) if sz == 1 else (r.batch, sz)
+    d = 4 if r.type_id in _WIDE_TYPES else 2
+    return (r.batch, d, d)
+
+
+def _as_real(buf: torch.Tensor, view: torch.Tensor, base: torch.Tensor) -> torch.Tensor:
+    """float64 interleaved view of ``buf`` at the position ``view`` occupies inside ``base``."""
+    off = (view.data_ptr() - base.data_ptr()) // 16
+    return torch.view_as_real(buf[off:off + view.numel()]).view(-1)
+
+
+def _block_needs_grad(blk) -> bool:
+    return any((hasattr(m, "native") and m.native.params.requires_grad) or m.needs_grad for m in blk.members)
+
+
+def _generic128(m) -> torch.Tensor:
+    t = m.source if m.source is not None else m.operand
+    t = engine.kernel_operand(t.to(torch.complex128))
+    m._op128_keep = t
+    return t
+
+
+def fusable(op) -> bool:
+    """Ops the block kernels can fold into a fused block."""
+    if not op.wires or getattr(op, "uncompute", None) is not None:
+        return False
+    nw = len(op.wires)
+    if op.kind in (engine.KIND_X, engine.KIND_SWAP, engine.KIND_PHASE):
+        return nw <= 6
+    if op.kind == engine.KIND_DIAG:
+        return nw <= 4
+    if op.kind == engine.KIND_CTRL:
+        return len(op.targets) <= 2 and nw <= 6
+    return nw <= 2
