@@ -98,6 +98,21 @@ int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uint64_t* xmas
                      const uint64_t* zmask, int m, double* out, void* scratch,
                      int64_t scratch_bytes, void* stream);
 
+/* Same result as tqk_pauli_expval, without caller scratch: the block partials live in
+ * a 1 MiB array inside libtqk.so (one per device, shared by every call), so the call
+ * allocates nothing.  For callers that cannot allocate: a host binding this C ABI over
+ * FFI that holds only raw pointers to its own buffers and has no device allocator, or
+ * a service held to a fixed device-memory budget.  No counterpart in the upstream
+ * project.  Limits: partials (tqk_pauli_expval_scratch_bytes) must fit
+ * tqk_pauli_expval_noalloc_capacity() bytes and m <= 4096, else
+ * TQK_SCRATCH_TOO_SMALL / TQK_BAD_SHAPE.  Calls that overlap on the GPU race on the
+ * shared array.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress, device current); make that first call before any stream
+ * capture. */
+int64_t tqk_pauli_expval_noalloc_capacity(void);
+int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, const uint64_t* xmask,
+                             const uint64_t* zmask, int m, double* out, void* stream);
+
 /* out = sum_j coef[b*m + j] * P_j psi  (complex64 [bsz, 2^n]; coef float32 device).
  * The backward of the expvals above (cotangent of psi). */
 int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const uint64_t* xmask,

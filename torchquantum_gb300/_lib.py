@@ -59,6 +59,8 @@ _SIGS = {
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp]),
     "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
     "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
+    "tqk_pauli_expval_noalloc_capacity": (_i64, []),
+    "tqk_pauli_expval_noalloc": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp]),
     "tqk_gate_operand_size": (_int, [_int]),
     "tqk_gate_operands": (_int, [_vp, _int, _vp]),
     "tqk_param_grads": (_int, [_vp, _int, _vp]),

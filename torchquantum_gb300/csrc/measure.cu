@@ -328,3 +328,126 @@ extern "C" int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const 
   }
   return TQK_OK;
 }
+
+// ------------------------------------------------------------------ no-allocation variant
+// tqk_pauli_expval_noalloc: the same computation as tqk_pauli_expval for callers that
+// cannot hand the library a scratch buffer: a host program binding the C ABI from
+// another language over FFI with only raw pointers to its own buffers and no device
+// allocator to draw from, or a service that runs inside a fixed device-memory budget
+// where the library must not call cudaMalloc.  Its block partials live in the
+// file-scope array below instead of caller scratch, so the call allocates nothing,
+// neither device memory nor host heap.
+//
+// Limits: the partials must fit kNoAllocScratchBytes (1 MiB): bsz * blocks_per_row * 8
+// doubles, where blocks_per_row = min(ceil(1216 / bsz), ceil(2^n / 1024)); and at most
+// kNoAllocMaxStrings strings per call.  Larger calls are rejected with
+// TQK_SCRATCH_TOO_SMALL / TQK_BAD_SHAPE before any launch.
+//
+// Every call shares the one array per device and it keeps the last call's contents.
+// Nothing in it needs to start at zero: every partial a call reads back was written
+// earlier in the same call.  Calls whose kernels overlap on the GPU (different
+// streams, or different host threads without ordering) race on the array.
+//
+// Set-up: the first call on each device looks up the array's device address with
+// cudaGetSymbolAddress (the device must be current) and caches it; make that first
+// call before any stream capture.
+namespace tqk {
+
+constexpr int64_t kNoAllocScratchBytes = 1 << 20;
+constexpr int kNoAllocMaxStrings = 4096;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocScratchBytes / sizeof(double)];
+
+static void* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+static int noalloc_scratch(void** out, const char* what) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(TQK_CUDA_ERROR, "%s: cudaGetDevice failed", what);
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(TQK_UNSUPPORTED, "%s: device %d beyond %d", what, dev,
+                                                        kNoAllocMaxDevices);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess || p == nullptr)
+      return fail(TQK_CUDA_ERROR, "%s: cudaGetSymbolAddress failed: %s", what, cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return TQK_OK;
+}
+
+}  // namespace tqk
+
+extern "C" int64_t tqk_pauli_expval_noalloc_capacity(void) { return tqk::kNoAllocScratchBytes; }
+
+extern "C" int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, const uint64_t* xmask,
+                                        const uint64_t* zmask, int m, double* out, void* stream) {
+  const char* what = "tqk_pauli_expval_noalloc";
+  int rc = check_state(state, bsz, n, what);
+  if (rc) return rc;
+  if (m <= 0) return TQK_OK;
+  if (m > kNoAllocMaxStrings)
+    return fail(TQK_BAD_SHAPE, "%s: %d strings exceed the limit of %d per call", what, m, kNoAllocMaxStrings);
+  if (!xmask || !zmask || !out) return fail(TQK_BAD_POINTER, "%s: null mask/output pointer", what);
+  const int64_t need = tqk_pauli_expval_scratch_bytes(bsz, n, m);
+  if (need > kNoAllocScratchBytes)
+    return fail(TQK_SCRATCH_TOO_SMALL, "%s: needs %lld bytes of partials, the static array holds %lld (reduce bsz)",
+                what, (long long)need, (long long)kNoAllocScratchBytes);
+  const uint64_t lim = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+  for (int j = 0; j < m; ++j)
+    if ((xmask[j] | zmask[j]) & ~lim) return fail(TQK_BAD_WIRES, "%s: string %d has bits beyond n_wires=%d", what, j, n);
+  void* scratch = nullptr;
+  if ((rc = noalloc_scratch(&scratch, what))) return rc;
+  cudaStream_t st = as_stream(stream);
+  const int64_t nblk = reduce_blocks_per_row(bsz, n);
+  double* partial = static_cast<double*>(scratch);
+  unsigned char done[kNoAllocMaxStrings];
+  for (int j = 0; j < m; ++j) done[j] = 0;
+  for (int j0 = 0; j0 < m; ++j0) {
+    if (done[j0]) continue;
+    ExpvalParams p;
+    p.state = static_cast<const float2*>(state);
+    p.n = n;
+    p.x = xmask[j0];
+    p.ns = 0;
+    p.m = kMaxStringsPerPass;
+    p.partial = partial;
+    FinishCols cols;
+    for (int j = j0; j < m && p.ns < kMaxStringsPerPass; ++j) {
+      if (done[j] || xmask[j] != p.x) continue;
+      done[j] = 1;
+      p.z[p.ns] = zmask[j];
+      p.ny[p.ns] = __builtin_popcountll(xmask[j] & zmask[j]) & 3;
+      cols.c[p.ns] = j;
+      p.col[p.ns] = j;
+      p.ns++;
+    }
+    for (int s = p.ns; s < kMaxStringsPerPass; ++s) {
+      p.z[s] = 0;
+      p.ny[s] = 0;
+      p.col[s] = 0;
+      cols.c[s] = 0;
+    }
+    dim3 grid(static_cast<unsigned>(nblk), static_cast<unsigned>(bsz), 1);
+    if (p.x == 0) {
+      p.work = (1ll << n) >> 1;
+      k_expval_diag<<<grid, 256, 0, st>>>(p);
+    } else {
+      p.hbit = 63 - __builtin_clzll(p.x);
+      if (p.x == 1ull) {
+        p.work = (1ll << n) >> 1;
+        k_expval_pair<true><<<grid, 256, 0, st>>>(p);
+      } else {
+        p.work = (1ll << n) >> 2;
+        k_expval_pair<false><<<grid, 256, 0, st>>>(p);
+      }
+    }
+    if ((rc = launch_status(what))) return rc;
+    const int64_t nout = bsz * p.ns;
+    k_expval_finish<<<static_cast<unsigned>((nout + 127) / 128), 128, 0, st>>>(partial, nblk, p.ns,
+                                                                               kMaxStringsPerPass, cols, m, out, bsz);
+    if ((rc = launch_status(what))) return rc;
+  }
+  return TQK_OK;
+}
