@@ -111,3 +111,123 @@ def test_tc_tile_roundtrip_matches_oracle(tb_choice):
     assert sorted(touched) == list(range(1 << n))
     ref = O.apply(state, u[None], wires, n)
     np.testing.assert_allclose(out, ref, atol=1e-12)
+
+
+# ---------------------------------------------------------------- v2 (cp.async staging)
+def stage_chunk(c):
+    return c ^ ((c >> 5) & 31)
+
+
+def tc_setup(n, tb, adj):
+    used = sum(1 << b for b in tb)
+    ncol = 6 if adj else 7
+    colbits = [q for q in range(n) if not (used >> q) & 1][:ncol]
+    sbits = sorted(set(tb) | set(colbits))
+    col_pos = [sbits.index(b) for b in colbits]
+    tgt_pos = [sbits.index(b) for b in tb]
+    return sbits, col_pos, tgt_pos
+
+
+def scatter(u, sbits):
+    return sum(1 << sbits[b] for b in range(len(sbits)) if (u >> b) & 1)
+
+
+def emulate_v2(states, n, tb, adj, bimg):
+    """Run the v2 data path for every tile; returns (outputs per state, cross term or None)."""
+    sbits, col_pos, tgt_pos = tc_setup(n, tb, adj)
+    assert sbits[0] == 0  # 16-byte chunks hold address-adjacent amplitude pairs
+    cols = 64 if adj else 128
+    nbits = 12 if adj else 13
+    chunks = 1 << (nbits - 1)
+    offs = offsets(tb)
+    uj = [sum(1 << tgt_pos[jb] for jb in range(6) if (j >> (5 - jb)) & 1) for j in range(64)]
+    schunk = [scatter(512 * s, sbits) for s in range(16)]
+    out = [s.copy() for s in states]
+    tiles = (1 << (n - 6)) // cols
+    cross = np.zeros((128, 128)) if adj else None
+    B = np.array([[image_read(bimg, nn, k) for k in range(128)] for nn in range(128)])
+    for t in range(tiles):
+        c0 = t * cols
+        tbase = insert_zero_bits(c0, tb)
+        stage = [np.full(chunks * 2, np.nan, dtype=np.complex128) for _ in range(2 if adj else 1)]
+        for tid in range(256):
+            a_tid = scatter(2 * tid, sbits)
+            for s in range(16):
+                st, sl = (s >> 3, s & 7) if adj else (0, s)
+                c = tid + 256 * sl
+                g = tbase + a_tid + schunk[sl]
+                assert g == tbase + scatter(2 * c, sbits) and g % 2 == 0 and g + 1 < (1 << n)
+                ph = stage_chunk(c)
+                assert 0 <= ph < chunks
+                assert np.isnan(stage[st][2 * ph])
+                stage[st][2 * ph] = states[st][0, g]
+                stage[st][2 * ph + 1] = states[st][0, g + 1]
+        aimg = np.full(IMG // 2, np.nan)
+        for tid in range(256):
+            crow = tid & 127
+            ccol = crow & 63 if adj else crow
+            st = crow >> 6 if adj else 0
+            ucol = sum(1 << col_pos[b] for b in range(6 if adj else 7) if (ccol >> b) & 1)
+            for s in range(8):
+                q = (tid >> 7) + 2 * s
+                o = sw128_off(crow, q)
+                for r in range(4):
+                    u = ucol | uj[4 * q + r]
+                    a = stage[st][stage_chunk(u >> 1) * 2 + (u & 1)]
+                    assert not np.isnan(a)
+                    aimg[(o + 4 * r) // 2] = a.real
+                    aimg[(o + 4 * r + 2) // 2] = a.imag
+        assert not np.isnan(aimg).any()
+        A = np.array([[image_read(aimg, i, k) for k in range(128)] for i in range(128)])
+        D = A @ B.T
+        if adj:  # cross term: lam rows 64..127 against psi rows 0..63
+            cross += np.array([[sum(A[64 + i, m] * A[i, nn] for i in range(64)) for nn in range(128)]
+                               for m in range(128)])
+        for tid in range(256):
+            warp, lane = tid >> 5, tid & 31
+            sub, half = warp & 3, warp >> 2
+            erow = sub * 32 + lane
+            st = erow >> 6 if adj else 0
+            ib = insert_zero_bits(erow & 63 if adj else erow, tb)
+            for col in range(half * 64, half * 64 + 64, 2):
+                j = col >> 1
+                out[st][0, tbase + ib + offs[j]] = D[erow, col] + 1j * D[erow, col + 1]
+    return out, cross
+
+
+@pytest.mark.parametrize("tb", [[13, 12, 11, 10, 9, 8], [0, 1, 2, 3, 4, 5], [2, 9, 0, 12, 5, 7]])
+def test_v2_apply_matches_oracle(tb):
+    rng = np.random.default_rng(sum(tb) + 7)
+    n = 14
+    wires = [n - 1 - b for b in tb]
+    state = rng.normal(size=(1, 1 << n)) + 1j * rng.normal(size=(1, 1 << n))
+    z = rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64))
+    u, _ = np.linalg.qr(z)
+    out, _ = emulate_v2([state], n, tb, False, build_b(u))
+    np.testing.assert_allclose(out[0], O.apply(state, u[None], wires, n), atol=1e-10)
+
+
+@pytest.mark.parametrize("tb", [[13, 12, 11, 10, 9, 8], [2, 9, 0, 12, 5, 7]])
+def test_v2_adjoint_matches_oracle(tb):
+    rng = np.random.default_rng(sum(tb) + 11)
+    n = 14
+    wires = [n - 1 - b for b in tb]
+    psi = rng.normal(size=(1, 1 << n)) + 1j * rng.normal(size=(1, 1 << n))
+    lam = rng.normal(size=(1, 1 << n)) + 1j * rng.normal(size=(1, 1 << n))
+    z = rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64))
+    u, _ = np.linalg.qr(z)
+    uh = u.conj().T
+    (po, lo), cross = emulate_v2([psi, lam], n, tb, True, build_b(uh))
+    np.testing.assert_allclose(po, O.apply(psi, uh[None], wires, n), atol=1e-10)
+    np.testing.assert_allclose(lo, O.apply(lam, uh[None], wires, n), atol=1e-10)
+    # M[j][j'] = sum_cols lam[j] conj(psi[j'])
+    d = cross.reshape(64, 2, 64, 2)
+    m = (d[:, 0, :, 0] + d[:, 1, :, 1]) + 1j * (d[:, 1, :, 0] - d[:, 0, :, 1])
+    offs = offsets(tb)
+    ref = np.zeros((64, 64), dtype=complex)
+    for c in range(1 << (n - 6)):
+        base = insert_zero_bits(c, tb)
+        lv = lam[0, [base + offs[j] for j in range(64)]]
+        pv = psi[0, [base + offs[j] for j in range(64)]]
+        ref += np.outer(lv, pv.conj())
+    np.testing.assert_allclose(m, ref, atol=1e-9)

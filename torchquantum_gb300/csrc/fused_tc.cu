@@ -127,19 +127,6 @@ __device__ __forceinline__ uint32_t sw128_off(int r, int chunk) {
   return kb * kKBlockBytes + (r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4);
 }
 
-struct ApplyParams {
-  float2* state;
-  int n;
-  int64_t bsz;
-  BitInsert ins;             // the 6 target bits
-  uint64_t off[64];          // amplitude offset of target pattern j (j bit 5 = tb[0])
-  const uint8_t* uimg;       // [u_batch][2 images][32 KB]
-  int64_t u_batch;
-  int64_t tiles_per_row;
-  int64_t tiles;
-  int* status;
-};
-
 __device__ __forceinline__ uint32_t pack_bf2(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&v);
@@ -158,34 +145,6 @@ __device__ __forceinline__ void split4(const float2 (&a)[4], uint4& hi, uint4& l
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Load tile t (128 columns x 64 patterns) from global, split, write A images at abuf.
-__device__ __forceinline__ void produce(const ApplyParams& p, int64_t t, uint8_t* abuf, const uint64_t* offs) {
-  const int64_t b = t / p.tiles_per_row;
-  const int64_t c0 = (t % p.tiles_per_row) * kTileCols;
-  const float2* row = p.state + (b << p.n);
-  // 2048 (column, quad) pairs; lanes on consecutive columns
-#pragma unroll
-  for (int e = threadIdx.x; e < kTileCols * 16; e += kThreads) {
-    const int i = e & (kTileCols - 1);
-    const int q = e >> 7;
-    const uint64_t base = insert_zero_bits(static_cast<uint64_t>(c0 + i), p.ins);
-    float2 a[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) a[r] = row[base + offs[4 * q + r]];
-    uint4 hi, lo;
-    split4(a, hi, lo);
-    const uint32_t o = sw128_off(i, q);
-    *reinterpret_cast<uint4*>(abuf + o) = hi;
-    *reinterpret_cast<uint4*>(abuf + kImgBytes + o) = lo;
-  }
-}
-
-__device__ __forceinline__ void load_u(const ApplyParams& p, int64_t b, uint8_t* bimg) {
-  const uint4* src = reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? b : 0) * 2 * kImgBytes);
-  uint4* dst = reinterpret_cast<uint4*>(bimg);
-  for (int i = threadIdx.x; i < 2 * kImgBytes / 16; i += kThreads) dst[i] = src[i];
-}
-
 __device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_t b_s) {
   constexpr uint32_t idesc = idesc_bf16(128, 128);
   // (A image, B image): hi.hi, hi.lo, lo.hi
@@ -202,193 +161,8 @@ __device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_
   }
 }
 
-__device__ __forceinline__ void epilogue(const ApplyParams& p, int64_t t, uint32_t d_tmem, const uint64_t* offs) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = warp & 3, half = warp >> 2;
-  const int64_t b = t / p.tiles_per_row;
-  const int64_t c0 = (t % p.tiles_per_row) * kTileCols;
-  const int i = sub * 32 + lane;
-  float2* row = p.state + (b << p.n);
-  const uint64_t base = insert_zero_bits(static_cast<uint64_t>(c0 + i), p.ins);
-#pragma unroll
-  for (int part = 0; part < 2; ++part) {
-    const int col = half * 64 + part * 32;
-    uint32_t r[32];
-    tmem_ld32(d_tmem + (static_cast<uint32_t>(sub * 32) << 16) + col, r);
-    tmem_wait_ld();
-#pragma unroll
-    for (int v = 0; v < 16; ++v) {
-      const int j = (col >> 1) + v;
-      row[base + offs[j]] = make_float2(__uint_as_float(r[2 * v]), __uint_as_float(r[2 * v + 1]));
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kThreads, 1) k_tc_apply(const ApplyParams p) {
-  extern __shared__ uint8_t smem_raw[];
-  const uint32_t raw = smem_u32(smem_raw);
-  uint8_t* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
-  uint8_t* bimg = smem;                         // 64 KB: U hi, U lo
-  uint8_t* abuf0 = smem + 2 * kImgBytes;        // 64 KB each: tile hi, tile lo
-  uint8_t* abuf1 = abuf0 + 2 * kImgBytes;
-  uint64_t* offs = reinterpret_cast<uint64_t*>(abuf1 + 2 * kImgBytes);  // 64 entries
-  uint64_t* bars = offs + 64;                   // 2 mbarriers
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
-
-  const int64_t per = (p.tiles + gridDim.x - 1) / gridDim.x;
-  const int64_t t_begin = blockIdx.x * per;
-  const int64_t t_end = min(p.tiles, t_begin + per);
-  if (t_begin >= t_end) return;  // uniform for the block
-
-  if (threadIdx.x < 64) offs[threadIdx.x] = p.off[threadIdx.x];
-  if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (threadIdx.x < 32) {  // warp 0 owns the tensor memory
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    tc_fence_before();
-  }
-  int64_t cur_b = t_begin / p.tiles_per_row;
-  load_u(p, cur_b, bimg);
-  __syncthreads();  // offsets, barriers, tmem slot visible
-  tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-  const uint32_t b_s = smem_u32(bimg);
-  uint8_t* abufs[2] = {abuf0, abuf1};
-  uint32_t phase[2] = {0u, 0u};
-  int aborted = 0;
-
-  // prologue: tile t_begin -> A[0] -> D[0]
-  produce(p, t_begin, abufs[0], offs);
-  fence_proxy_async();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    tc_fence_after();
-    issue_mma(tmem, smem_u32(abufs[0]), b_s);
-    mma_commit(&bars[0]);
-  }
-  int inflight[2] = {1, 0};
-
-  for (int64_t t = t_begin; t < t_end; ++t) {
-    const int buf = static_cast<int>((t - t_begin) & 1);
-    const bool more = t + 1 < t_end;
-    if (more && !aborted) produce(p, t + 1, abufs[buf ^ 1], offs);
-    // MMA(t) complete?  (a wait that gives up leaves the MMA marked in flight so the
-    // drain below waits for it again, bounded, before the tensor memory is freed)
-    int timed_out = 0;
-    const bool waiting = !aborted && inflight[buf];
-    if (waiting) timed_out = mbar_wait(&bars[buf], phase[buf]) ? 0 : 1;
-    const int any_timeout = __syncthreads_or(timed_out);
-    if (waiting && !any_timeout) {
-      phase[buf] ^= 1u;
-      inflight[buf] = 0;
-    }
-    if (any_timeout) {
-      if (threadIdx.x == 0) atomicExch(p.status, TQK_TIMEOUT);
-      aborted = 1;
-    }
-    tc_fence_after();
-    if (more && !aborted) {
-      const int64_t nb = (t + 1) / p.tiles_per_row;
-      if (p.u_batch > 1 && nb != cur_b) {  // per-row U: all MMAs have completed here
-        load_u(p, nb, bimg);
-        cur_b = nb;
-      }
-      fence_proxy_async();
-      tc_fence_before();
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        tc_fence_after();
-        issue_mma(tmem + static_cast<uint32_t>((buf ^ 1) * 128), smem_u32(abufs[buf ^ 1]), b_s);
-        mma_commit(&bars[buf ^ 1]);
-      }
-      inflight[buf ^ 1] = 1;
-    }
-    if (!aborted) epilogue(p, t, tmem + static_cast<uint32_t>(buf * 128), offs);
-    tc_fence_before();
-    __syncthreads();
-  }
-  // drain: bounded wait for anything still in flight, then free tensor memory
-  for (int bsel = 0; bsel < 2; ++bsel)
-    if (inflight[bsel]) mbar_wait(&bars[bsel], phase[bsel]);
-  tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
-  }
-}
-
-// ------------------------------------------------------------------ adjoint step
-// One reverse step of the adjoint method for a fused block, per tile of 128 columns:
-//   psi <- U^H psi, lam <- U^H lam   (two K-major GEMMs against the image of U^H)
-//   Mr += Lam~^T Psi~                 (the cross term, reduced over the tile's columns)
-// where Lam~ / Psi~ are the tiles' real embeddings [column][2j+p].  The cross GEMM
-// reads the same swizzled tiles as MN-major operands (M = N = 128 = (j, p), K = the
-// tile's columns, 16 per instruction: start address + 2048 B per K step, LBO = 16 KB
-// between the two 64-element (j, p) halves, SBO = 1024 B between 8-column groups).
-// Mr is flushed to float64 (atomicAdd into mr_out[row or 0][128][128]) at the end and
-// whenever a per-row U changes with the batch row; the host forms
-//   M[j][j'] = sum lam[j] conj(psi[j'])  from Mr, and the cotangent of U as M U.
-// Single-buffered: shared memory holds U^H (64 KB) and the psi and lam tiles (64 KB each).
-struct AdjParams {
-  float2* psi;
-  float2* lam;
-  int n;
-  BitInsert ins;
-  uint64_t off[64];
-  const uint8_t* uimg;   // image of U^H
-  int64_t u_batch;
-  int64_t tiles_per_row;
-  int64_t tiles;
-  double* mr_out;        // [u_batch][128][128] or null (no gradient)
-  int* status;
-};
-
-__device__ __forceinline__ void produce_rows(const float2* row, int64_t c0, const BitInsert& ins, uint8_t* abuf,
-                                             const uint64_t* offs) {
-#pragma unroll
-  for (int e = threadIdx.x; e < kTileCols * 16; e += kThreads) {
-    const int i = e & (kTileCols - 1);
-    const int q = e >> 7;
-    const uint64_t base = insert_zero_bits(static_cast<uint64_t>(c0 + i), ins);
-    float2 a[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) a[r] = row[base + offs[4 * q + r]];
-    uint4 hi, lo;
-    split4(a, hi, lo);
-    const uint32_t o = sw128_off(i, q);
-    *reinterpret_cast<uint4*>(abuf + o) = hi;
-    *reinterpret_cast<uint4*>(abuf + kImgBytes + o) = lo;
-  }
-}
-
-__device__ __forceinline__ void epilogue_rows(float2* row, int64_t c0, const BitInsert& ins, uint32_t d_tmem,
-                                              const uint64_t* offs) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = warp & 3, half = warp >> 2;
-  const int i = sub * 32 + lane;
-  const uint64_t base = insert_zero_bits(static_cast<uint64_t>(c0 + i), ins);
-#pragma unroll
-  for (int part = 0; part < 2; ++part) {
-    const int col = half * 64 + part * 32;
-    uint32_t r[32];
-    tmem_ld32(d_tmem + (static_cast<uint32_t>(sub * 32) << 16) + col, r);
-    tmem_wait_ld();
-#pragma unroll
-    for (int v = 0; v < 16; ++v) {
-      const int j = (col >> 1) + v;
-      row[base + offs[j]] = make_float2(__uint_as_float(r[2 * v]), __uint_as_float(r[2 * v + 1]));
-    }
-  }
-}
-
-// MN-major SWIZZLE_128B descriptor over a [column][128 (j,p)] tile image.
+// MN-major SWIZZLE_128B descriptor over a [column][128 (j,p)] tile image: the two
+// 64-element (j,p) halves are 16 KB apart (LBO), 8-column groups 1024 B apart (SBO).
 __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
@@ -399,18 +173,139 @@ __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr) {
   return d;
 }
 
-__device__ __forceinline__ void issue_cross(uint32_t d_tmem, uint32_t lam_s, uint32_t psi_s, bool first) {
-  // kind::f16, D fp32, bf16 A/B, A and B MN-major (bits 15, 16), M = N = 128
+// Cross term of the adjoint tile: D_M[m][n] += sum over the tile's 64 columns of
+// lam~[m] psi~[n]; lam rows are tile rows 64..127, psi rows 0..63 (K = column, MN-major).
+__device__ __forceinline__ void issue_cross(uint32_t d_tmem, uint32_t a_s, bool first) {
   constexpr uint32_t idesc = idesc_bf16(128, 128) | (1u << 15) | (1u << 16);
+  const uint32_t lam_s = a_s + 64 * 128, psi_s = a_s;
   const uint32_t ao[3] = {0u, 0u, static_cast<uint32_t>(kImgBytes)};
   const uint32_t bo[3] = {0u, static_cast<uint32_t>(kImgBytes), 0u};
 #pragma unroll
   for (int prod = 0; prod < 3; ++prod) {
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
+    for (int s = 0; s < 4; ++s) {
       const uint32_t koff = s * 2048;
       mma_bf16(d_tmem, desc_sw128_mn(lam_s + ao[prod] + koff), desc_sw128_mn(psi_s + bo[prod] + koff), idesc,
                (first && prod == 0 && s == 0) ? 0u : 1u);
+    }
+  }
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* gptr) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gptr) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Stage layout: per state a region of 4096 / 2048 16-byte chunks (compressed address
+// order, chunk c holds amplitudes 2c, 2c+1); chunk c is stored at c ^ ((c >> 5) & 31)
+// so that column-strided reads of the conversion spread over the banks.
+__device__ __forceinline__ uint32_t stage_chunk(uint32_t c) { return c ^ ((c >> 5) & 31u); }
+
+// Tile geometry.  APPLY: 128 columns of one state.  ADJ: 64 columns of psi (rows 0..63)
+// and the same 64 columns of lam (rows 64..127).
+template <bool ADJ>
+struct TileGeom {
+  static constexpr int kCols = ADJ ? 64 : 128;       // columns per state
+  static constexpr int kBits = ADJ ? 12 : 13;        // compressed bits per state
+  static constexpr int kChunks = 1 << (kBits - 1);   // 16-byte chunks per state
+  static constexpr int kStateBytes = kChunks * 16;   // 32 KB / 64 KB
+};
+
+struct TcParams {
+  float2* psi;               // state (APPLY) / psi (ADJ)
+  float2* lam;               // ADJ only
+  int n;
+  BitInsert ins;             // the 6 target bits
+  uint64_t off[64];          // amplitude offset of target pattern j (j bit 5 = tb[0])
+  int sbits[13];             // tile bits (targets + lowest column bits), ascending
+  int col_pos[7];            // position in the compressed index of column bit b
+  int tgt_pos[6];            // position in the compressed index of target bit tb[jb]
+  const uint8_t* uimg;       // [u_batch][2 images][32 KB] (U for APPLY, U^H for ADJ)
+  int64_t u_batch;
+  int64_t tiles_per_row;
+  int64_t tiles;
+  double* mr_out;            // ADJ: [u_batch][128][128] cross term, or null
+  int* status;
+};
+
+__device__ __forceinline__ uint64_t scatter_bits(uint32_t u, const int* sbits, int nb) {
+  uint64_t a = 0;
+  for (int b = 0; b < nb; ++b)
+    if ((u >> b) & 1u) a |= 1ull << sbits[b];
+  return a;
+}
+
+struct TcShared {
+  uint64_t off[64];          // target pattern offsets
+  uint32_t uj[64];           // compressed-index contribution of target pattern j
+  uint64_t schunk[16];       // scatter of 512*s (chunk offsets of the cp.async loop)
+};
+
+template <bool ADJ>
+__device__ __forceinline__ void issue_loads(const TcParams& p, int64_t t, uint32_t stage_s, uint64_t a_tid,
+                                            const TcShared& sh) {
+  using G = TileGeom<ADJ>;
+  const int64_t b = t / p.tiles_per_row;
+  const int64_t c0 = (t % p.tiles_per_row) * G::kCols;
+  const uint64_t tbase = insert_zero_bits(static_cast<uint64_t>(c0), p.ins) + (static_cast<uint64_t>(b) << p.n);
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int st = ADJ ? (s >> 3) : 0;
+    const int sl = ADJ ? (s & 7) : s;
+    const float2* base = st ? p.lam : p.psi;
+    const uint32_t c = static_cast<uint32_t>(threadIdx.x + kThreads * sl);
+    const float2* g = base + tbase + a_tid + sh.schunk[sl];
+    cp_async16(stage_s + st * G::kStateBytes + stage_chunk(c) * 16, g);
+  }
+  cp_async_commit();
+}
+
+// stage (fp32, compressed order) -> A images (bf16 hi/lo, SWIZZLE_128B K-major)
+template <bool ADJ>
+__device__ __forceinline__ void convert(const uint8_t* stage, uint8_t* abuf, uint32_t ucol, int row,
+                                        const TcShared& sh) {
+  using G = TileGeom<ADJ>;
+  const int st = ADJ ? (row >> 6) : 0;
+  const float2* sp = reinterpret_cast<const float2*>(stage + st * G::kStateBytes);
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int q = (threadIdx.x >> 7) + 2 * s;
+    float2 a[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const uint32_t u = ucol | sh.uj[4 * q + r];
+      a[r] = sp[stage_chunk(u >> 1) * 2 + (u & 1u)];
+    }
+    uint4 hi, lo;
+    split4(a, hi, lo);
+    const uint32_t o = sw128_off(row, q);
+    *reinterpret_cast<uint4*>(abuf + o) = hi;
+    *reinterpret_cast<uint4*>(abuf + kImgBytes + o) = lo;
+  }
+}
+
+template <bool ADJ>
+__device__ __forceinline__ void epilogue(const TcParams& p, int64_t t, uint32_t d_tmem, uint64_t ibase,
+                                         const TcShared& sh) {
+  using G = TileGeom<ADJ>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = warp & 3, half = warp >> 2;
+  const int64_t b = t / p.tiles_per_row;
+  const int64_t c0 = (t % p.tiles_per_row) * G::kCols;
+  const int row = sub * 32 + lane;
+  const int st = ADJ ? (row >> 6) : 0;
+  float2* base = (st ? p.lam : p.psi) + (b << p.n) + insert_zero_bits(static_cast<uint64_t>(c0), p.ins) + ibase;
+#pragma unroll
+  for (int part = 0; part < 2; ++part) {
+    const int col = half * 64 + part * 32;
+    uint32_t r[32];
+    tmem_ld32(d_tmem + (static_cast<uint32_t>(sub * 32) << 16) + col, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int v = 0; v < 16; ++v) {
+      const int j = (col >> 1) + v;
+      base[sh.off[j]] = make_float2(__uint_as_float(r[2 * v]), __uint_as_float(r[2 * v + 1]));
     }
   }
 }
@@ -430,104 +325,154 @@ __device__ __forceinline__ void flush_cross(double* dst, uint32_t d_tmem) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const AdjParams p) {
+__device__ __forceinline__ void load_u(const TcParams& p, int64_t b, uint8_t* bimg) {
+  const uint4* src = reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? b : 0) * 2 * kImgBytes);
+  uint4* dst = reinterpret_cast<uint4*>(bimg);
+  for (int i = threadIdx.x; i < 2 * kImgBytes / 16; i += kThreads) dst[i] = src[i];
+}
+
+// One kernel for the forward block application (ADJ = false) and the adjoint step
+// (ADJ = true).  Shared memory: U (or U^H) image 64 KB, A image 64 KB, raw stage 64 KB.
+// TMEM: two 128-column accumulators for the block product (+ one for the cross term).
+// Per iteration t: the loads of tile t+2 go out (cp.async) right after tile t+1 is
+// converted and its MMAs issued, so one full iteration hides their latency; the
+// epilogue of tile t overlaps the MMAs of tile t+1.
+template <bool ADJ>
+__global__ void __launch_bounds__(kThreads, 1) k_tc(const TcParams p) {
+  using G = TileGeom<ADJ>;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
-  uint8_t* bimg = smem;                        // U^H hi, lo
-  uint8_t* apsi = smem + 2 * kImgBytes;        // psi tile hi, lo
-  uint8_t* alam = apsi + 2 * kImgBytes;        // lam tile hi, lo
-  uint64_t* offs = reinterpret_cast<uint64_t*>(alam + 2 * kImgBytes);
-  uint64_t* bar = offs + 64;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  uint8_t* bimg = smem;                          // 64 KB
+  uint8_t* abuf = smem + 2 * kImgBytes;          // 64 KB
+  uint8_t* stage = abuf + 2 * kImgBytes;         // 64 KB
+  TcShared* sh = reinterpret_cast<TcShared*>(stage + 2 * kImgBytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sh + 1);  // 2 mbarriers
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
 
   const int64_t per = (p.tiles + gridDim.x - 1) / gridDim.x;
   const int64_t t_begin = blockIdx.x * per;
   const int64_t t_end = min(p.tiles, t_begin + per);
-  if (t_begin >= t_end) return;
+  if (t_begin >= t_end) return;  // uniform for the block
 
-  if (threadIdx.x < 64) offs[threadIdx.x] = p.off[threadIdx.x];
+  const uint32_t ncols_tmem = ADJ ? 512u : 256u;
+  if (threadIdx.x < 64) {
+    const int j = threadIdx.x;
+    sh->off[j] = p.off[j];
+    uint32_t u = 0;
+    for (int jb = 0; jb < 6; ++jb)
+      if ((j >> (5 - jb)) & 1) u |= 1u << p.tgt_pos[jb];
+    sh->uj[j] = u;
+  }
+  if (threadIdx.x < 16) sh->schunk[threadIdx.x] = scatter_bits(512u * threadIdx.x, p.sbits, G::kBits);
   if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(512u)
+                 "r"(ncols_tmem)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     tc_fence_before();
   }
+  // per-thread constants
+  const uint64_t a_tid = scatter_bits(2u * threadIdx.x, p.sbits, G::kBits);
+  const int crow = threadIdx.x & 127;                 // conversion row
+  const int ccol = ADJ ? (crow & 63) : crow;          // its column within the state
+  uint32_t ucol = 0;
+  for (int bb = 0; bb < (ADJ ? 6 : 7); ++bb)
+    if ((ccol >> bb) & 1) ucol |= 1u << p.col_pos[bb];
+  const int erow = (threadIdx.x >> 5 & 3) * 32 + (threadIdx.x & 31);  // epilogue row
+  const uint64_t ibase = insert_zero_bits(static_cast<uint64_t>(ADJ ? (erow & 63) : erow), p.ins);
+
   int64_t cur_b = t_begin / p.tiles_per_row;
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? cur_b : 0) * 2 * kImgBytes);
-    uint4* dst = reinterpret_cast<uint4*>(bimg);
-    for (int i = threadIdx.x; i < 2 * kImgBytes / 16; i += kThreads) dst[i] = src[i];
-  }
+  load_u(p, cur_b, bimg);
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t d_psi = tmem, d_lam = tmem + 128, d_m = tmem + 256;
-  const uint32_t b_s = smem_u32(bimg), psi_s = smem_u32(apsi), lam_s = smem_u32(alam);
-  uint32_t phase = 0;
-  int aborted = 0, inflight = 0;
+  const uint32_t d_m = tmem + 256;
+  const uint32_t b_s = smem_u32(bimg), a_s = smem_u32(abuf), stage_s = smem_u32(stage);
+  const bool want_cross = ADJ && p.mr_out != nullptr;
   bool first_cross = true;
 
-  for (int64_t t = t_begin; t < t_end && !aborted; ++t) {
-    const int64_t b = t / p.tiles_per_row;
-    const int64_t c0 = (t % p.tiles_per_row) * kTileCols;
-    if (p.u_batch > 1 && b != cur_b) {
-      // per-row U: flush the cross term of the previous row, reload U^H
-      if (p.mr_out && !first_cross) {
-        tc_fence_after();
-        flush_cross(p.mr_out + cur_b * 128 * 128, d_m);
-        first_cross = true;
-      }
-      const uint4* src = reinterpret_cast<const uint4*>(p.uimg + b * 2 * kImgBytes);
-      uint4* dst = reinterpret_cast<uint4*>(bimg);
-      for (int i = threadIdx.x; i < 2 * kImgBytes / 16; i += kThreads) dst[i] = src[i];
-      cur_b = b;
+  // prologue: tile t_begin -> A -> D[0]; loads of t_begin+1 in flight
+  issue_loads<ADJ>(p, t_begin, stage_s, a_tid, *sh);
+  cp_async_wait_all();
+  __syncthreads();
+  convert<ADJ>(stage, abuf, ucol, crow, *sh);
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    issue_mma(tmem, a_s, b_s);
+    if (want_cross) issue_cross(d_m, a_s, true);
+    mma_commit(&bars[0]);
+  }
+  if (want_cross) first_cross = false;
+  // stage is free again once every thread's conversion is done (barrier above)
+  if (t_begin + 1 < t_end) issue_loads<ADJ>(p, t_begin + 1, stage_s, a_tid, *sh);
+  uint32_t phase[2] = {0u, 0u};
+  int inflight[2] = {1, 0};
+  int aborted = 0;
+
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    const int buf = static_cast<int>((t - t_begin) & 1);
+    const bool more = t + 1 < t_end;
+    if (more) cp_async_wait_all();
+    int timed_out = 0;
+    const bool waiting = !aborted && inflight[buf];
+    if (waiting) timed_out = mbar_wait(&bars[buf], phase[buf]) ? 0 : 1;
+    const int any_timeout = __syncthreads_or(timed_out);
+    if (waiting && !any_timeout) {
+      phase[buf] ^= 1u;
+      inflight[buf] = 0;
     }
-    float2* prow = p.psi + (b << p.n);
-    float2* lrow = p.lam + (b << p.n);
-    produce_rows(prow, c0, p.ins, apsi, offs);
-    produce_rows(lrow, c0, p.ins, alam, offs);
-    fence_proxy_async();
-    tc_fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      tc_fence_after();
-      issue_mma(d_psi, psi_s, b_s);
-      issue_mma(d_lam, lam_s, b_s);
-      if (p.mr_out) issue_cross(d_m, lam_s, psi_s, first_cross);
-      mma_commit(bar);
-    }
-    inflight = 1;
-    first_cross = false;
-    const int timed_out = mbar_wait(bar, phase) ? 0 : 1;
-    if (__syncthreads_or(timed_out)) {
+    if (any_timeout) {
       if (threadIdx.x == 0) atomicExch(p.status, TQK_TIMEOUT);
       aborted = 1;
-      break;
     }
-    phase ^= 1u;
-    inflight = 0;
     tc_fence_after();
-    epilogue_rows(prow, c0, p.ins, d_psi, offs);
-    epilogue_rows(lrow, c0, p.ins, d_lam, offs);
+    if (more && !aborted) {
+      const int64_t nb = (t + 1) / p.tiles_per_row;
+      if (nb != cur_b) {  // a new batch row: flush its cross term, reload a per-row U
+        if (want_cross) {
+          flush_cross(p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, d_m);
+          first_cross = true;
+        }
+        if (p.u_batch > 1) load_u(p, nb, bimg);
+        cur_b = nb;
+      }
+      convert<ADJ>(stage, abuf, ucol, crow, *sh);
+      fence_proxy_async();
+      tc_fence_before();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tc_fence_after();
+        issue_mma(tmem + static_cast<uint32_t>((buf ^ 1) * 128), a_s, b_s);
+        if (want_cross) issue_cross(d_m, a_s, first_cross);
+        mma_commit(&bars[buf ^ 1]);
+      }
+      first_cross = false;
+      inflight[buf ^ 1] = 1;
+      if (t + 2 < t_end) issue_loads<ADJ>(p, t + 2, stage_s, a_tid, *sh);
+    }
+    if (!aborted) epilogue<ADJ>(p, t, tmem + static_cast<uint32_t>(buf * 128), ibase, *sh);
     tc_fence_before();
     __syncthreads();
   }
-  if (aborted && inflight) mbar_wait(bar, phase);
-  if (!aborted && p.mr_out && !first_cross) {
-    tc_fence_after();
-    flush_cross(p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, d_m);
-  }
+  cp_async_wait_all();
+  for (int bsel = 0; bsel < 2; ++bsel)
+    if (inflight[bsel]) mbar_wait(&bars[bsel], phase[bsel]);
+  tc_fence_after();
+  if (want_cross && !aborted && !first_cross) flush_cross(p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, d_m);
   tc_fence_before();
   __syncthreads();
   if (threadIdx.x < 32) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_tmem) : "memory");
   }
 }
 
@@ -582,6 +527,67 @@ extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, void* image, vo
   return launch_status("tqk_fused_prepare");
 }
 
+namespace {
+
+int tc_setup(tqk::tc::TcParams& p, int64_t bsz, int n, const int32_t* wires, bool adj, const char* what) {
+  using namespace tqk;
+  int tb[6];
+  uint64_t used = 0;
+  int rc = wires_to_bits(n, wires, 6, tb, &used, what);
+  if (rc) return rc;
+  p.n = n;
+  p.ins = make_insert(used);
+  for (int j = 0; j < 64; ++j) {
+    uint64_t o = 0;
+    for (int jb = 0; jb < 6; ++jb)
+      if ((j >> (5 - jb)) & 1) o |= 1ull << tb[jb];
+    p.off[j] = o;
+  }
+  // tile bits: the 6 targets + the lowest 7 (apply) / 6 (adjoint) column bits
+  const int ncolbits = adj ? 6 : 7;
+  int colbits[7];
+  int nc = 0;
+  for (int q = 0; q < n && nc < ncolbits; ++q)
+    if (!(used & (1ull << q))) colbits[nc++] = q;
+  uint64_t smask = used;
+  for (int i = 0; i < nc; ++i) smask |= 1ull << colbits[i];
+  int ns = 0;
+  for (int q = 0; q < 64 && ns < 13; ++q)
+    if (smask & (1ull << q)) p.sbits[ns++] = q;
+  for (int i = ns; i < 13; ++i) p.sbits[i] = 0;
+  auto pos_of = [&](int bit) {
+    for (int i = 0; i < ns; ++i)
+      if (p.sbits[i] == bit) return i;
+    return -1;
+  };
+  for (int i = 0; i < 7; ++i) p.col_pos[i] = i < nc ? pos_of(colbits[i]) : 0;
+  for (int jb = 0; jb < 6; ++jb) p.tgt_pos[jb] = pos_of(tb[jb]);
+  const int cols = adj ? 64 : 128;
+  p.tiles_per_row = (1ll << (n - 6)) / cols;
+  p.tiles = p.tiles_per_row * bsz;
+  return TQK_OK;
+}
+
+int tc_launch(const tqk::tc::TcParams& p, bool adj, void* stream, const char* what) {
+  using namespace tqk;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = 1024 + 6 * tc::kImgBytes + sizeof(tc::TcShared) + 2 * 8 + 16;
+  static int attr_dev[2] = {-1, -1};
+  if (attr_dev[adj] != dev) {
+    if (adj) cudaFuncSetAttribute(tc::k_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    else cudaFuncSetAttribute(tc::k_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    attr_dev[adj] = dev;
+  }
+  const int64_t grid = p.tiles < sms ? p.tiles : sms;
+  if (adj) tc::k_tc<true><<<static_cast<unsigned>(grid), tc::kThreads, smem, as_stream(stream)>>>(p);
+  else tc::k_tc<false><<<static_cast<unsigned>(grid), tc::kThreads, smem, as_stream(stream)>>>(p);
+  return launch_status(what);
+}
+
+}  // namespace
+
 extern "C" int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires,
                                  const void* image_h, int64_t u_batch, double* mr_out, int* status, void* stream) {
   const char* what = "tqk_fused_adjoint";
@@ -591,38 +597,15 @@ extern "C" int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const
   if ((rc = check_batch(u_batch, bsz, what))) return rc;
   if (!image_h || !status) return fail(TQK_BAD_POINTER, "%s: null image/status", what);
   if (n < 13) return fail(TQK_UNSUPPORTED, "%s: needs n_wires >= 13 (got %d)", what, n);
-  int tb[6];
-  uint64_t used = 0;
-  if ((rc = wires_to_bits(n, wires, 6, tb, &used, what))) return rc;
-  tc::AdjParams p;
+  tc::TcParams p;
   p.psi = static_cast<float2*>(psi);
   p.lam = static_cast<float2*>(lam);
-  p.n = n;
-  p.ins = make_insert(used);
-  for (int j = 0; j < 64; ++j) {
-    uint64_t o = 0;
-    for (int jb = 0; jb < 6; ++jb)
-      if ((j >> (5 - jb)) & 1) o |= 1ull << tb[jb];
-    p.off[j] = o;
-  }
   p.uimg = static_cast<const uint8_t*>(image_h);
   p.u_batch = u_batch;
-  p.tiles_per_row = (1ll << (n - 6)) / tc::kTileCols;
-  p.tiles = p.tiles_per_row * bsz;
   p.mr_out = mr_out;
   p.status = status;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = 1024 + 6 * tc::kImgBytes + 64 * 8 + 8 + 16;
-  static int attr_dev = -1;
-  if (attr_dev != dev) {
-    cudaFuncSetAttribute(tc::k_tc_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    attr_dev = dev;
-  }
-  const int64_t grid = p.tiles < sms ? p.tiles : sms;
-  tc::k_tc_adjoint<<<static_cast<unsigned>(grid), tc::kThreads, smem, as_stream(stream)>>>(p);
-  return launch_status(what);
+  if ((rc = tc_setup(p, bsz, n, wires, true, what))) return rc;
+  return tc_launch(p, true, stream, what);
 }
 
 extern "C" int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
@@ -634,35 +617,13 @@ extern "C" int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* w
   if (!image || !status) return fail(TQK_BAD_POINTER, "%s: null image/status", what);
   if ((reinterpret_cast<uintptr_t>(image) & 15u) != 0) return fail(TQK_BAD_POINTER, "%s: image alignment", what);
   if (n < 13) return fail(TQK_UNSUPPORTED, "%s: needs n_wires >= 13 (got %d)", what, n);
-  int tb[6];
-  uint64_t used = 0;
-  if ((rc = wires_to_bits(n, wires, 6, tb, &used, what))) return rc;
-  tc::ApplyParams p;
-  p.state = static_cast<float2*>(state);
-  p.n = n;
-  p.bsz = bsz;
-  p.ins = make_insert(used);
-  for (int j = 0; j < 64; ++j) {
-    uint64_t o = 0;
-    for (int jb = 0; jb < 6; ++jb)
-      if ((j >> (5 - jb)) & 1) o |= 1ull << tb[jb];
-    p.off[j] = o;
-  }
+  tc::TcParams p;
+  p.psi = static_cast<float2*>(state);
+  p.lam = nullptr;
   p.uimg = static_cast<const uint8_t*>(image);
   p.u_batch = u_batch;
-  p.tiles_per_row = (1ll << (n - 6)) / tc::kTileCols;
-  p.tiles = p.tiles_per_row * bsz;
+  p.mr_out = nullptr;
   p.status = status;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = 1024 + 6 * tc::kImgBytes + 64 * 8 + 2 * 8 + 16;
-  static int attr_dev = -1;
-  if (attr_dev != dev) {
-    cudaFuncSetAttribute(tc::k_tc_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    attr_dev = dev;
-  }
-  const int64_t grid = p.tiles < sms ? p.tiles : sms;
-  tc::k_tc_apply<<<static_cast<unsigned>(grid), tc::kThreads, smem, as_stream(stream)>>>(p);
-  return launch_status(what);
+  if ((rc = tc_setup(p, bsz, n, wires, false, what))) return rc;
+  return tc_launch(p, false, stream, what);
 }
