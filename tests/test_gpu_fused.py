@@ -118,9 +118,15 @@ def test_dense_k_wire_adjoint_vs_fd(kw):
     assert np.abs(ut.grad.cpu().numpy()[0] - gnum).max() < 1e-4
 
 
-@pytest.mark.parametrize("n,bsz,per_row", [(13, 1, False), (14, 3, True), (16, 2, False), (14, 2, True)])
+@pytest.mark.parametrize(
+    "n,bsz,per_row", [(13, 1, False), (14, 3, True), (16, 2, False), (14, 2, True), (20, 3, True), (20, 3, False)]
+)
 def test_tensor_core_block_vs_cuda_cores(n, bsz, per_row):
-    """The tcgen05 split-BF16 kernel against the CUDA-core dense kernel on random 6-wire unitaries."""
+    """The tcgen05 split-BF16 kernel against the CUDA-core dense kernel on random 6-wire unitaries.
+
+    n = 20, bsz = 3 gives every CTA several tiles (accumulator and A-buffer reuse) and a
+    batch-row change inside a CTA (per-row U reload).
+    """
     from torchquantum_gb300 import _lib
 
     rng = np.random.default_rng(n * 10 + bsz)
@@ -159,7 +165,9 @@ def test_fused_tensor_core_circuit_vs_oracle():
     assert np.abs(got - O.run(n, bsz, gates)).max() < 1e-5
 
 
-@pytest.mark.parametrize("n,bsz,per_row", [(13, 1, False), (14, 3, True), (15, 2, False)])
+@pytest.mark.parametrize(
+    "n,bsz,per_row", [(13, 1, False), (14, 3, True), (15, 2, False), (20, 3, True), (20, 3, False)]
+)
 def test_tensor_core_adjoint_vs_cuda_cores(n, bsz, per_row):
     """tcgen05 adjoint step (psi, lam <- U^H, cotangent M U) against the CUDA-core dense adjoint."""
     from torchquantum_gb300 import _lib

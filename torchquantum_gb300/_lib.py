@@ -269,10 +269,11 @@ def fused_adjoint(psi, lam, n, wires, image_h, u_batch, mr_out):
 
 
 def cross_to_complex(mr: torch.Tensor) -> torch.Tensor:
-    """[B, 128, 128] real cross term -> M [B, 64, 64] complex128, M[j][j'] = sum lam[j] conj(psi[j'])."""
-    d = mr.view(-1, 64, 2, 64, 2)
-    re = d[:, :, 0, :, 0] + d[:, :, 1, :, 1]
-    im = d[:, :, 1, :, 0] - d[:, :, 0, :, 1]
+    """[B, 128, 128] real cross term (rows/cols 64p + j, p = 0 real part, 1 imaginary part)
+    -> M [B, 64, 64] complex128, M[j][j'] = sum over columns of lam[j] conj(psi[j'])."""
+    d = mr.view(-1, 2, 64, 2, 64)
+    re = d[:, 0, :, 0, :] + d[:, 1, :, 1, :]
+    im = d[:, 1, :, 0, :] - d[:, 0, :, 1, :]
     return torch.complex(re, im)
 
 
