@@ -375,15 +375,16 @@ def roofline(args, dev):
         rng = np.random.default_rng(0)
         z = rng.normal(size=(bsz, 64, 64)) + 1j * rng.normal(size=(bsz, 64, 64))
         u = torch.tensor(np.linalg.qr(z)[0], dtype=torch.complex128, device=dev)
-        img = _lib.fused_prepare(u)
-        imgh = _lib.fused_prepare(u.conj().transpose(-1, -2).contiguous())
-        mr = torch.zeros(bsz, 128, 128, dtype=torch.float64, device=dev)
         wsets = [[int(x) for x in np.random.default_rng(i).choice(n, 6, replace=False)] for i in range(reps + 3)]
+        imgs = [_lib.fused_prepare(u, w) for w in wsets]
+        imghs = [_lib.fused_prepare(u.conj().transpose(-1, -2).contiguous(), w) for w in wsets]
+        mr = torch.zeros(bsz, 128, 128, dtype=torch.float64, device=dev)
         tiles = bsz * (1 << (n - 6)) // 128
         fl_apply = tiles * 24 * 128 * 128 * 16 * 2
         extra = {
-            "fused6_tc_fwd": (lambda i: _lib.fused_apply(psi, n, wsets[i], img, bsz), 2 * S, fl_apply),
-            "fused6_tc_adj": (lambda i: _lib.fused_adjoint(psi, lam, n, wsets[i], imgh, bsz, mr), 4 * S, 3 * fl_apply),
+            "fused6_tc_fwd": (lambda i: _lib.fused_apply(psi, n, wsets[i], imgs[i], bsz), 2 * S, fl_apply),
+            "fused6_tc_adj": (lambda i: _lib.fused_adjoint(psi, lam, n, wsets[i], imghs[i], bsz, mr), 4 * S,
+                              3 * fl_apply),
         }
         for name, (fn, nbytes, flops) in extra.items():
             t = timeit(fn)

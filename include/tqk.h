@@ -147,16 +147,18 @@ int tqk_adjoint_diagonal(void* psi, void* lam, int64_t bsz, int n, const int32_t
  *
  * tqk_fused_prepare converts U (complex128 [u_batch, 64, 64], row-major, rows = output
  * pattern, wires[0] the most significant bit) into the operand image the kernel reads
- * (tqk_fused_image_bytes(u_batch) bytes, 16-byte aligned).  tqk_fused_apply needs
+ * (tqk_fused_image_bytes(u_batch) bytes, 16-byte aligned).  The image is laid out for
+ * the block's target bits: pass the same 6 wires (in the same order) that the image
+ * will be applied on; only their relative order matters.  tqk_fused_apply needs
  * n >= 13; u_batch is 1 or bsz.  `status` is a device int: the kernel writes
  * TQK_TIMEOUT there if one of its bounded waits gives up (it then stops early). */
 int64_t tqk_fused_image_bytes(int64_t u_batch);
-int tqk_fused_prepare(const void* u, int64_t u_batch, void* image, void* stream);
+int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream);
 int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
                     int64_t u_batch, int* status, void* stream);
 
 /* Adjoint step of a fused block on the tensor cores: psi <- U^H psi, lam <- U^H lam
- * (image_h = tqk_fused_prepare of U^H), and, if mr_out != NULL, the real cross term
+ * (image_h = tqk_fused_prepare of U^H on the same wires), and, if mr_out != NULL, the real cross term
  * mr_out[g][2j+p][2j'+q] += sum over columns of Re/Im parts lam_{j,p} * psi_{j',q}
  * (float64, g = batch row if u_batch == bsz > 1 else 0; zeroed by the caller), from
  * which M[j][j'] = sum lam[j] conj(psi[j']) and the cotangent of U, M U, follow.

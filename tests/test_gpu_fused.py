@@ -146,7 +146,7 @@ def test_tensor_core_block_vs_cuda_cores(n, bsz, per_row):
         st = torch.tensor(s, dtype=torch.complex64, device="cuda")
         ref = st.clone()
         _lib.apply_matrix(ref, n, wires, u128.to(torch.complex64).contiguous(), b)
-        img = _lib.fused_prepare(u128)
+        img = _lib.fused_prepare(u128, wires)
         _lib.fused_apply(st, n, wires, img, b)
         torch.cuda.synchronize()
         _lib.check_status(st.device)
@@ -193,7 +193,7 @@ def test_tensor_core_adjoint_vs_cuda_cores(n, bsz, per_row):
         _lib.adjoint_matrix(psi_r, lam_r, n, wires, u.to(torch.complex64).contiguous(), b, g_ref)
         uh = u.conj().transpose(-1, -2).contiguous()
         mr = torch.zeros(b, 128, 128, dtype=torch.float64, device="cuda")
-        _lib.fused_adjoint(psi, lam, n, wires, _lib.fused_prepare(uh), b, mr)
+        _lib.fused_adjoint(psi, lam, n, wires, _lib.fused_prepare(uh, wires), b, mr)
         torch.cuda.synchronize()
         _lib.check_status(psi.device)
         assert (psi - psi_r).abs().max().item() < 2e-5 * psi_r.abs().max().item()

@@ -56,7 +56,7 @@ _SIGS = {
     "tqk_adjoint_phase": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_fused_image_bytes": (_i64, [_i64]),
-    "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp]),
+    "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp, _vp]),
     "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
     "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
     "tqk_pauli_expval_noalloc_capacity": (_i64, []),
@@ -249,12 +249,13 @@ def check_status(device) -> None:
         raise TQKError(v, "a tensor-core kernel gave up waiting on its pipeline (bounded wait timed out)")
 
 
-def fused_prepare(u128: torch.Tensor) -> torch.Tensor:
-    """complex128 [B, 64, 64] -> operand image (uint8 tensor) for fused_apply."""
+def fused_prepare(u128: torch.Tensor, wires: Sequence[int]) -> torch.Tensor:
+    """complex128 [B, 64, 64] -> operand image (uint8 tensor) for fused_apply /
+    fused_adjoint on the same 6 wires (the image's layout follows their bit positions)."""
     lib = load()
     b = int(u128.shape[0])
     img = torch.empty(lib.tqk_fused_image_bytes(b), dtype=torch.uint8, device=u128.device)
-    _check(lib.tqk_fused_prepare(u128.data_ptr(), b, img.data_ptr(), _stream(u128)))
+    _check(lib.tqk_fused_prepare(u128.data_ptr(), b, _i32(wires), img.data_ptr(), _stream(u128)))
     return img
 
 

@@ -37,8 +37,8 @@ namespace tc {
 
 constexpr int kImgBytes = 32768;        // one 128-row x 128-K bf16 A image
 constexpr int kKBlockBytes = 16384;     // A: 128 rows x 128 B (64 bf16 of K)
-constexpr int kBImgBytes = 16384;       // one 64-row x 128-K bf16 B image
-constexpr int kBKBlockBytes = 8192;     // B: 64 rows x 128 B
+constexpr int kBImgBytes = 32768;       // one 128-row x 128-K bf16 B image
+constexpr int kBKBlockBytes = 16384;    // B: 128 rows x 128 B
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -144,22 +144,23 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4& hi, uint4& lo
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Block product into D (two 64-column halves: re at d, im at d + 64); 48 MMAs.
-__device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_t b_s) {
-  constexpr uint32_t idesc = idesc_bf16(128, 64);
-  constexpr uint32_t idesc_neg = idesc | (1u << 13);  // negate A
-  const uint32_t ao[3] = {0u, 0u, static_cast<uint32_t>(kImgBytes)};
-  const uint32_t bo[3] = {0u, static_cast<uint32_t>(kBImgBytes), 0u};
+// Block product: 24 MMAs of 128x128x16 (three split-bf16 terms x 8 K-steps).
+// Row-major orientation (tr = false): D[i][m] = sum_K A[i][K] B[m][K] -- TMEM lane =
+// tile row i, column m = 2 j' + q.  Transposed (tr = true): the operands swap roles,
+// D[m][i] -- TMEM lane m, column i.
+__device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_t b_s, bool tr) {
+  constexpr uint32_t idesc = idesc_bf16(128, 128);
+  const uint32_t ao[3] = {0u, 0u, static_cast<uint32_t>(kImgBytes)};   // x: hi, hi, lo
+  const uint32_t bo[3] = {0u, static_cast<uint32_t>(kBImgBytes), 0u};  // U: hi, lo, hi
 #pragma unroll
   for (int prod = 0; prod < 3; ++prod) {
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
       const int kb = s >> 2;
       const uint32_t koff = (s & 3) * 32;
-      const uint64_t ad = desc_sw128(a_s + ao[prod] + kb * kKBlockBytes + koff);
-      const uint32_t acc = (prod > 0 || s > 0) ? 1u : 0u;
-      mma_bf16(d_tmem, ad, desc_sw128(b_s + bo[prod] + kb * kBKBlockBytes + koff), kb ? idesc_neg : idesc, acc);
-      mma_bf16(d_tmem + 64, ad, desc_sw128(b_s + bo[prod] + (kb ^ 1) * kBKBlockBytes + koff), idesc, acc);
+      const uint64_t xd = desc_sw128(a_s + ao[prod] + kb * kKBlockBytes + koff);
+      const uint64_t ud = desc_sw128(b_s + bo[prod] + kb * kBKBlockBytes + koff);
+      mma_bf16(d_tmem, tr ? ud : xd, tr ? xd : ud, idesc, (prod > 0 || s > 0) ? 1u : 0u);
     }
   }
 }
@@ -208,23 +209,47 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Pattern orders.  The natural index of a target pattern has wires[0] as its most
+// significant bit.  Inside the kernels two other orders are used, both fixed by the
+// target bits' positions alone: the output order o (bit b = the b-th lowest target bit)
+// indexes output rows, and the K order jk (bit b = the b-th highest target bit) indexes
+// the K dimension of the operand images, so that a 16-byte image chunk (K bits 0-2)
+// always spans the three highest target bits.  tqk_fused_prepare builds U's image in
+// these orders.
+//
+// A tile is a sub-cube of 13 free dimensions: the 6 target bits, the lowest 7 other
+// bits (tile row = column i; ADJ: the lowest 6, plus a psi/lam dimension that selects
+// the state and adds 64 to the row).  Producer thread (warp w, lane l) holds 32
+// amplitudes r = e + 8c: e = K bits 0-2 (one chunk), c = two more dimensions; its lanes
+// run over the 5 lowest-address remaining dimensions, so every load instruction is
+// coalesced whatever the target bits are.
 struct TcParams {
   float2* psi;               // state (APPLY) / psi (ADJ)
   float2* lam;               // ADJ only
   int n;
   BitInsert ins;             // the 6 target bits
-  uint64_t off[64];          // amplitude offset of target pattern j (j bit 5 = tb[0])
-  const uint8_t* uimg;       // [u_batch][2 images][16 KB] (U for APPLY, U^H for ADJ)
+  const uint8_t* uimg;       // [u_batch][2 images][32 KB] (U for APPLY, U^H for ADJ)
   int64_t u_batch;
-  int64_t tiles_per_row;
+  int64_t tiles_per_row;     // a power of two
+  int tpr_log2;
   int64_t tiles;
   double* mr_out;            // ADJ: [u_batch][128][128] cross term, or null
   int* status;
+  int transposed;            // output orientation (fewer store sectors per warp)
+  uint64_t off[64];          // amplitude offset of output pattern j'
+  uint64_t col_off[128];     // amplitude offset of tile row i (ADJ: i & 63)
+  uint64_t lane_off[32];     // producer mapping: offsets, tile rows and chunk indices
+  uint64_t warp_off[8];
+  uint64_t reg_off[32];
+  uint8_t lane_row[32], lane_g[32];
+  uint8_t warp_row[8], warp_g[8], warp_lam[8];
+  uint8_t c_row[4], c_g[4];
+  uint8_t nat_of_k[64];      // natural pattern index of K-order index jk (cross term)
 };
 
-// Warp roles: warps 0-7 produce A images (two threads per tile row), warps 8-11 drain
-// the tensor-memory accumulators (warp w reads TMEM lanes 32*(w%4)...), warp 12 owns
-// the tensor memory and lane 0 of it issues the MMAs.
+// Warp roles (416 threads): warps 0-7 produce A images, warps 8-11 drain the tensor-
+// memory accumulators (warp w reads TMEM lanes 32*(w%4)...), warp 12 owns the tensor
+// memory and lane 0 of it issues the MMAs.
 constexpr int kProdThreads = 256;
 constexpr int kEpiThreads = 128;
 constexpr int kThreadsWS = kProdThreads + kEpiThreads + 32;
@@ -233,7 +258,6 @@ constexpr int kABufs = 2;
 
 struct Sync {
   uint64_t a_full[kABufs], a_empty[kABufs], d_full[2], d_empty[2], x_full, x_empty;
-  uint64_t off[64];
   uint32_t tmem_base;
   int abort;
 };
@@ -256,34 +280,28 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, Sy
   return __all_sync(0xffffffffu, ok);
 }
 
-template <bool ADJ>
-struct TileGeom {
-  static constexpr int kCols = ADJ ? 64 : 128;  // columns per state in a tile
-};
+// amplitude offset of tile t within its state (batch row + fixed column bits)
+__device__ __forceinline__ int64_t tile_base(const TcParams& p, int64_t t, bool adj) {
+  const int cols = adj ? 64 : 128;
+  const int64_t b = t >> p.tpr_log2;
+  const int64_t c0 = (t & (p.tiles_per_row - 1)) * cols;
+  return (b << p.n) + static_cast<int64_t>(insert6(static_cast<uint64_t>(c0), p.ins));
+}
 
-// Producer: half gh of row `row` of the A image (column `row` of the state for APPLY;
-// psi column row or lam column row-64 for ADJ).  The 32 amplitudes of target patterns
-// 32*gh .. 32*gh+31 come straight from global memory (a warp's lanes are consecutive
-// columns), are split into bf16 hi/lo and stored at K = 64p + j.
-template <bool ADJ>
-__device__ __forceinline__ void produce_row(const TcParams& p, const Sync* sy, int64_t t, uint8_t* abuf, int row,
-                                            int gh, uint64_t ibase) {
-  using G = TileGeom<ADJ>;
-  const int64_t b = t / p.tiles_per_row;
-  const int64_t c0 = (t % p.tiles_per_row) * G::kCols;
-  const float2* src = ((ADJ && row >= 64) ? p.lam : p.psi) + (b << p.n) +
-                      insert6(static_cast<uint64_t>(c0), p.ins) + ibase;
+// Producer: load the thread's 32 amplitudes of tile t, split them into bf16 hi/lo and
+// store its four 16-byte chunks (K = 64p + 8g + e) into the A image.
+__device__ __forceinline__ void produce_tile(const TcParams& p, const float2* src, uint8_t* abuf, int row0, int g0) {
   float2 a[32];
 #pragma unroll
-  for (int e = 0; e < 32; ++e) a[e] = __ldcs(src + sy->off[32 * gh + e]);
+  for (int r = 0; r < 32; ++r) a[r] = __ldcs(src + p.reg_off[r]);
 #pragma unroll
-  for (int h = 0; h < 4; ++h) {
-    const int g = 4 * gh + h;
+  for (int c = 0; c < 4; ++c) {
+    const int row = row0 + p.c_row[c], g = g0 + p.c_g[c];
     float re[8], im[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-      re[e] = a[8 * h + e].x;
-      im[e] = a[8 * h + e].y;
+      re[e] = a[8 * c + e].x;
+      im[e] = a[8 * c + e].y;
     }
     uint4 hi, lo;
     split8(re, hi, lo);
@@ -297,42 +315,64 @@ __device__ __forceinline__ void produce_row(const TcParams& p, const Sync* sy, i
   }
 }
 
+// Row-major drain: TMEM lane = tile row; columns 2j' + q hold part q of output j'.
 template <bool ADJ>
-__device__ __forceinline__ void epilogue_tile(const TcParams& p, const Sync* sy, int64_t t, uint32_t d_tmem,
-                                              int sub, int lane, uint64_t ibase) {
-  using G = TileGeom<ADJ>;
-  const int64_t b = t / p.tiles_per_row;
-  const int64_t c0 = (t % p.tiles_per_row) * G::kCols;
+__device__ __forceinline__ void drain_rows(const TcParams& p, int64_t tb, uint32_t d_tmem, int sub, int lane) {
   const int row = sub * 32 + lane;
-  float2* dst = ((ADJ && row >= 64) ? p.lam : p.psi) + (b << p.n) + insert6(static_cast<uint64_t>(c0), p.ins) + ibase;
+  float2* dst = ((ADJ && row >= 64) ? p.lam : p.psi) + tb + p.col_off[row];
   const uint32_t lanes = static_cast<uint32_t>(sub * 32) << 16;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    uint32_t re[16], im[16];
-    tmem_ld16(d_tmem + lanes + q * 16, re);
-    tmem_ld16(d_tmem + lanes + 64 + q * 16, im);
+    uint32_t v[32];
+    tmem_ld16(d_tmem + lanes + q * 32, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
+    tmem_ld16(d_tmem + lanes + q * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
     tmem_wait_ld();
 #pragma unroll
-    for (int v = 0; v < 16; ++v)
-      __stcs(dst + sy->off[q * 16 + v], make_float2(__uint_as_float(re[v]), __uint_as_float(im[v])));
+    for (int h = 0; h < 16; ++h)
+      __stcs(dst + p.off[q * 16 + h], make_float2(__uint_as_float(v[2 * h]), __uint_as_float(v[2 * h + 1])));
   }
 }
 
-__device__ __forceinline__ void flush_cross(double* dst, uint32_t d_tmem, int sub, int lane) {
+// Transposed drain: TMEM lane m = 2j' + q, columns = tile rows; lanes of a warp write 16
+// consecutive outputs' real and imaginary parts.
+template <bool ADJ>
+__device__ __forceinline__ void drain_cols(const TcParams& p, int64_t tb, uint32_t d_tmem, int sub, int lane) {
   const int m = sub * 32 + lane;
   const uint32_t lanes = static_cast<uint32_t>(sub * 32) << 16;
+  const int64_t o = tb + static_cast<int64_t>(p.off[m >> 1]);
+  float* dpsi = reinterpret_cast<float*>(p.psi + o) + (m & 1);
+  float* dlam = ADJ ? reinterpret_cast<float*>(p.lam + o) + (m & 1) : nullptr;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    uint32_t v[16];
+    tmem_ld16(d_tmem + lanes + q * 16, v);
+    tmem_wait_ld();
+    float* d = (ADJ && q >= 4) ? dlam : dpsi;
+#pragma unroll
+    for (int h = 0; h < 16; ++h) __stcs(d + 2 * p.col_off[q * 16 + h], __uint_as_float(v[h]));
+  }
+}
+
+// Cross term (K-order rows and columns 64p + jk) added into dst in natural order.
+__device__ __forceinline__ void flush_cross(const TcParams& p, double* dst, uint32_t d_tmem, int sub, int lane) {
+  const int m = sub * 32 + lane;
+  const uint32_t lanes = static_cast<uint32_t>(sub * 32) << 16;
+  double* drow = dst + ((m & 64) + p.nat_of_k[m & 63]) * 128;
 #pragma unroll
   for (int part = 0; part < 8; ++part) {
     uint32_t r[16];
     tmem_ld16(d_tmem + lanes + part * 16, r);
     tmem_wait_ld();
 #pragma unroll
-    for (int v = 0; v < 16; ++v) atomicAdd(dst + m * 128 + part * 16 + v, static_cast<double>(__uint_as_float(r[v])));
+    for (int v = 0; v < 16; ++v) {
+      const int c = part * 16 + v;
+      atomicAdd(drow + (c & 64) + p.nat_of_k[c & 63], static_cast<double>(__uint_as_float(r[v])));
+    }
   }
 }
 
 // Warp-specialised kernel for the forward block application (ADJ = false) and the
-// adjoint step (ADJ = true).  Shared memory: U (U^H) image 32 KB + kABufs A images of
+// adjoint step (ADJ = true).  Shared memory: U (U^H) image 64 KB + two A images of
 // 64 KB.  Hand-offs: a_full/a_empty (producers <-> MMA), d_full/d_empty (MMA <->
 // epilogue, two accumulators), x_full/x_empty (adjoint cross term of a finished row).
 template <bool ADJ>
@@ -340,7 +380,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
-  uint8_t* bimg = smem;                    // 32 KB
+  uint8_t* bimg = smem;                    // 64 KB
   uint8_t* abufs = smem + 2 * kBImgBytes;  // kABufs x 64 KB
   Sync* sy = reinterpret_cast<Sync*>(abufs + kABufs * 2 * kImgBytes);
 
@@ -353,8 +393,8 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
   const uint32_t ncols_tmem = ADJ ? 512u : 256u;
   const bool want_cross = ADJ && p.mr_out != nullptr;
   const bool flush_per_row = want_cross && p.u_batch > 1;
+  const bool tr = p.transposed != 0;
 
-  if (threadIdx.x < 64) sy->off[threadIdx.x] = p.off[threadIdx.x];
   if (threadIdx.x == 0) {
     for (int i = 0; i < kABufs; ++i) {
       mbar_init(&sy->a_full[i], kProdThreads);
@@ -376,7 +416,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     // U (or U^H) image of the first row
     const uint4* src =
-        reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? t_begin / p.tiles_per_row : 0) * 2 * kBImgBytes);
+        reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? (t_begin >> p.tpr_log2) : 0) * 2 * kBImgBytes);
     uint4* dstb = reinterpret_cast<uint4*>(bimg);
     for (int i = lane; i < 2 * kBImgBytes / 16; i += 32) dstb[i] = src[i];
     fence_proxy_async();
@@ -388,30 +428,30 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
 
   if (threadIdx.x < kProdThreads) {
     // ------------------------------------------------------------ producers
-    const int row = threadIdx.x & 127, gh = threadIdx.x >> 7;
-    const uint64_t ibase = insert6(static_cast<uint64_t>(ADJ ? (row & 63) : row), p.ins);
+    const int64_t toff = static_cast<int64_t>(p.lane_off[lane] + p.warp_off[warp]);
+    const int row0 = p.lane_row[lane] + p.warp_row[warp];
+    const int g0 = p.lane_g[lane] + p.warp_g[warp];
+    const float2* base = (ADJ && p.warp_lam[warp]) ? p.lam : p.psi;
     for (int64_t k = 0; k < ntiles; ++k) {
       const int buf = static_cast<int>(k % kABufs);
       if (k >= kABufs && !wait_or_abort(&sy->a_empty[buf], static_cast<uint32_t>((k / kABufs - 1) & 1), sy)) break;
-      produce_row<ADJ>(p, sy, t_begin + k, abufs + buf * 2 * kImgBytes, row, gh, ibase);
+      produce_tile(p, base + tile_base(p, t_begin + k, ADJ) + toff, abufs + buf * 2 * kImgBytes, row0, g0);
       fence_proxy_async();
       mbar_arrive(&sy->a_full[buf]);
     }
   } else if (warp < kMmaWarp) {
     // ------------------------------------------------------------ epilogue
     const int sub = warp & 3;
-    const int row = sub * 32 + lane;
-    const uint64_t ibase = insert6(static_cast<uint64_t>(ADJ ? (row & 63) : row), p.ins);
-    int64_t cur_b = t_begin / p.tiles_per_row;
+    int64_t cur_b = t_begin >> p.tpr_log2;
     uint32_t xphase = 0;
     bool ok = true;
     for (int64_t k = 0; k < ntiles; ++k) {
       const int64_t t = t_begin + k;
-      const int64_t b = t / p.tiles_per_row;
+      const int64_t b = t >> p.tpr_log2;
       if (flush_per_row && b != cur_b) {
         if (!(ok = wait_or_abort(&sy->x_full, xphase, sy))) break;
         tc_fence_after();
-        flush_cross(p.mr_out + cur_b * 128 * 128, tmem + 256, sub, lane);
+        flush_cross(p, p.mr_out + cur_b * 128 * 128, tmem + 256, sub, lane);
         tc_fence_before();
         mbar_arrive(&sy->x_empty);
         xphase ^= 1u;
@@ -420,24 +460,26 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
       const int d = static_cast<int>(k & 1);
       if (!(ok = wait_or_abort(&sy->d_full[d], static_cast<uint32_t>((k >> 1) & 1), sy))) break;
       tc_fence_after();
-      epilogue_tile<ADJ>(p, sy, t, tmem + static_cast<uint32_t>(d * 128), sub, lane, ibase);
+      const uint32_t dt = tmem + static_cast<uint32_t>(d * 128);
+      if (tr) drain_cols<ADJ>(p, tile_base(p, t, ADJ), dt, sub, lane);
+      else drain_rows<ADJ>(p, tile_base(p, t, ADJ), dt, sub, lane);
       tc_fence_before();
       mbar_arrive(&sy->d_empty[d]);
     }
     if (ok && want_cross && wait_or_abort(&sy->x_full, xphase, sy)) {
       tc_fence_after();
-      flush_cross(p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, tmem + 256, sub, lane);
+      flush_cross(p, p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, tmem + 256, sub, lane);
       tc_fence_before();
     }
   } else {
     // ------------------------------------------------------------ MMA issuer
-    int64_t cur_b = t_begin / p.tiles_per_row;
+    int64_t cur_b = t_begin >> p.tpr_log2;
     bool first_cross = true;
     uint32_t xphase = 0;
     int64_t issued = 0;
     for (int64_t k = 0; k < ntiles; ++k) {
       const int64_t t = t_begin + k;
-      const int64_t b = t / p.tiles_per_row;
+      const int64_t b = t >> p.tpr_log2;
       if (b != cur_b) {
         if (flush_per_row) {  // hand the finished row's cross term to the epilogue warps
           if (lane == 0) mma_commit(&sy->x_full);
@@ -463,7 +505,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
       tc_fence_after();
       if (lane == 0) {
         const uint32_t a_s = smem_u32(abufs + buf * 2 * kImgBytes);
-        issue_mma(tmem + static_cast<uint32_t>(d * 128), a_s, smem_u32(bimg));
+        issue_mma(tmem + static_cast<uint32_t>(d * 128), a_s, smem_u32(bimg), tr);
         if (want_cross) issue_cross(tmem + 256, a_s, first_cross);
         mma_commit(&sy->a_empty[buf]);
         mma_commit(&sy->d_full[d]);
@@ -489,23 +531,56 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
   }
 }
 
-// U (complex128 [u_batch][64][64], row-major) -> hi/lo bf16 images of the B operand
-// expected by k_tc: row j' = output pattern, K = 64p + j holds part p (Re, Im) of
-// U[j'][j], SWIZZLE_128B K-major.  One thread per (batch, row, 16-byte chunk).
-__global__ void k_tc_prep(const double2* u, int64_t u_batch, uint8_t* img) {
+struct PatternOrders {
+  uint8_t nat_of_out[64];  // natural index of output-order index o
+  uint8_t nat_of_k[64];    // natural index of K-order index jk
+};
+
+// Output and K orders of a block from its wires: the wire with the largest number is the
+// lowest target bit.
+__host__ PatternOrders pattern_orders(const int32_t* wires) {
+  int asc[6];  // asc[b] = position jb in `wires` of the b-th lowest target bit
+  for (int i = 0; i < 6; ++i) asc[i] = i;
+  for (int x = 1; x < 6; ++x)
+    for (int y = x; y > 0 && wires[asc[y - 1]] < wires[asc[y]]; --y) {
+      const int t = asc[y];
+      asc[y] = asc[y - 1];
+      asc[y - 1] = t;
+    }
+  PatternOrders o;
+  for (int x = 0; x < 64; ++x) {
+    int no = 0, nk = 0;
+    for (int b = 0; b < 6; ++b) {
+      if ((x >> b) & 1) {
+        no |= 1 << (5 - asc[b]);
+        nk |= 1 << (5 - asc[5 - b]);
+      }
+    }
+    o.nat_of_out[x] = static_cast<uint8_t>(no);
+    o.nat_of_k[x] = static_cast<uint8_t>(nk);
+  }
+  return o;
+}
+
+// U (complex128 [u_batch][64][64], row-major, natural order) -> hi/lo bf16 images of the
+// U operand expected by k_tc (SWIZZLE_128B K-major, 128 rows, K = 64p + jk): row 2o holds
+// [Re U[o][jk] | -Im U[o][jk]], row 2o+1 holds [Im U[o][jk] | Re U[o][jk]] (o, jk in
+// the output and K orders), so one N = 128 product with a tile [Re x | Im x] gives the
+// real and imaginary parts of (U x)[o] side by side.  One thread per (batch, row,
+// 16-byte chunk).
+__global__ void k_tc_prep(const double2* u, int64_t u_batch, uint8_t* img, const PatternOrders ord) {
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= u_batch * 64 * 16) return;
-  const int64_t b = idx / (64 * 16);
-  const int row = static_cast<int>((idx / 16) % 64);
+  if (idx >= u_batch * 128 * 16) return;
+  const int64_t b = idx / (128 * 16);
+  const int row = static_cast<int>((idx / 16) % 128);
   const int chunk = static_cast<int>(idx % 16);
-  const double2* ub = u + b * 64 * 64;
+  const double2* ub = u + b * 64 * 64 + ord.nat_of_out[row >> 1] * 64;
   float hv[8], lv[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int kk = chunk * 8 + e;
-    const int part = kk >> 6, j = kk & 63;
-    const double2 z = ub[row * 64 + j];
-    const double v = part ? z.y : z.x;
+    const double2 z = ub[ord.nat_of_k[kk & 63]];
+    const double v = (row & 1) == 0 ? (kk < 64 ? z.x : -z.y) : (kk < 64 ? z.y : z.x);
     const __nv_bfloat16 h = __double2bfloat16(v);
     hv[e] = __bfloat162float(h);
     lv[e] = static_cast<float>(v - static_cast<double>(hv[e]));
@@ -525,35 +600,136 @@ using namespace tqk;
 
 extern "C" int64_t tqk_fused_image_bytes(int64_t u_batch) { return u_batch * 2 * tc::kBImgBytes; }
 
-extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, void* image, void* stream) {
-  if (!u || !image) return fail(TQK_BAD_POINTER, "tqk_fused_prepare: null pointer");
+extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream) {
+  if (!u || !image || !wires) return fail(TQK_BAD_POINTER, "tqk_fused_prepare: null pointer");
   if ((reinterpret_cast<uintptr_t>(image) & 15u) != 0)
     return fail(TQK_BAD_POINTER, "tqk_fused_prepare: image must be 16-byte aligned");
   if (u_batch < 1) return fail(TQK_BAD_SHAPE, "tqk_fused_prepare: u_batch must be >= 1");
-  const int64_t work = u_batch * 64 * 16;
+  for (int i = 0; i < 6; ++i) {
+    if (wires[i] < 0) return fail(TQK_BAD_WIRES, "tqk_fused_prepare: negative wire %d", wires[i]);
+    for (int k = 0; k < i; ++k)
+      if (wires[k] == wires[i]) return fail(TQK_BAD_WIRES, "tqk_fused_prepare: wire %d used twice", wires[i]);
+  }
+  const int64_t work = u_batch * 128 * 16;
   tc::k_tc_prep<<<static_cast<unsigned>((work + 255) / 256), 256, 0, as_stream(stream)>>>(
-      static_cast<const double2*>(u), u_batch, static_cast<uint8_t*>(image));
+      static_cast<const double2*>(u), u_batch, static_cast<uint8_t*>(image), tc::pattern_orders(wires));
   return launch_status("tqk_fused_prepare");
 }
 
 namespace {
 
+// One free dimension of a tile and what it adds to an amplitude offset, the tile row
+// (i, plus 64 for lam), the image chunk index g (pattern bits 3-5) and the state choice.
+struct TileDim {
+  int addr;  // address bit (-1: the psi/lam dimension)
+  uint64_t off;
+  int row, g, lam;
+};
+
 int tc_setup(tqk::tc::TcParams& p, int64_t bsz, int n, const int32_t* wires, bool adj, const char* what) {
   using namespace tqk;
-  int tb[6];
   uint64_t used = 0;
-  int rc = wires_to_bits(n, wires, 6, tb, &used, what);
+  int rc = wires_to_bits(n, wires, 6, nullptr, &used, what);
   if (rc) return rc;
   p.n = n;
   p.ins = make_insert(used);
-  for (int j = 0; j < 64; ++j) {
-    uint64_t o = 0;
-    for (int jb = 0; jb < 6; ++jb)
-      if ((j >> (5 - jb)) & 1) o |= 1ull << tb[jb];
-    p.off[j] = o;
+  int tasc[6];  // target bits ascending
+  for (int i = 0, q = 0; q < n; ++q)
+    if ((used >> q) & 1ull) tasc[i++] = q;
+  for (int o = 0; o < 64; ++o) {  // output order: bit b = b-th lowest target bit
+    uint64_t x = 0;
+    for (int b = 0; b < 6; ++b)
+      if ((o >> b) & 1) x |= 1ull << tasc[b];
+    p.off[o] = x;
   }
-  const int cols = adj ? 64 : 128;
-  p.tiles_per_row = (1ll << (n - 6)) / cols;
+  const tc::PatternOrders ord = tc::pattern_orders(wires);
+  for (int x = 0; x < 64; ++x) p.nat_of_k[x] = ord.nat_of_k[x];
+  auto koff = [&](int jk) {  // K order: bit b = b-th highest target bit
+    uint64_t x = 0;
+    for (int b = 0; b < 6; ++b)
+      if ((jk >> b) & 1) x |= 1ull << tasc[5 - b];
+    return x;
+  };
+  const int ncol = adj ? 6 : 7;
+  int colbit[7], nc = 0;
+  for (int q = 0; q < n && nc < ncol; ++q)
+    if (!((used >> q) & 1ull)) colbit[nc++] = q;
+  for (int i = 0; i < 128; ++i) {
+    const int ii = adj ? (i & 63) : i;
+    uint64_t o = 0;
+    for (int c = 0; c < ncol; ++c)
+      if ((ii >> c) & 1) o |= 1ull << colbit[c];
+    p.col_off[i] = o;
+  }
+  // Producer mapping.  Register bits 0-2: K bits 0-2 (the three highest target bits);
+  // the remaining address dimensions sorted by address bit: 5 lanes, 2 register bits,
+  // the rest warp bits; ADJ adds the psi/lam dimension as the top warp bit.
+  TileDim rest[10];
+  int nr = 0;
+  for (int b = 3; b < 6; ++b) rest[nr++] = {tasc[5 - b], 1ull << tasc[5 - b], 0, 1 << (b - 3), 0};
+  for (int c = 0; c < ncol; ++c) rest[nr++] = {colbit[c], 1ull << colbit[c], 1 << c, 0, 0};
+  for (int x = 1; x < nr; ++x)  // insertion sort by address bit
+    for (int y = x; y > 0 && rest[y - 1].addr > rest[y].addr; --y) {
+      const TileDim t = rest[y];
+      rest[y] = rest[y - 1];
+      rest[y - 1] = t;
+    }
+  TileDim wdim[3];
+  int nw = 0;
+  for (int x = 7; x < nr; ++x) wdim[nw++] = rest[x];
+  if (adj) wdim[nw++] = {-1, 0, 64, 0, 1};
+  for (int l = 0; l < 32; ++l) {
+    uint64_t o = 0;
+    int row = 0, g = 0;
+    for (int bb = 0; bb < 5; ++bb)
+      if ((l >> bb) & 1) {
+        o += rest[bb].off;
+        row += rest[bb].row;
+        g += rest[bb].g;
+      }
+    p.lane_off[l] = o;
+    p.lane_row[l] = static_cast<uint8_t>(row);
+    p.lane_g[l] = static_cast<uint8_t>(g);
+  }
+  for (int w = 0; w < 8; ++w) {
+    uint64_t o = 0;
+    int row = 0, g = 0, lam = 0;
+    for (int bb = 0; bb < 3; ++bb)
+      if ((w >> bb) & 1) {
+        o += wdim[bb].off;
+        row += wdim[bb].row;
+        g += wdim[bb].g;
+        lam |= wdim[bb].lam;
+      }
+    p.warp_off[w] = o;
+    p.warp_row[w] = static_cast<uint8_t>(row);
+    p.warp_g[w] = static_cast<uint8_t>(g);
+    p.warp_lam[w] = static_cast<uint8_t>(lam);
+  }
+  for (int c = 0; c < 4; ++c) {
+    p.c_row[c] = static_cast<uint8_t>(((c & 1) ? rest[5].row : 0) + ((c & 2) ? rest[6].row : 0));
+    p.c_g[c] = static_cast<uint8_t>(((c & 1) ? rest[5].g : 0) + ((c & 2) ? rest[6].g : 0));
+  }
+  for (int r = 0; r < 32; ++r) {
+    uint64_t o = koff(r & 7);  // K bits 0-2
+    if (r & 8) o += rest[5].off;
+    if (r & 16) o += rest[6].off;
+    p.reg_off[r] = o;
+  }
+  // Output orientation: 32-byte sectors one warp store touches -- row-major: 32
+  // consecutive tile rows of one output; transposed: both parts of 16 consecutive outputs.
+  auto distinct_sectors = [](const uint64_t* o, int m) {
+    int cnt = 0;
+    for (int x = 0; x < m; ++x) {
+      bool seen = false;
+      for (int y = 0; y < x && !seen; ++y) seen = (o[y] >> 2) == (o[x] >> 2);
+      cnt += !seen;
+    }
+    return cnt;
+  };
+  p.transposed = distinct_sectors(p.off, 16) < distinct_sectors(p.col_off, 32) ? 1 : 0;
+  p.tiles_per_row = (1ll << (n - 6)) / (adj ? 64 : 128);
+  p.tpr_log2 = n - 6 - (adj ? 6 : 7);
   p.tiles = p.tiles_per_row * bsz;
   return TQK_OK;
 }

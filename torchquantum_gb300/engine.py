@@ -125,7 +125,7 @@ def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: O
     cotangent of U as M U with M = sum over columns of lam conj(psi)^T (U unitary),
     added into ``grad`` (float64 interleaved view of a complex128 [batch, 64, 64])."""
     u = u128.detach()
-    img_h = _lib.fused_prepare(kernel_operand(u.conj().transpose(-1, -2)))
+    img_h = _lib.fused_prepare(kernel_operand(u.conj().transpose(-1, -2)), wires)
     mr = None
     if grad is not None:
         mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=psi.device)

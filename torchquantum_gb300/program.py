@@ -245,7 +245,7 @@ class Segment:
         _lib.block_build(bt, len(bdescs), maxb, ot, dev)
         for blk in self.blocks:
             if blk.tc:
-                blk.image = _lib.fused_prepare(blk.u128)
+                blk.image = _lib.fused_prepare(blk.u128, blk.wires)
             else:
                 blk.operand = blk.u128.to(torch.complex64)
         # keep operands of non-native members alive in complex128
