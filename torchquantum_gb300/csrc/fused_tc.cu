@@ -258,6 +258,7 @@ constexpr int kABufs = 2;
 
 struct Sync {
   uint64_t a_full[kABufs], a_empty[kABufs], d_full[2], d_empty[2], x_full, x_empty;
+  int nat_of_k[128];      // natural row/column of cross-term index 64p + jk
   uint32_t tmem_base;
   int abort;
 };
@@ -293,7 +294,7 @@ __device__ __forceinline__ int64_t tile_base(const TcParams& p, int64_t t, bool 
 __device__ __forceinline__ void produce_tile(const TcParams& p, const float2* src, uint8_t* abuf, int row0, int g0) {
   float2 a[32];
 #pragma unroll
-  for (int r = 0; r < 32; ++r) a[r] = __ldcs(src + p.reg_off[r]);
+  for (int r = 0; r < 32; ++r) a[r] = src[p.reg_off[r]];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const int row = row0 + p.c_row[c], g = g0 + p.c_g[c];
@@ -354,20 +355,18 @@ __device__ __forceinline__ void drain_cols(const TcParams& p, int64_t tb, uint32
 }
 
 // Cross term (K-order rows and columns 64p + jk) added into dst in natural order.
-__device__ __forceinline__ void flush_cross(const TcParams& p, double* dst, uint32_t d_tmem, int sub, int lane) {
+__device__ __forceinline__ void flush_cross(const Sync* sy, double* dst, uint32_t d_tmem, int sub, int lane) {
   const int m = sub * 32 + lane;
   const uint32_t lanes = static_cast<uint32_t>(sub * 32) << 16;
-  double* drow = dst + ((m & 64) + p.nat_of_k[m & 63]) * 128;
-#pragma unroll
+  double* drow = dst + sy->nat_of_k[m] * 128;
+#pragma unroll 1
   for (int part = 0; part < 8; ++part) {
     uint32_t r[16];
     tmem_ld16(d_tmem + lanes + part * 16, r);
     tmem_wait_ld();
 #pragma unroll
-    for (int v = 0; v < 16; ++v) {
-      const int c = part * 16 + v;
-      atomicAdd(drow + (c & 64) + p.nat_of_k[c & 63], static_cast<double>(__uint_as_float(r[v])));
-    }
+    for (int v = 0; v < 16; ++v)
+      atomicAdd(drow + sy->nat_of_k[part * 16 + v], static_cast<double>(__uint_as_float(r[v])));
   }
 }
 
@@ -395,6 +394,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
   const bool flush_per_row = want_cross && p.u_batch > 1;
   const bool tr = p.transposed != 0;
 
+  if (threadIdx.x < 128) sy->nat_of_k[threadIdx.x] = (threadIdx.x & 64) + p.nat_of_k[threadIdx.x & 63];
   if (threadIdx.x == 0) {
     for (int i = 0; i < kABufs; ++i) {
       mbar_init(&sy->a_full[i], kProdThreads);
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
       if (flush_per_row && b != cur_b) {
         if (!(ok = wait_or_abort(&sy->x_full, xphase, sy))) break;
         tc_fence_after();
-        flush_cross(p, p.mr_out + cur_b * 128 * 128, tmem + 256, sub, lane);
+        flush_cross(sy, p.mr_out + cur_b * 128 * 128, tmem + 256, sub, lane);
         tc_fence_before();
         mbar_arrive(&sy->x_empty);
         xphase ^= 1u;
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
     }
     if (ok && want_cross && wait_or_abort(&sy->x_full, xphase, sy)) {
       tc_fence_after();
-      flush_cross(p, p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, tmem + 256, sub, lane);
+      flush_cross(sy, p.mr_out + (p.u_batch > 1 ? cur_b : 0) * 128 * 128, tmem + 256, sub, lane);
       tc_fence_before();
     }
   } else {
@@ -568,7 +568,7 @@ __host__ PatternOrders pattern_orders(const int32_t* wires) {
 // the output and K orders), so one N = 128 product with a tile [Re x | Im x] gives the
 // real and imaginary parts of (U x)[o] side by side.  One thread per (batch, row,
 // 16-byte chunk).
-__global__ void k_tc_prep(const double2* u, int64_t u_batch, uint8_t* img, const PatternOrders ord) {
+__global__ void k_tc_prep(const double2* u, int64_t u_batch, uint8_t* img, const __grid_constant__ PatternOrders ord) {
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= u_batch * 128 * 16) return;
   const int64_t b = idx / (128 * 16);
