@@ -383,7 +383,8 @@ __global__ void k_block_build(const tqk_block_desc* blocks, const tqk_block_op* 
 
 // grad of op (operand cotangent) = sum over rows/cols of X[row][col] conj(W[row'][col]) restricted
 // to the op's structure; W = product of the ops before it, X = (ops after)^H dL/dU.
-__device__ void op_cotangent(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+// One sweep per entry: ops outside the specialised shapes below.
+__device__ void op_cotangent_generic(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
   const int nw = op.nw, nc = op.nctrl;
   uint32_t cmask = 0, tmask = 0;
   for (int j = 0; j < nc; ++j) cmask |= 1u << op.pos[j];
@@ -443,6 +444,151 @@ __device__ void op_cotangent(const C2* X, const C2* W, int D, const tqk_block_op
       }
     }
     __syncthreads();
+  }
+}
+
+// Row r with zeros inserted at the (ascending) bit positions pos[0..m).
+__device__ __forceinline__ int insert_zeros(int r, const int* pos, int m) {
+  for (int j = 0; j < m; ++j) r = ((r >> pos[j]) << (pos[j] + 1)) | (r & ((1 << pos[j]) - 1));
+  return r;
+}
+
+// Sum of NE complex partial sums over the block; entries added (or stored) into gout.
+template <int NE>
+__device__ void block_reduce_entries(double (&acc)[2 * NE], double2* gout, int nent, bool accumulate) {
+  __shared__ double red[8][2 * 16];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 2 * NE; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * nent) {
+    double t = 0.0;
+    for (int w = 0; w < nwarps; ++w) t += red[w][threadIdx.x];
+    double* g = reinterpret_cast<double*>(gout) + threadIdx.x;
+    if (accumulate) atomicAdd(g, t);
+    else *g = t;
+  }
+  __syncthreads();
+}
+
+// Cotangent of the op's operand from X (cotangent rows) and W (state rows):
+// entry (a, b) = sum over rows r with the op's control bits set and target pattern a, and
+// columns c, of X[r][c] conj(W[r with target pattern b][c]) (diagonal ops: a = b over
+// all op bits; phase ops: the single all-ones pattern).  One sweep over (row with the op's
+// bits cleared, column) pairs evaluates every entry.
+template <int KT>
+__device__ void cot_dense(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+  constexpr int DT = 1 << KT, NE = DT * DT;
+  const int nc = op.nctrl;
+  uint32_t cmask = 0;
+  for (int j = 0; j < nc; ++j) cmask |= 1u << op.pos[j];
+  int tbit[KT], tsorted[KT];
+#pragma unroll
+  for (int j = 0; j < KT; ++j) tbit[j] = op.pos[nc + j];  // j = 0 is the pattern's most significant bit
+#pragma unroll
+  for (int j = 0; j < KT; ++j) tsorted[j] = tbit[j];
+  if (KT == 2 && tsorted[0] > tsorted[1]) {
+    const int t = tsorted[0];
+    tsorted[0] = tsorted[1];
+    tsorted[1] = t;
+  }
+  int pat[DT];
+#pragma unroll
+  for (int a = 0; a < DT; ++a) {
+    int r = 0;
+#pragma unroll
+    for (int j = 0; j < KT; ++j)
+      if ((a >> (KT - 1 - j)) & 1) r |= 1 << tbit[j];
+    pat[a] = r;
+  }
+  double acc[2 * NE];
+#pragma unroll
+  for (int q = 0; q < 2 * NE; ++q) acc[q] = 0.0;
+  const int nbase = D >> KT;
+  for (int w = threadIdx.x; w < nbase * D; w += blockDim.x) {
+    const int c = w % D;
+    const int r = insert_zeros(w / D, tsorted, KT);
+    if ((static_cast<uint32_t>(r) & cmask) != cmask) continue;
+    C2 xs[DT], ws[DT];
+#pragma unroll
+    for (int a = 0; a < DT; ++a) {
+      xs[a] = X[(r | pat[a]) * D + c];
+      ws[a] = W[(r | pat[a]) * D + c];
+    }
+#pragma unroll
+    for (int a = 0; a < DT; ++a)
+#pragma unroll
+      for (int b2 = 0; b2 < DT; ++b2) {
+        acc[2 * (a * DT + b2)] += xs[a].x * ws[b2].x + xs[a].y * ws[b2].y;  // x * conj(w)
+        acc[2 * (a * DT + b2) + 1] += xs[a].y * ws[b2].x - xs[a].x * ws[b2].y;
+      }
+  }
+  block_reduce_entries<NE>(acc, gout, NE, accumulate);
+}
+
+// Diagonal ops (entries = pattern over all NW op bits) and phase ops (one entry: all bits set).
+template <int NW>
+__device__ void cot_diag(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate,
+                         bool phase) {
+  constexpr int DT = 1 << NW;
+  int bit[NW], srt[NW];
+#pragma unroll
+  for (int j = 0; j < NW; ++j) srt[j] = bit[j] = op.pos[j];
+  if (NW == 2 && srt[0] > srt[1]) {
+    const int t = srt[0];
+    srt[0] = srt[1];
+    srt[1] = t;
+  }
+  int pat[DT];
+#pragma unroll
+  for (int a = 0; a < DT; ++a) {
+    int r = 0;
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+      if ((a >> (NW - 1 - j)) & 1) r |= 1 << bit[j];
+    pat[a] = r;
+  }
+  double acc[2 * DT];
+#pragma unroll
+  for (int q = 0; q < 2 * DT; ++q) acc[q] = 0.0;
+  const int nbase = D >> NW;
+  for (int w = threadIdx.x; w < nbase * D; w += blockDim.x) {
+    const int c = w % D;
+    const int r = insert_zeros(w / D, srt, NW);
+#pragma unroll
+    for (int a = 0; a < DT; ++a) {
+      if (phase && a != DT - 1) continue;
+      const C2 xv = X[(r | pat[a]) * D + c], wv = W[(r | pat[a]) * D + c];
+      acc[2 * a] += xv.x * wv.x + xv.y * wv.y;
+      acc[2 * a + 1] += xv.y * wv.x - xv.x * wv.y;
+    }
+  }
+  if (phase) {  // the single entry sits at index DT - 1
+    acc[0] = acc[2 * (DT - 1)];
+    acc[1] = acc[2 * (DT - 1) + 1];
+  }
+  block_reduce_entries<DT>(acc, gout, phase ? 1 : DT, accumulate);
+}
+
+__device__ void op_cotangent(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+  const int kt = op.nw - op.nctrl;
+  const bool diag = op.kind == TQK_K_PHASE || op.kind == TQK_K_DIAG;
+  if ((diag && (op.nw < 1 || op.nw > 4)) || (!diag && (kt < 1 || kt > 2))) {
+    op_cotangent_generic(X, W, D, op, gout, accumulate);
+  } else if (diag) {
+    const bool phase = op.kind == TQK_K_PHASE;
+    if (op.nw == 1) cot_diag<1>(X, W, D, op, gout, accumulate, phase);
+    else if (op.nw == 2) cot_diag<2>(X, W, D, op, gout, accumulate, phase);
+    else if (op.nw == 3) cot_diag<3>(X, W, D, op, gout, accumulate, phase);
+    else cot_diag<4>(X, W, D, op, gout, accumulate, phase);
+  } else if (kt == 1) {
+    cot_dense<1>(X, W, D, op, gout, accumulate);
+  } else {
+    cot_dense<2>(X, W, D, op, gout, accumulate);
   }
 }
 

@@ -131,7 +131,9 @@ def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: O
         mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=psi.device)
     _lib.fused_adjoint(psi, lam, n, wires, img_h, batch, mr)
     if grad is not None:
-        gu = torch.matmul(_lib.cross_to_complex(mr), u)
+        # M carries fp32 accuracy (tensor-memory accumulation), so M U in complex64 loses
+        # nothing and avoids the slow float64 path
+        gu = torch.matmul(_lib.cross_to_complex(mr).to(torch.complex64), u.to(torch.complex64))
         torch.view_as_complex(grad.view(-1, 2)).view(u.shape).add_(gu)
 
 
