@@ -33,6 +33,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "fwd+bwd circuits/s fused+adjoint vs plain at <=1e-5 vs FP64; HBM GB/s per gate"
+
+# DRAM traffic (read + write bytes) of one tensor-core adjoint launch, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on a smaller case of the same kernel
+# (n_wires=22, bsz=8, per-row U); the kernel streams every amplitude of psi and lam once,
+# so traffic scales with the amplitudes processed.
+ADJ_TRAFFIC_CAPTURE = {"n": 22, "bsz": 8, "dram_bytes": 539.099648e6 + 477.703168e6}
 UNIT = "circuits/s"
 
 
@@ -392,14 +398,20 @@ def roofline(args, dev):
             res[name] = {"us": t * 1e6, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak,
                          "tensor_TFLOP/s": flops / t / 1e12}
         _lib.check_status(dev)
+    traffic = None
     if args.method == "fused" and "fused6_tc_adj" in res:
         dom = res["fused6_tc_adj"]
-        kname = "tqk::tc::k_tc_adjoint (adjoint step of a fused 6-wire block, tcgen05 split-BF16)"
+        kname = "tqk::tc::k_tc<true> (adjoint step of a fused 6-wire block, tcgen05 split-BF16)"
+        cap = ADJ_TRAFFIC_CAPTURE
+        traffic = cap["dram_bytes"] * (bsz << n) / (cap["bsz"] << cap["n"])
     else:
         dom = res["dense1_adj"]
         kname = "k_dense_adj<2> (adjoint step of a dense 1-wire gate)"
     roof = {"bound": "hbm", "achieved": dom["GB/s"], "peak": peak, "unit": "GB/s", "frac": dom["GB/s"] / peak,
-            "traffic": None, "kernel": kname, "peak_source": f"{peak_kind} hbm_gbs"}
+            "traffic": traffic, "algorithmic_bytes": dom["bytes"], "kernel": kname,
+            "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=22, bsz=8, scaled by amplitudes"
+            if traffic is not None else None}
     return roof, res
 
 
