@@ -60,10 +60,9 @@ def parse_args():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from torchquantum_gb300.replicas import rank_env
+
+    return rank_env()
 
 
 # ------------------------------------------------------------------ CPU (oracle) leg
@@ -199,12 +198,12 @@ class ClockSampler:
 def run_ours(args):
     import torch
 
+    from torchquantum_gb300 import replicas as R
+
     rank, world, local = dist_env()
     if world > 1:
-        import torch.distributed as dist
-
         torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        R.init("nccl")
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import torchquantum_gb300 as tq
@@ -213,7 +212,7 @@ def run_ours(args):
 
     n, bsz = args.n, args.bsz
     gates, ncols = W.random_circuit(n, args.depth, seed=0)
-    theta_host = W.random_params(bsz, ncols, seed=1 + rank)
+    theta_host = W.random_params(bsz, ncols, seed=R.rank_seed(1, rank))
     paulis = W.random_paulis(n, 8, seed=2)
     pw = torch.tensor(np.random.default_rng(3).normal(size=(1, 8)), dtype=torch.float32, device=dev)
     theta_dev = torch.tensor(theta_host, device=dev)
@@ -229,9 +228,7 @@ def run_ours(args):
         (ev * pw).sum().backward()
         return ev, pr
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    barrier = R.barrier
 
     th = theta_dev.clone().requires_grad_(True)
     for _ in range(args.warmup):
@@ -251,12 +248,8 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     launches = _lib.LAUNCHES[0] - launches0
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t.item())
-    value = bsz * args.steps * world / (ms / 1e3)
+    ms = R.max_over_ranks(e0.elapsed_time(e1), dev)
+    value = R.job_throughput(bsz * args.steps, world, ms / 1e3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": _config(args, args.method),
@@ -278,12 +271,8 @@ def run_ours(args):
             step(th, "plain")
         e1.record(stream)
         torch.cuda.synchronize()
-        ms_plain = e0.elapsed_time(e1)
-        t = torch.tensor([ms_plain], device=dev)
-        if world > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_plain = float(t.item())
-        v_plain = bsz * args.steps * world / (ms_plain / 1e3)
+        ms_plain = R.max_over_ranks(e0.elapsed_time(e1), dev)
+        v_plain = R.job_throughput(bsz * args.steps, world, ms_plain / 1e3)
         line["plain_method"] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps}
         line["fused_speedup_vs_plain"] = value / v_plain
     if not args.quick:
@@ -301,12 +290,8 @@ def run_ours(args):
             out_g.copy_(thd.grad, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms_e2e = e0.elapsed_time(e1)
-        t = torch.tensor([ms_e2e], device=dev)
-        if world > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-        line["e2e"] = {"value": bsz * args.steps * world / (ms_e2e / 1e3), "unit": UNIT,
+        ms_e2e = R.max_over_ranks(e0.elapsed_time(e1), dev)
+        line["e2e"] = {"value": R.job_throughput(bsz * args.steps, world, ms_e2e / 1e3), "unit": UNIT,
                        "h2d_bytes_per_step": int(pin_theta.numel() * 4),
                        "d2h_bytes_per_step": int(out_ev.numel() * 4 + out_g.numel() * 4)}
         # ---------------- roofline of the dominant kernel (adjoint dense 1-wire step)
@@ -315,9 +300,7 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.quick:
         v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
-    if world > 1:
-        torch.distributed.barrier()
-        torch.distributed.destroy_process_group()
+    R.finish()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
