@@ -56,6 +56,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the baseline sample")
     ap.add_argument("--quick", action="store_true", help="skip e2e/roofline/baseline (profiling runs)")
+    ap.add_argument("--workload", default="random", choices=["random", "c1", "c3", "c5"],
+                    help="random: the headline circuit (default); c1: small encoder+U3+CNOT model (n=4, bsz=32); "
+                         "c3: fused widths k=4..6 at n=26/28; c5: differentiation workload (n=20, bsz=64)")
     return ap.parse_args()
 
 
@@ -398,10 +401,172 @@ def roofline(args, dev):
     return roof, res
 
 
+# ------------------------------------------------------------------ other configurations
+def _timed(fn, steps, warmup, dev):
+    """Device time of ``steps`` calls (CUDA events on the current stream) after warm-up,
+    plus each call's own duration for latency percentiles."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        fn()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+    return ev[0].elapsed_time(ev[-1]), per
+
+
+def _line(args, workload_cfg, value, ms, extra):
+    d = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+         "dtype": "c64", "data": "synthetic", "config": workload_cfg}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def run_c1(args):
+    """Small model: GeneralEncoder(rx, ry, rz, rx on 4 wires) + 2 x (U3 on every wire,
+    CNOT ring) + Z on every wire, n=4, bsz=32, forward + backward per step."""
+    import torch
+
+    import torchquantum_gb300 as tq
+
+    dev = torch.device("cuda")
+
+    class Model(tq.QuantumModule):
+        def __init__(self):
+            super().__init__()
+            self.enc = tq.GeneralEncoder([{"input_idx": [4 * g + w], "func": ["rx", "ry", "rz", "rx"][g],
+                                           "wires": [w]} for g in range(4) for w in range(4)])
+            self.u3 = tq.QuantumModuleList([tq.Op1QAllLayer(op=tq.U3, n_wires=4, has_params=True, trainable=True)
+                                            for _ in range(2)])
+            self.cx = tq.QuantumModuleList([tq.Op2QAllLayer(op=tq.CNOT, n_wires=4, circular=True) for _ in range(2)])
+            self.meas = tq.MeasureAll(tq.PauliZ)
+
+        def forward(self, x):
+            q = tq.QuantumDevice(n_wires=4, bsz=x.shape[0], device=dev)
+            self.enc(q, x)
+            for a, b in zip(self.u3, self.cx):
+                a(q)
+                b(q)
+            return self.meas(q)
+
+    model = Model().to(dev)
+    x = torch.rand(32, 16, device=dev, generator=torch.Generator(device=dev).manual_seed(0)) * np.pi
+
+    def step():
+        model.zero_grad(set_to_none=True)
+        model(x).sum().backward()
+
+    ms, per = _timed(step, args.steps, args.warmup, dev)
+    _line(args, {"workload": "n=4 bsz=32: encoder (16 rotations) + 2 x (U3 on each wire, CNOT ring), Z per wire, "
+                             "fwd + bwd", "n_wires": 4, "global_batch": 32},
+          32 * args.steps / (ms / 1e3), ms, {"p50_ms": float(np.percentile(per, 50)),
+                                             "p99_ms": float(np.percentile(per, 99))})
+
+
+def run_c3(args):
+    """Fused forward at scale: the headline random circuit at (n=26, bsz=8) with fused
+    widths k = 4, 5, 6 and (n=28, bsz=1) with k = 6; circuits/s of the forward pass."""
+    import torch
+
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import workloads as W
+
+    dev = torch.device("cuda")
+    res = {}
+    for n, bsz, k in [(26, 8, 4), (26, 8, 5), (26, 8, 6), (28, 1, 6)]:
+        gates, ncols = W.random_circuit(n, args.depth, seed=0)
+        th = torch.tensor(W.random_params(bsz, ncols, seed=1), device=dev)
+        holder = {}
+
+        def step():
+            q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
+            q.method = "fused"
+            q.fuse_wires = k
+            W.apply_circuit(q, gates, th)
+            holder["out"] = q.get_states_1d()
+            holder["q"] = q
+
+        ms, _ = _timed(step, args.steps, args.warmup, dev)
+        q = holder["q"]
+        blocks = sum(len(sg.exec_ops) for sg in q._tape)
+        tcb = sum(1 for sg in q._tape for op in sg.exec_ops if getattr(op, "tc", False))
+        per_step = ms / args.steps
+        S = bsz * (1 << n) * 8
+        res[f"n{n}_bsz{bsz}_k{k}"] = {"circuits_per_s": bsz * 1e3 / per_step, "ms_per_step": per_step,
+                                      "passes": blocks, "tensor_core_blocks": tcb,
+                                      "hbm_GBps_2S_per_pass": 2 * S * blocks / (per_step / 1e3) / 1e9}
+        del holder
+    main = res["n26_bsz8_k6"]
+    _line(args, {"workload": f"random circuit depth {args.depth}, fused forward, n=26 bsz=8 (k=4,5,6) and n=28 bsz=1 "
+                             "(k=6)", "n_wires": 26, "global_batch": 8},
+          main["circuits_per_s"], main["ms_per_step"] * args.steps, {"cases": res})
+
+
+def run_c5(args):
+    """Differentiation workload: n=20, bsz=64, 10 layers of (RY, RZ on every wire with
+    shared parameters, CZ ladder) = 400 parameters, loss = sum_j w_j <P_j> over 50 random
+    Pauli strings; fwd + adjoint bwd per step.  Literal variant (|0> input: all rows equal)
+    and a variant with a per-sample RY(x_b) input layer."""
+    import torch
+
+    import torchquantum_gb300 as tq
+    import torchquantum_gb300.functional as tqf
+    from torchquantum_gb300 import workloads as W
+
+    dev = torch.device("cuda")
+    n, bsz, layers, m = 20, 64, 10, 50
+    gates, ncols = W.hea_circuit(n, layers)
+    rng = np.random.default_rng(7)
+    theta = torch.tensor(rng.uniform(-np.pi, np.pi, size=(1, ncols)).astype(np.float32), device=dev,
+                         requires_grad=True)
+    x = torch.tensor(rng.uniform(0, np.pi, size=(bsz, n)).astype(np.float32), device=dev)
+    paulis = W.random_paulis(n, m, seed=8)
+    w = torch.tensor(rng.normal(size=m).astype(np.float32), device=dev)
+    out = {}
+    for variant in ("literal", "per_sample_input"):
+        def step():
+            theta.grad = None
+            q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
+            q.method = "fused"
+            q.fuse_wires = 6
+            if variant == "per_sample_input":
+                for wi in range(n):
+                    tqf.ry(q, wires=wi, params=x[:, wi:wi + 1])
+            W.apply_circuit(q, gates, theta)
+            (tq.expval_joint_analytical_batch(q, paulis) * w).sum().backward()
+
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        ms, _ = _timed(step, args.steps, args.warmup, dev)
+        peak = torch.cuda.max_memory_allocated() - base
+        S = bsz * (1 << n) * 8
+        out[variant] = {"circuits_per_s": bsz * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                        "peak_bytes": int(peak), "peak_states": peak / S,
+                        "autograd_estimate_bytes": int(len(gates) * S)}
+    main = out["per_sample_input"]
+    _line(args, {"workload": "n=20 bsz=64, 10 x (RY, RZ per wire, shared params; CZ ladder), 400 params, "
+                             "sum of 50 weighted Pauli strings, fwd + adjoint bwd", "n_wires": n, "global_batch": bsz},
+          main["circuits_per_s"], main["ms_per_step"] * args.steps, {"variants": out})
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c1":
+        run_c1(args)
+    elif args.workload == "c3":
+        run_c3(args)
+    elif args.workload == "c5":
+        run_c5(args)
     else:
         run_ours(args)
 
