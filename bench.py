@@ -56,9 +56,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the baseline sample")
     ap.add_argument("--quick", action="store_true", help="skip e2e/roofline/baseline (profiling runs)")
-    ap.add_argument("--workload", default="random", choices=["random", "c1", "c3", "c5"],
+    ap.add_argument("--workload", default="random", choices=["random", "c1", "c3", "c4", "c5"],
                     help="random: the headline circuit (default); c1: small encoder+U3+CNOT model (n=4, bsz=32); "
-                         "c3: fused widths k=4..6 at n=26/28; c5: differentiation workload (n=20, bsz=64)")
+                         "c3: fused widths k=4..6 at n=26/28; c4: 256 uneven circuits in one persistent batch; "
+                         "c5: differentiation workload (n=20, bsz=64)")
     return ap.parse_args()
 
 
@@ -557,6 +558,67 @@ def run_c5(args):
           main["circuits_per_s"], main["ms_per_step"] * args.steps, {"variants": out})
 
 
+def run_c4(args):
+    """Uneven batching: 256 independent circuits, n ~ U{8..20}, L ~ U{2..40} layers of
+    (RY, RZ on every wire, angles ~ U[-pi, pi); CZ ladder), output <Z_0> of each, run as
+    one persistent batch (tqk_batch_run).  value = circuits/s of the launch; e2e adds the
+    host compile (IR + plan) and the host<->device copies; latency = each circuit's
+    completion time after the launch started."""
+    import torch
+
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import batch as B
+
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(0)
+    specs = [(int(rng.integers(8, 21)), int(rng.integers(2, 41))) for _ in range(256)]
+    angles = [(rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n))) for n, L in specs]
+
+    def build():
+        cb = B.CircuitBatch()
+        for (n, _), (ry, rz) in zip(specs, angles):
+            cb.add_layered(n, ry, rz)
+        return cb
+
+    for _ in range(args.warmup):
+        build().run(dev)
+    kms, wall, res = [], [], None
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = build().run(dev)
+        torch.cuda.synchronize()
+        wall.append(time.perf_counter() - t0)
+        kms.append(res.kernel_ms)
+    ms = float(np.sum(kms))
+    # the same circuits one at a time through the engine (fused method), on a sample
+    sample = list(range(0, 256, 16))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in sample:
+        (n, L), (ry, rz) = specs[i], angles[i]
+        q = tq.QuantumDevice(n_wires=n, bsz=1, device=dev)
+        q.method = "fused"
+        for l in range(L):
+            for w in range(n):
+                tq.functional.ry(q, wires=w, params=float(ry[l, w]))
+                tq.functional.rz(q, wires=w, params=float(rz[l, w]))
+            for w in range(n - 1):
+                tq.functional.cz(q, wires=[w, w + 1])
+        tq.expval_joint_analytical(q, "Z" + "I" * (n - 1))
+    torch.cuda.synchronize()
+    per_circuit_engine = (time.perf_counter() - t0) / len(sample)
+    _line(args, {"workload": "256 circuits, n~U{8..20}, L~U{2..40} x (RY, RZ per wire; CZ ladder), <Z_0> each, one "
+                             "persistent batch", "circuits": 256, "n_range": [8, 20], "layers_range": [2, 40]},
+          256 * args.steps / (ms / 1e3), ms,
+          {"e2e": {"value": 256 * args.steps / float(np.sum(wall)), "unit": UNIT, "includes": "host IR build + plan + "
+                   "copies + launch + read-back"},
+           "latency_ms": {"p50": float(np.percentile(res.latency_ms, 50)), "p99": float(np.percentile(res.latency_ms, 99)),
+                          "max": float(res.latency_ms.max())},
+           "engine_one_circuit_at_a_time": {"circuits_per_s": 1.0 / per_circuit_engine,
+                                            "sample": f"{len(sample)} of the 256 circuits, fused method, sequential"}})
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -565,6 +627,8 @@ def main():
         run_c1(args)
     elif args.workload == "c3":
         run_c3(args)
+    elif args.workload == "c4":
+        run_c4(args)
     elif args.workload == "c5":
         run_c5(args)
     else:

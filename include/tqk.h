@@ -231,6 +231,75 @@ int tqk_block_build(const tqk_block_desc* blocks, int nblocks, int max_batch, co
 int tqk_block_unbuild(const tqk_block_desc* blocks, int nblocks, int max_batch,
                       const tqk_block_op* ops, void* stream);
 
+/* ---------------------------------------------------------------- persistent circuit batches
+ * Many independent circuits of different sizes (n <= 24) in one launch.  tqk_batch_plan
+ * splits each circuit into passes whose target bits fit a tile of 2^14 amplitudes held in
+ * shared memory (circuits with n <= 14: one pass, one tile, never touching HBM; larger
+ * ones stream their state, states + state_off, once per pass).  tqk_batch_items lists the
+ * work: one item per (circuit, pass, tile), in waves of pass index, so a pass's tiles run
+ * on many SMs at once.  One persistent CTA per SM takes items in order; an item of pass
+ * p > 0 first waits (bounded) until every tile of pass p - 1 of its circuit is done.
+ * Outputs <Z_{z_wire}> per circuit (float64) and, if t_done != NULL, each circuit's
+ * completion time (globaltimer ns; t_done[ncirc] = the launch's start).  Upstream runs
+ * such batches as a Python loop over circuits, each gate a torch bmm
+ * (functional/gate_wrapper.py:96-140). */
+enum { TQK_B_DENSE1 = 0, TQK_B_CTRL1 = 1, TQK_B_CZ = 2, TQK_B_CZ_LADDER = 3 };
+enum { TQK_BATCH_TILE_BITS = 14, TQK_BATCH_MAX_QUBITS = 24 };
+
+typedef struct {
+  int32_t kind;  /* TQK_B_* */
+  int32_t w0;    /* DENSE1: target; CTRL1: control; CZ: first wire; CZ_LADDER: first wire */
+  int32_t w1;    /* CTRL1: target; CZ: second wire; CZ_LADDER: last wire (CZ on (w, w+1), w0 <= w < w1) */
+  int32_t mat;   /* DENSE1 / CTRL1: index of a row-major 2x2 complex64 matrix in `mats` */
+} tqk_batch_op; /* 16 bytes */
+
+typedef struct {
+  int32_t n;          /* qubits, 1..TQK_BATCH_MAX_QUBITS */
+  int32_t z_wire;     /* output <Z> on this wire */
+  int32_t first_op;   /* ops[first_op .. first_op + num_ops) */
+  int32_t num_ops;
+  int64_t state_off;  /* amplitude offset of the circuit's state in `states`; -1 for none
+                         (allowed only for single-pass circuits without written states) */
+  int32_t first_pass; /* written by tqk_batch_plan */
+  int32_t num_passes; /* written by tqk_batch_plan */
+} tqk_batch_circuit; /* 32 bytes */
+
+typedef struct {
+  int32_t first_op;   /* into the planned op array */
+  int32_t num_ops;
+  uint32_t tile_mask; /* amplitude-index bits inside the tile (min(n, 14) of them) */
+  int32_t flags;      /* 1: first pass (starts from |0..0>), 2: last pass (reduces <Z>) */
+} tqk_batch_pass; /* 16 bytes */
+
+typedef struct {
+  int32_t circuit;    /* index into circuits */
+  int32_t pass;       /* index into passes (a pass of that circuit) */
+  int32_t tile;       /* 0 .. 2^(n - popcount(tile_mask)) - 1 */
+  int32_t pad;
+} tqk_batch_item; /* 16 bytes */
+
+/* Host only (no GPU work): validate `circuits` and their ops (matrix indices < n_mats),
+ * write each circuit's passes into passes[0 .. return value) and its ops, regrouped by
+ * pass (ops that commute may move across passes), into ops_out at the same positions;
+ * fills first_pass/num_passes.  Returns the number of passes, or -TQK_* on error
+ * (-TQK_SCRATCH_TOO_SMALL if more than max_passes are needed). */
+int tqk_batch_plan(tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops_in, int n_mats,
+                   tqk_batch_op* ops_out, tqk_batch_pass* passes, int max_passes);
+/* Host only: the work items of planned circuits in dispatch order (wave w = every
+ * circuit's w-th pass, circuits in array order, tiles ascending); returns their number,
+ * or -TQK_SCRATCH_TOO_SMALL if more than max_items. */
+int64_t tqk_batch_items(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_pass* passes,
+                        tqk_batch_item* items, int64_t max_items);
+/* Device arrays: circuits (planned), ops (= ops_out of the plan), passes, items, mats
+ * (complex64 [*, 2, 2]), states (complex64; may be NULL if no circuit needs one),
+ * z_out[ncirc], pass_done[npasses] and counter (one int) all zeroed by the caller before
+ * each launch, t_done[ncirc + 1] or NULL, status (device int; TQK_TIMEOUT if a wait gave
+ * up).  write_states != 0 stores every final state. */
+int tqk_batch_run(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops,
+                  const tqk_batch_pass* passes, const tqk_batch_item* items, int64_t n_items,
+                  const void* mats, void* states, int write_states, double* z_out, int* pass_done,
+                  uint64_t* t_done, int* counter, int* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

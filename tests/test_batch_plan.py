@@ -1,0 +1,165 @@
+"""Circuit batches on the CPU: the IR compiler (torchquantum_gb300.batch) and the host
+planner (tqk_batch_plan, host code in libtqk.so) checked with the oracle.
+
+* the IR a gate list compiles to (fused one-qubit matrices, controlled blocks, CZ)
+  simulates to the oracle's state;
+* the planner only regroups ops of one circuit, keeps every pass's targets inside its
+  tile of 2^14 amplitudes (with address bits 0-4, for coalescing), flags the first and
+  last passes, and its regrouped order simulates to the same state as the original;
+* invalid circuits are rejected with the library's status codes.
+"""
+import numpy as np
+import pytest
+
+from oracle import statevec as O
+from torchquantum_gb300 import batch as B
+
+
+def _simulate_ir(n, ops, mats):
+    """The IR's semantics, op by op, with the oracle's dense application."""
+    s = O.init_state(n, 1).astype(np.complex128)
+    for op in ops:
+        k, w0, w1 = int(op["kind"]), int(op["w0"]), int(op["w1"])
+        if k == B.DENSE1:
+            s = O.apply(s, mats[op["mat"]][None], [w0], n)
+        elif k == B.CTRL1:
+            m = np.eye(4, dtype=np.complex128)
+            m[2:, 2:] = mats[op["mat"]]
+            s = O.apply(s, m[None], [w0, w1], n)
+        elif k == B.CZ:
+            s = O.apply(s, np.diag([1, 1, 1, -1]).astype(np.complex128)[None], [w0, w1], n)
+        else:
+            for w in range(w0, w1):
+                s = O.apply(s, np.diag([1, 1, 1, -1]).astype(np.complex128)[None], [w, w + 1], n)
+    return s[0]
+
+
+def _random_gates(rng, n, depth):
+    names1 = ["u3", "rx", "ry", "rz", "hadamard", "s", "t", "sx"]
+    names2 = ["cnot", "cz", "crx", "cry", "crz", "cu3", "cu1"]
+    from torchquantum_gb300 import gates as G
+
+    out = []
+    for _ in range(depth):
+        if rng.random() < 0.6:
+            name = names1[rng.integers(len(names1))]
+            wires = [int(rng.integers(n))]
+        else:
+            name = names2[rng.integers(len(names2))]
+            wires = [int(w) for w in rng.choice(n, 2, replace=False)]
+        npar = G.GATES[G.canonical_name(name)].num_params
+        p = rng.uniform(-np.pi, np.pi, size=npar) if npar else None
+        out.append({"name": name, "wires": wires, "params": p})
+    return out
+
+
+@pytest.mark.parametrize("n", [3, 6, 9])
+def test_compiled_ir_matches_oracle(n):
+    rng = np.random.default_rng(n)
+    gates = _random_gates(rng, n, 60)
+    cb = B.CircuitBatch()
+    cb.add_gates(n, gates)
+    got = _simulate_ir(n, cb._ops[0], cb._mats[0].astype(np.complex128))
+    ref = O.run(n, 1, [dict(g, params=None if g["params"] is None else np.asarray(g["params"])[None]) for g in gates])
+    np.testing.assert_allclose(got, ref[0], atol=1e-5)
+    assert len(cb._ops[0]) < len(gates)  # consecutive one-qubit gates were fused
+
+
+def test_layered_ir_matches_gate_list():
+    n, L = 5, 3
+    rng = np.random.default_rng(1)
+    ry, rz = rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n))
+    cb = B.CircuitBatch()
+    cb.add_layered(n, ry, rz)
+    gates = []
+    for l in range(L):
+        gates += [{"name": "ry", "wires": [w], "params": np.array([[ry[l, w]]])} for w in range(n)]
+        gates += [{"name": "rz", "wires": [w], "params": np.array([[rz[l, w]]])} for w in range(n)]
+        gates += [{"name": "cz", "wires": [w, w + 1], "params": None} for w in range(n - 1)]
+    got = _simulate_ir(n, cb._ops[0], cb._mats[0].astype(np.complex128))
+    np.testing.assert_allclose(got, O.run(n, 1, gates)[0], atol=1e-6)
+
+
+def test_plan_regroups_legally():
+    rng = np.random.default_rng(3)
+    cb = B.CircuitBatch()
+    sizes = [15, 4, 16, 12, 17]
+    for n in sizes:
+        if n % 2:
+            L = int(rng.integers(2, 5))
+            cb.add_layered(n, rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n)), z_wire=n - 1)
+        else:
+            cb.add_gates(n, _random_gates(rng, n, 40))
+    circ, ops, passes, items, mats, order, state_amps = cb.compile()
+    # work items: one per (circuit, pass, tile); a pass's items come after all items of
+    # the circuit's previous pass
+    seen = {}
+    for k, it in enumerate(items):
+        seen.setdefault(int(it["pass"]), []).append(k)
+    for slot in range(len(circ)):
+        c = circ[slot]
+        for w in range(int(c["num_passes"])):
+            pi = int(c["first_pass"]) + w
+            ks = seen[pi]
+            assert len(ks) == 1 << (int(c["n"]) - bin(int(passes[pi]["tile_mask"])).count("1"))
+            assert all(int(items[k]["circuit"]) == slot for k in ks)
+            if w:
+                assert min(ks) > max(seen[pi - 1])
+    assert sorted(order) == list(range(len(sizes)))
+    assert state_amps == sum(1 << n for n in sizes if n > B.TILE_BITS)
+    for slot, i in enumerate(order):
+        c = circ[slot]
+        n = int(c["n"])
+        assert n == sizes[i]
+        mine = ops[c["first_op"]:c["first_op"] + c["num_ops"]]
+        orig = cb._ops[i]
+        key = lambda a: sorted(map(tuple, np.stack([a["kind"], a["w0"], a["w1"]], 1).tolist()))
+        assert key(mine) == key(orig)  # a permutation of the circuit's own ops
+        ps = passes[c["first_pass"]:c["first_pass"] + c["num_passes"]]
+        assert ps[0]["flags"] & 1 and ps[-1]["flags"] & 2
+        covered = 0
+        for p in ps:
+            tm = int(p["tile_mask"])
+            assert bin(tm).count("1") == min(n, B.TILE_BITS) and tm < (1 << n)
+            if n > B.TILE_BITS:
+                assert tm & 0x1F == 0x1F
+            for op in ops[p["first_op"]:p["first_op"] + p["num_ops"]]:
+                k = int(op["kind"])
+                tgt = int(op["w0"]) if k == B.DENSE1 else int(op["w1"]) if k == B.CTRL1 else None
+                if tgt is not None:
+                    assert (tm >> (n - 1 - tgt)) & 1
+            covered += int(p["num_ops"])
+        assert covered == len(orig)
+        m64 = cb._mats[i].astype(np.complex128)
+        mine_local = mine.copy()
+        mine_local["mat"] = np.where(mine["mat"] >= 0, mine["mat"] - _mat_base(cb, order, slot), -1)
+        np.testing.assert_allclose(_simulate_ir(n, mine_local, m64), _simulate_ir(n, orig, m64), atol=1e-9)
+
+
+def _mat_base(cb, order, slot):
+    return sum(len(cb._mats[j]) for j in order[:slot])
+
+
+def test_plan_rejects_invalid():
+    from torchquantum_gb300 import _lib
+
+    cb = B.CircuitBatch()
+    cb.add_ops(3, np.array([(B.CTRL1, 1, 1, 0)], dtype=B.OP_T), np.eye(2)[None])
+    with pytest.raises(_lib.TQKError, match="BAD_WIRES"):
+        cb.compile()
+    cb = B.CircuitBatch()
+    cb.add_ops(3, np.array([(B.DENSE1, 5, 0, 0)], dtype=B.OP_T), np.eye(2)[None])
+    with pytest.raises(_lib.TQKError, match="BAD_WIRES"):
+        cb.compile()
+    cb = B.CircuitBatch()
+    cb.add_ops(4, np.array([(B.CZ_LADDER, 2, 1, -1)], dtype=B.OP_T), np.zeros((0, 2, 2)))
+    with pytest.raises(_lib.TQKError, match="BAD_WIRES"):
+        cb.compile()
+    cb = B.CircuitBatch()
+    cb.add_ops(3, np.array([(B.DENSE1, 0, 0, 1)], dtype=B.OP_T), np.eye(2)[None])  # only matrix 0 exists
+    with pytest.raises(_lib.TQKError, match="BAD_SHAPE"):
+        cb.compile()
+    with pytest.raises(ValueError):
+        B.CircuitBatch().add_ops(25, np.zeros(0, B.OP_T), np.zeros((0, 2, 2)))
+    with pytest.raises(ValueError, match="not supported"):
+        B.CircuitBatch().add_gates(3, [{"name": "swap", "wires": [0, 1], "params": None}])

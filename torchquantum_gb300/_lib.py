@@ -57,6 +57,9 @@ _SIGS = {
     "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_fused_image_bytes": (_i64, [_i64]),
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp, _vp]),
+    "tqk_batch_plan": (_int, [_vp, _int, _vp, _int, _vp, _vp, _int]),
+    "tqk_batch_items": (_i64, [_vp, _int, _vp, _vp, _i64]),
+    "tqk_batch_run": (_int, [_vp, _int, _vp, _vp, _vp, _i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
     "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
     "tqk_pauli_expval_noalloc_capacity": (_i64, []),

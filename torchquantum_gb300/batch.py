@@ -1,0 +1,225 @@
+"""Persistent batches of many independent circuits of different sizes on one GPU.
+
+Upstream runs such a batch as a Python loop over circuits, each gate a torch bmm
+(functional/gate_wrapper.py:96-140).  Here a batch is compiled to a compact op list
+(C ABI ``tqk_batch_op``: dense 1-qubit, controlled 1-qubit, CZ, CZ ladder), planned on
+the host into shared-memory tile passes (``tqk_batch_plan``), listed as (circuit, pass,
+tile) work items (``tqk_batch_items``) and executed by one persistent kernel
+(``tqk_batch_run``): circuits with n <= 14 are one item and live entirely in shared
+memory; the tiles of a larger circuit's pass run on many SMs at once and its state is
+streamed once per pass.  Outputs: <Z> on one wire per circuit, each circuit's completion time (for
+latency percentiles) and, on request, the final states.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import gates as G
+
+OP_T = np.dtype([("kind", "<i4"), ("w0", "<i4"), ("w1", "<i4"), ("mat", "<i4")])
+CIRC_T = np.dtype([("n", "<i4"), ("z_wire", "<i4"), ("first_op", "<i4"), ("num_ops", "<i4"), ("state_off", "<i8"),
+                   ("first_pass", "<i4"), ("num_passes", "<i4")])
+PASS_T = np.dtype([("first_op", "<i4"), ("num_ops", "<i4"), ("tile_mask", "<u4"), ("flags", "<i4")])
+ITEM_T = np.dtype([("circuit", "<i4"), ("pass", "<i4"), ("tile", "<i4"), ("pad", "<i4")])
+DENSE1, CTRL1, CZ, CZ_LADDER = 0, 1, 2, 3
+TILE_BITS = 14
+MAX_QUBITS = 24
+_X = np.array([[0, 1], [1, 0]], dtype=np.complex128)
+
+
+@dataclass
+class BatchResult:
+    z: np.ndarray                        # <Z_{z_wire}> per circuit (float64), in the order added
+    latency_ms: np.ndarray               # completion time of each circuit after the launch started
+    kernel_ms: float                     # device time of the launch (CUDA events)
+    states: Optional[List[torch.Tensor]]  # final states (complex64 [2^n]) if requested
+
+
+class CircuitBatch:
+    """Collects circuits (``add_gates`` / ``add_layered``), then ``run`` executes them all
+    with one persistent kernel launch."""
+
+    def __init__(self):
+        self._n: List[int] = []
+        self._z: List[int] = []
+        self._ops: List[np.ndarray] = []
+        self._mats: List[np.ndarray] = []
+
+    def __len__(self):
+        return len(self._n)
+
+    # ------------------------------------------------------------------ building
+    def add_ops(self, n: int, ops: np.ndarray, mats: np.ndarray, z_wire: int = 0) -> int:
+        """A circuit in the IR: ``ops`` (OP_T, ``mat`` indexes ``mats`` [m, 2, 2])."""
+        if not 1 <= n <= MAX_QUBITS:
+            raise ValueError(f"n_wires must be in 1..{MAX_QUBITS} (got {n})")
+        self._n.append(int(n))
+        self._z.append(int(z_wire))
+        self._ops.append(np.asarray(ops, dtype=OP_T))
+        self._mats.append(np.asarray(mats, dtype=np.complex64).reshape(-1, 2, 2))
+        return len(self._n) - 1
+
+    def add_gates(self, n: int, gates: Sequence[Dict], z_wire: int = 0) -> int:
+        """A circuit as a gate list ``{name, wires, params}`` (params: P reals or None).
+        Consecutive one-qubit gates on a wire are fused into one 2x2 matrix; controlled
+        one-qubit gates, CNOT and controlled phases use their lower-right 2x2 block; CZ
+        becomes a diagonal op."""
+        pending: Dict[int, np.ndarray] = {}
+        ops, mats = [], []
+
+        def emit(kind, w0, w1=0, m=None):
+            idx = -1
+            if m is not None:
+                mats.append(m)
+                idx = len(mats) - 1
+            ops.append((kind, w0, w1, idx))
+
+        def flush(w):
+            m = pending.pop(w, None)
+            if m is not None:
+                emit(DENSE1, w, 0, m)
+
+        for g in gates:
+            name = G.canonical_name(g["name"])
+            wires = [int(w) for w in g["wires"]]
+            gd = G.GATES[name]
+            p = g.get("params")
+            pt = None if p is None else torch.tensor(np.asarray(p, np.float64).reshape(1, -1))
+            mat = G.gate_matrix(name, pt, len(wires), dtype=torch.complex128)[0].numpy()
+            if len(wires) == 1:
+                pending[wires[0]] = mat @ pending.get(wires[0], np.eye(2))
+                continue
+            if len(wires) != 2 or gd.struct[0] not in ("ctrl", "x", "phase", "diag", "dense"):
+                raise ValueError(f"gate {name} on {len(wires)} wires is not supported in a circuit batch")
+            for w in wires:
+                flush(w)
+            off = mat.copy()
+            off[2:, 2:] = 0
+            if np.abs(off - np.eye(4) * np.array([1, 1, 0, 0])).max() > 1e-12:
+                raise ValueError(f"gate {name} is not a controlled one-qubit gate")
+            sub = mat[2:, 2:]
+            if np.abs(sub - np.diag([1, -1])).max() < 1e-12:
+                emit(CZ, wires[0], wires[1])
+            else:
+                emit(CTRL1, wires[0], wires[1], sub)
+        for w in sorted(pending):
+            flush(w)
+        arr = np.array(ops, dtype=OP_T) if ops else np.zeros(0, dtype=OP_T)
+        return self.add_ops(n, arr, np.array(mats) if mats else np.zeros((0, 2, 2)), z_wire)
+
+    def add_layered(self, n: int, ry: np.ndarray, rz: np.ndarray, z_wire: int = 0) -> int:
+        """L layers of (RY(ry[l, w]), RZ(rz[l, w]) on every wire w, then CZ(w, w+1) for
+        w = 0..n-2): one fused 2x2 per (layer, wire) and one CZ-ladder op per layer."""
+        ry = np.asarray(ry, np.float64).reshape(-1, n)
+        rz = np.asarray(rz, np.float64).reshape(-1, n)
+        L = ry.shape[0]
+        c, s = np.cos(ry / 2), np.sin(ry / 2)
+        em, ep = np.exp(-0.5j * rz), np.exp(0.5j * rz)
+        m = np.empty((L, n, 2, 2), dtype=np.complex128)  # RZ(b) RY(a)
+        m[..., 0, 0], m[..., 0, 1] = em * c, -em * s
+        m[..., 1, 0], m[..., 1, 1] = ep * s, ep * c
+        per = n + (1 if n >= 2 else 0)
+        ops = np.zeros(L * per, dtype=OP_T)
+        ops = ops.reshape(L, per)
+        ops["kind"][:, :n] = DENSE1
+        ops["w0"][:, :n] = np.arange(n)[None, :]
+        ops["mat"][:, :n] = np.arange(L * n).reshape(L, n)
+        if n >= 2:
+            ops["kind"][:, n] = CZ_LADDER
+            ops["w0"][:, n] = 0
+            ops["w1"][:, n] = n - 1
+            ops["mat"][:, n] = -1
+        return self.add_ops(n, ops.reshape(-1), m.reshape(-1, 2, 2), z_wire)
+
+    # ------------------------------------------------------------------ execution
+    def compile(self, return_states: bool = False):
+        """Host tables in execution order (costly circuits first): circuits, planned ops,
+        passes, matrices, the execution order and the state buffer size (amplitudes)."""
+        nc = len(self._n)
+        cost = [len(o) * (1 << n) for o, n in zip(self._ops, self._n)]
+        order = sorted(range(nc), key=lambda i: -cost[i])
+        circ = np.zeros(nc, dtype=CIRC_T)
+        ops_l, mats_l = [], []
+        nops = nmats = 0
+        state_amps = 0
+        for slot, i in enumerate(order):
+            n = self._n[i]
+            o = self._ops[i].copy()
+            o["mat"] = np.where(o["mat"] >= 0, o["mat"] + nmats, -1)
+            circ[slot] = (n, self._z[i], nops, len(o), -1, 0, 0)
+            if return_states or n > TILE_BITS:
+                circ[slot]["state_off"] = state_amps
+                state_amps += 1 << n
+            ops_l.append(o)
+            mats_l.append(self._mats[i])
+            nops += len(o)
+            nmats += len(self._mats[i])
+        ops_in = np.concatenate(ops_l) if ops_l else np.zeros(0, OP_T)
+        mats = np.concatenate(mats_l).astype(np.complex64) if mats_l else np.zeros((0, 2, 2), np.complex64)
+        ops_out = np.zeros_like(ops_in)
+        max_passes = len(ops_in) + nc
+        passes = np.zeros(max(1, max_passes), dtype=PASS_T)
+        lib = _lib.load()
+        npass = lib.tqk_batch_plan(circ.ctypes.data, nc, ops_in.ctypes.data if len(ops_in) else None, len(mats),
+                                   ops_out.ctypes.data if len(ops_out) else None, passes.ctypes.data, max_passes)
+        if npass < 0:
+            raise _lib.TQKError(-npass, lib.tqk_last_error().decode())
+        passes = passes[:npass]
+        n_items = sum(1 << (int(c["n"]) - bin(int(p["tile_mask"])).count("1"))
+                      for c in circ for p in passes[c["first_pass"]:c["first_pass"] + c["num_passes"]])
+        items = np.zeros(max(1, n_items), dtype=ITEM_T)
+        got = lib.tqk_batch_items(circ.ctypes.data, nc, passes.ctypes.data, items.ctypes.data, n_items)
+        if got < 0:
+            raise _lib.TQKError(-got, lib.tqk_last_error().decode())
+        return circ, ops_out, passes, items[:got], mats, order, state_amps
+
+    def run(self, device=None, return_states: bool = False) -> BatchResult:
+        dev = torch.device(device if device is not None else "cuda")
+        if dev.type != "cuda":
+            raise _lib.TQKError(8, "circuit batches run on a CUDA device only")
+        nc = len(self._n)
+        if nc == 0:
+            return BatchResult(np.zeros(0), np.zeros(0), 0.0, [] if return_states else None)
+        circ, ops, passes, items, mats, order, state_amps = self.compile(return_states)
+
+        def up(a):
+            return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).pin_memory().to(dev, non_blocking=True)
+
+        d_circ, d_ops, d_pass = up(circ), up(ops if len(ops) else np.zeros(1, OP_T)), up(passes)
+        d_items = up(items)
+        d_mats = up(mats if len(mats) else np.zeros((1, 2, 2), np.complex64))
+        states = torch.empty(max(1, state_amps), dtype=torch.complex64, device=dev)
+        z = torch.zeros(nc, dtype=torch.float64, device=dev)
+        pass_done = torch.zeros(len(passes), dtype=torch.int32, device=dev)
+        t_done = torch.empty(nc + 1, dtype=torch.int64, device=dev)
+        counter = torch.zeros(1, dtype=torch.int32, device=dev)
+        stream = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib._check(_lib.load().tqk_batch_run(d_circ.data_ptr(), nc, d_ops.data_ptr(), d_pass.data_ptr(),
+                                              d_items.data_ptr(), len(items), d_mats.data_ptr(), states.data_ptr(),
+                                              int(return_states), z.data_ptr(), pass_done.data_ptr(),
+                                              t_done.data_ptr(), counter.data_ptr(),
+                                              _lib.status_word(dev).data_ptr(), stream.cuda_stream))
+        e1.record(stream)
+        zh = z.cpu().numpy()
+        th = t_done.cpu().numpy()
+        _lib.check_status(dev)
+        kernel_ms = e0.elapsed_time(e1)
+        out_z = np.empty(nc)
+        lat = np.empty(nc)
+        for slot, i in enumerate(order):
+            out_z[i] = zh[slot]
+            lat[i] = (th[slot] - th[nc]) / 1e6
+        out_states = None
+        if return_states:
+            out_states = [None] * nc
+            for slot, i in enumerate(order):
+                off = int(circ[slot]["state_off"])
+                out_states[i] = states[off:off + (1 << self._n[i])].clone()
+        return BatchResult(out_z, lat, kernel_ms, out_states)

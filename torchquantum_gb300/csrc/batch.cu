@@ -1,0 +1,350 @@
+// batch.cu -- persistent runner for many independent circuits of different sizes.
+//
+// A circuit is a list of passes (tqk_batch_plan); a pass holds ops whose target bits lie
+// in a tile of 2^14 amplitudes (tile_mask), applied tile by tile in shared memory: gather
+// the tile from the circuit's state, apply every op of the pass, scatter it back.
+// Circuits with n <= 14 are one tile and one pass: their whole life is in shared memory.
+// Diagonal ops (CZ, CZ ladders) and controls need no tile bit -- they read the
+// amplitude's global index -- so the planner gives them to any pass.
+//
+// Work is one item per (circuit, pass, tile) (tqk_batch_items), handed out in waves of
+// pass index by a global counter to one persistent CTA per SM, so the tiles of a large
+// circuit's pass run on many SMs at once.  An item of pass p > 0 waits (bounded) for the
+// completion counter of pass p - 1; every item's dependencies are handed out before it,
+// so the earliest unfinished item can always run.  A tile publishes its stores
+// (__threadfence) before counting itself done; dependent tiles read through L2
+// (ld.global.cg) since their SM's L1 may hold the previous pass's lines.  Last-pass tiles
+// add their <Z> partial (float64 atomics) and the tile that completes a circuit stamps
+// its completion time.
+#include <stdint.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace tqk {
+namespace batch {
+
+constexpr int kTileBits = TQK_BATCH_TILE_BITS;
+constexpr int kThreads = 512;
+constexpr int kLowReserve = 5;  // address bits 0-4 stay in every tile: warps read 256-byte runs
+constexpr int kFirst = 1, kLast = 2;
+
+struct Tabs {
+  uint32_t lo[128];  // amplitude offset of tile index bits 0-6
+  uint32_t hi[128];  // ... and bits 7-13
+};
+
+__device__ __forceinline__ uint32_t dep(const Tabs& t, uint32_t l) { return t.lo[l & 127] + t.hi[l >> 7]; }
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // a * b + c
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+
+// 2x2 matrix m on local bit lb of the tile; if lc >= 0 only where local bit lc is set.
+__device__ __forceinline__ void apply_1q(float2* amp, int tb, int lb, int lc, const float2* m) {
+  const float2 m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+  const int half = 1 << (tb - 1);
+  for (int p = threadIdx.x; p < half; p += blockDim.x) {
+    const int i0 = ((p >> lb) << (lb + 1)) | (p & ((1 << lb) - 1));
+    if (lc >= 0 && !((i0 >> lc) & 1)) continue;
+    const int i1 = i0 | (1 << lb);
+    const float2 a0 = amp[i0], a1 = amp[i1];
+    amp[i0] = cfma(m00, a0, cmul(m01, a1));
+    amp[i1] = cfma(m10, a0, cmul(m11, a1));
+  }
+}
+
+__device__ void apply_op(const tqk_batch_op& op, float2* amp, int n, int tb, uint32_t tmask, uint32_t base,
+                         const Tabs& tabs, const float2* mats) {
+  const int tsz = 1 << tb;
+  switch (op.kind) {
+    case TQK_B_DENSE1: {
+      const int b = n - 1 - op.w0;
+      apply_1q(amp, tb, __popc(tmask & ((1u << b) - 1u)), -1, mats + 4 * op.mat);
+      break;
+    }
+    case TQK_B_CTRL1: {
+      const int cb = n - 1 - op.w0, b = n - 1 - op.w1;
+      const int lb = __popc(tmask & ((1u << b) - 1u));
+      if ((tmask >> cb) & 1u) {
+        apply_1q(amp, tb, lb, __popc(tmask & ((1u << cb) - 1u)), mats + 4 * op.mat);
+      } else if ((base >> cb) & 1u) {  // control outside the tile: set for the whole tile
+        apply_1q(amp, tb, lb, -1, mats + 4 * op.mat);
+      }
+      break;
+    }
+    case TQK_B_CZ: {
+      const int b0 = n - 1 - op.w0, b1 = n - 1 - op.w1;
+      for (int l = threadIdx.x; l < tsz; l += blockDim.x) {
+        const uint32_t g = base + dep(tabs, l);
+        if ((g >> b0) & (g >> b1) & 1u) amp[l] = make_float2(-amp[l].x, -amp[l].y);
+      }
+      break;
+    }
+    case TQK_B_CZ_LADDER: {
+      uint32_t m = 0;  // bit of wire w+1 for every pair (w, w+1); the pair's other bit is one above
+      for (int w = op.w0; w < op.w1; ++w) m |= 1u << (n - 2 - w);
+      for (int l = threadIdx.x; l < tsz; l += blockDim.x) {
+        const uint32_t g = base + dep(tabs, l);
+        if (__popc(g & (g >> 1) & m) & 1) amp[l] = make_float2(-amp[l].x, -amp[l].y);
+      }
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_batch(const tqk_batch_circuit* circ, int ncirc, const tqk_batch_op* ops, const tqk_batch_pass* passes,
+            const tqk_batch_item* items, long long n_items, const float2* mats, float2* states, int write_states,
+            double* z_out, int* pass_done, unsigned long long* t_done, int* counter, int* status) {
+  extern __shared__ float2 amp[];
+  __shared__ Tabs tabs;
+  __shared__ long long s_i;
+  __shared__ double red[kThreads / 32];
+  if (t_done != nullptr && blockIdx.x == 0 && threadIdx.x == 0) t_done[ncirc] = global_ns();
+  for (;;) {
+    if (threadIdx.x == 0) s_i = atomicAdd(counter, 1);
+    __syncthreads();
+    const long long i = s_i;
+    __syncthreads();
+    if (i >= n_items) break;
+    const tqk_batch_item it = items[i];
+    const tqk_batch_circuit C = circ[it.circuit];
+    const tqk_batch_pass P = passes[it.pass];
+    const int n = C.n;
+    const uint32_t tmask = P.tile_mask;
+    const int tb = __popc(tmask);
+    const int tsz = 1 << tb;
+    const int ntiles = 1 << (n - tb);
+    const uint32_t omask = (n >= 32 ? 0xffffffffu : ((1u << n) - 1u)) & ~tmask;
+    float2* st = states + (C.state_off >= 0 ? C.state_off : 0);
+    if (!(P.flags & kFirst) && threadIdx.x == 0) {  // every tile of the previous pass must be stored
+      const int prev_tiles = 1 << (n - __popc(passes[it.pass - 1].tile_mask));
+      const volatile int* d = pass_done + it.pass - 1;
+      const long long t0 = clock64();
+      while (*d < prev_tiles) {
+        if (clock64() - t0 > kWaitCycles) {
+          atomicExch(status, TQK_TIMEOUT);
+          break;
+        }
+      }
+      __threadfence();
+    }
+    if (threadIdx.x < 256) {  // deposit tables of the tile bits
+      const int part = threadIdx.x >> 7, x = threadIdx.x & 127;
+      uint32_t v = 0;
+      int j = 0;
+      for (int b = 0; b < n; ++b) {
+        if (!((tmask >> b) & 1u)) continue;
+        const int k = j++ - 7 * part;
+        if (k >= 0 && k < 7 && ((x >> k) & 1)) v |= 1u << b;
+      }
+      (part ? tabs.hi : tabs.lo)[x] = v;
+    }
+    uint32_t base = 0;
+    for (int b = 0, j = 0; b < n; ++b) {
+      if (!((omask >> b) & 1u)) continue;
+      if ((it.tile >> j) & 1) base |= 1u << b;
+      ++j;
+    }
+    __syncthreads();
+    if (P.flags & kFirst) {
+      for (int l = threadIdx.x; l < tsz; l += blockDim.x)
+        amp[l] = make_float2((base == 0u && l == 0) ? 1.f : 0.f, 0.f);
+    } else {
+#pragma unroll 4
+      for (int l = threadIdx.x; l < tsz; l += blockDim.x) amp[l] = __ldcg(st + base + dep(tabs, l));
+    }
+    __syncthreads();
+    for (int oi = 0; oi < P.num_ops; ++oi) {
+      apply_op(ops[P.first_op + oi], amp, n, tb, tmask, base, tabs, mats);
+      __syncthreads();
+    }
+    if (P.flags & kLast) {
+      const int zbit = n - 1 - C.z_wire;
+      double zacc = 0.0;
+      for (int l = threadIdx.x; l < tsz; l += blockDim.x) {
+        const float2 a = amp[l];
+        const double p2 = static_cast<double>(a.x) * a.x + static_cast<double>(a.y) * a.y;
+        zacc += (((base + dep(tabs, l)) >> zbit) & 1u) ? -p2 : p2;
+      }
+      for (int o = 16; o > 0; o >>= 1) zacc += __shfl_xor_sync(0xffffffffu, zacc, o);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = zacc;
+    }
+    if (((P.flags & kLast) == 0 || write_states) && C.state_off >= 0) {
+#pragma unroll 4
+      for (int l = threadIdx.x; l < tsz; l += blockDim.x) __stcg(st + base + dep(tabs, l), amp[l]);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (P.flags & kLast) {
+        double sum = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) sum += red[w];
+        atomicAdd(z_out + it.circuit, sum);
+        __threadfence();
+      }
+      const int old = atomicAdd(pass_done + it.pass, 1);
+      if ((P.flags & kLast) && old == ntiles - 1 && t_done != nullptr) t_done[it.circuit] = global_ns();
+    }
+    __syncthreads();
+  }
+}
+
+// Bits of an op's wires (all of them) and of its targets (the bits that must be in the tile).
+void op_bits(const tqk_batch_op& op, int n, uint32_t* wires, uint32_t* targets) {
+  auto bit = [n](int w) { return 1u << (n - 1 - w); };
+  switch (op.kind) {
+    case TQK_B_DENSE1:
+      *wires = *targets = bit(op.w0);
+      break;
+    case TQK_B_CTRL1:
+      *wires = bit(op.w0) | bit(op.w1);
+      *targets = bit(op.w1);
+      break;
+    case TQK_B_CZ:
+      *wires = bit(op.w0) | bit(op.w1);
+      *targets = 0;
+      break;
+    default: {  // ladder
+      uint32_t m = 0;
+      for (int w = op.w0; w <= op.w1; ++w) m |= bit(w);
+      *wires = m;
+      *targets = 0;
+    }
+  }
+}
+
+}  // namespace batch
+}  // namespace tqk
+
+using namespace tqk;
+
+extern "C" int tqk_batch_plan(tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops_in, int n_mats,
+                              tqk_batch_op* ops_out, tqk_batch_pass* passes, int max_passes) {
+  const char* what = "tqk_batch_plan";
+  if (ncirc < 0) return -fail(TQK_BAD_SHAPE, "%s: ncirc %d", what, ncirc);
+  if (ncirc > 0 && (!circuits || !passes || !ops_out)) return -fail(TQK_BAD_POINTER, "%s: null pointer", what);
+  constexpr int T = batch::kTileBits;
+  int np = 0;
+  for (int ci = 0; ci < ncirc; ++ci) {
+    tqk_batch_circuit& c = circuits[ci];
+    const int n = c.n;
+    if (n < 1 || n > TQK_BATCH_MAX_QUBITS) return -fail(TQK_TOO_MANY_QUBITS, "%s: circuit %d has n=%d", what, ci, n);
+    if (c.z_wire < 0 || c.z_wire >= n) return -fail(TQK_BAD_WIRES, "%s: circuit %d z_wire %d", what, ci, c.z_wire);
+    if (c.num_ops < 0 || c.first_op < 0 || (c.num_ops > 0 && !ops_in))
+      return -fail(TQK_BAD_SHAPE, "%s: circuit %d op range", what, ci);
+    for (int k = 0; k < c.num_ops; ++k) {
+      const tqk_batch_op& op = ops_in[c.first_op + k];
+      const bool two = op.kind == TQK_B_CTRL1 || op.kind == TQK_B_CZ || op.kind == TQK_B_CZ_LADDER;
+      if (op.kind < TQK_B_DENSE1 || op.kind > TQK_B_CZ_LADDER)
+        return -fail(TQK_BAD_SHAPE, "%s: circuit %d op %d kind %d", what, ci, k, op.kind);
+      if (op.w0 < 0 || op.w0 >= n || (two && (op.w1 < 0 || op.w1 >= n)))
+        return -fail(TQK_BAD_WIRES, "%s: circuit %d op %d wires out of range", what, ci, k);
+      if ((op.kind == TQK_B_CTRL1 || op.kind == TQK_B_CZ) && op.w0 == op.w1)
+        return -fail(TQK_BAD_WIRES, "%s: circuit %d op %d uses a wire twice", what, ci, k);
+      if (op.kind == TQK_B_CZ_LADDER && op.w1 <= op.w0)
+        return -fail(TQK_BAD_WIRES, "%s: circuit %d op %d ladder needs w0 < w1", what, ci, k);
+      if ((op.kind == TQK_B_DENSE1 || op.kind == TQK_B_CTRL1) && (op.mat < 0 || op.mat >= n_mats))
+        return -fail(TQK_BAD_SHAPE, "%s: circuit %d op %d matrix index %d (have %d)", what, ci, k, op.mat, n_mats);
+    }
+    c.first_pass = np;
+    const uint32_t full = (n >= 32) ? 0xffffffffu : ((1u << n) - 1u);
+    if (n <= T) {  // one tile, one pass
+      if (np >= max_passes) return -fail(TQK_SCRATCH_TOO_SMALL, "%s: more than %d passes", what, max_passes);
+      for (int k = 0; k < c.num_ops; ++k) ops_out[c.first_op + k] = ops_in[c.first_op + k];
+      passes[np++] = {c.first_op, c.num_ops, full, batch::kFirst | batch::kLast};
+    } else {
+      if (c.state_off < 0) return -fail(TQK_BAD_POINTER, "%s: circuit %d (n=%d) needs a state buffer", what, ci, n);
+      const uint32_t low = (1u << batch::kLowReserve) - 1u;
+      std::vector<int> pending(c.num_ops), rest;
+      for (int k = 0; k < c.num_ops; ++k) pending[k] = c.first_op + k;
+      int out = c.first_op;
+      do {
+        uint32_t tile = low, blocked = 0;
+        const int start = out;
+        rest.clear();
+        for (int idx : pending) {
+          uint32_t wb, tg;
+          batch::op_bits(ops_in[idx], n, &wb, &tg);
+          if ((wb & blocked) == 0u && __builtin_popcount(tile | tg) <= T) {
+            tile |= tg;
+            ops_out[out++] = ops_in[idx];
+          } else {  // stays for a later pass; later ops on these wires must wait too
+            blocked |= wb;
+            rest.push_back(idx);
+          }
+        }
+        for (int b = 0; b < n && __builtin_popcount(tile) < T; ++b) tile |= 1u << b;  // fill with low bits
+        if (np >= max_passes) return -fail(TQK_SCRATCH_TOO_SMALL, "%s: more than %d passes", what, max_passes);
+        passes[np++] = {start, out - start, tile & full, 0};
+        pending.swap(rest);
+      } while (!pending.empty());
+      passes[c.first_pass].flags |= batch::kFirst;
+      passes[np - 1].flags |= batch::kLast;
+    }
+    c.num_passes = np - c.first_pass;
+  }
+  return np;
+}
+
+extern "C" int64_t tqk_batch_items(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_pass* passes,
+                                   tqk_batch_item* items, int64_t max_items) {
+  const char* what = "tqk_batch_items";
+  if (ncirc < 0) return -fail(TQK_BAD_SHAPE, "%s: ncirc %d", what, ncirc);
+  if (ncirc > 0 && (!circuits || !passes || !items)) return -fail(TQK_BAD_POINTER, "%s: null pointer", what);
+  int max_np = 0;
+  for (int c = 0; c < ncirc; ++c) max_np = circuits[c].num_passes > max_np ? circuits[c].num_passes : max_np;
+  int64_t k = 0;
+  for (int w = 0; w < max_np; ++w) {
+    for (int c = 0; c < ncirc; ++c) {
+      if (w >= circuits[c].num_passes) continue;
+      const int pi = circuits[c].first_pass + w;
+      const int ntiles = 1 << (circuits[c].n - __builtin_popcount(passes[pi].tile_mask));
+      for (int t = 0; t < ntiles; ++t) {
+        if (k >= max_items) return -fail(TQK_SCRATCH_TOO_SMALL, "%s: more than %lld items", what, (long long)max_items);
+        items[k++] = {c, pi, t, 0};
+      }
+    }
+  }
+  return k;
+}
+
+extern "C" int tqk_batch_run(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops,
+                             const tqk_batch_pass* passes, const tqk_batch_item* items, int64_t n_items,
+                             const void* mats, void* states, int write_states, double* z_out, int* pass_done,
+                             uint64_t* t_done, int* counter, int* status, void* stream) {
+  const char* what = "tqk_batch_run";
+  if (ncirc <= 0 || n_items <= 0) return TQK_OK;
+  if (!circuits || !passes || !items || !z_out || !pass_done || !counter || !status)
+    return fail(TQK_BAD_POINTER, "%s: null pointer", what);
+  if (n_items > 0x7fffffff) return fail(TQK_BAD_SHAPE, "%s: too many items", what);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = sizeof(float2) << batch::kTileBits;
+  static int attr_dev = -1;
+  if (attr_dev != dev) {
+    cudaFuncSetAttribute(batch::k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    attr_dev = dev;
+  }
+  const int grid = n_items < sms ? static_cast<int>(n_items) : sms;
+  batch::k_batch<<<grid, batch::kThreads, smem, as_stream(stream)>>>(
+      circuits, ncirc, ops, passes, items, n_items, static_cast<const float2*>(mats), static_cast<float2*>(states),
+      write_states, z_out, pass_done, reinterpret_cast<unsigned long long*>(t_done), counter, status);
+  return launch_status(what);
+}
