@@ -18,6 +18,10 @@ Outputs (all small ``.npz`` files, committed):
   wire) + 2 x (``Op1QAllLayer(U3)`` + ``Op2QAllLayer(CNOT, circular)``) on 4 wires, bsz 32,
   Z expval per wire, forward and autograd backward, in the upstream default complex64
   and in complex128.
+* ``hea.npz`` -- the differentiation workload at reduced size (layered RY/RZ + CZ
+  ladder with shared parameters, optional per-sample RY input layer, weighted sum of
+  Pauli-string expvals): expvals and autograd gradients for the shared angles and the
+  inputs, complex64 and complex128.
 * ``known_answers.npz`` -- the upstream known-answer tests (``test/device/test_init.py:32``,
   ``test/functional/test_controlled_unitary.py:30``, ``test/functional/test_func_mat_exp.py:30``,
   ``test/operator/test_ControlledU.py:40``, ``test/operator/test_op_hamil_exp.py:32``) and the
@@ -259,6 +263,56 @@ def make_config1(rng):
     print("config1: done")
 
 
+def make_hea(rng):
+    """Differentiation workload at reduced size: optional per-sample RY(x) input layer,
+    then L layers of (RY on every wire, RZ on every wire, CZ ladder (i, i+1)) with one
+    shared [1, P] parameter row, loss = sum_b sum_j w_j <P_j>; upstream forward through
+    ``tqf.ry/rz/cz`` and autograd gradients for the shared angles and the inputs."""
+    out = {}
+    index = []
+    for ci, (n, bsz, layers, m, per_sample) in enumerate([(8, 4, 3, 10, True), (10, 2, 4, 12, True),
+                                                          (9, 3, 2, 8, False)]):
+        ncols = 2 * n * layers
+        theta = rng.uniform(-np.pi, np.pi, size=(1, ncols))
+        x = rng.uniform(0, np.pi, size=(bsz, n))
+        paulis = [random_pauli(rng, n) for _ in range(m)]
+        w = rng.normal(size=m)
+        key = f"h{ci}"
+        out[key + "__theta"], out[key + "__x"], out[key + "__weights"] = theta, x, w
+        for double in (False, True):
+            refimport.set_reference_precision(double)
+            fdt = torch.float64 if double else torch.float32
+            th = torch.tensor(theta, dtype=fdt, requires_grad=True)
+            xt = torch.tensor(x, dtype=fdt, requires_grad=True)
+            q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+            if double:
+                q.states = q.states.to(torch.complex128)
+            if per_sample:
+                for wi in range(n):
+                    tqf.ry(q, wires=wi, params=xt[:, wi:wi + 1])
+            off = 0
+            for _ in range(layers):
+                for fn in (tqf.ry, tqf.rz):
+                    for wi in range(n):
+                        fn(q, wires=wi, params=th[:, off:off + 1])
+                        off += 1
+                for wi in range(n - 1):
+                    tqf.cz(q, wires=[wi, wi + 1])
+            ev = torch.stack([expval_joint_analytical(q, p) for p in paulis], dim=-1)
+            (ev * torch.tensor(w, dtype=fdt)).sum().backward()
+            tag = "c128" if double else "c64"
+            out[f"{key}__{tag}__expval"] = ev.detach().numpy()
+            out[f"{key}__{tag}__grad_theta"] = th.grad.numpy()
+            if per_sample:
+                out[f"{key}__{tag}__grad_x"] = xt.grad.numpy()
+        index.append({"key": key, "n": n, "bsz": bsz, "layers": layers, "paulis": paulis,
+                      "per_sample": per_sample})
+    refimport.set_reference_precision(False)
+    out["__meta__"] = np.array(json.dumps(index))
+    np.savez_compressed(os.path.join(HERE, "hea.npz"), **out)
+    print(f"hea: {len(index)} cases")
+
+
 class _Recorder:
     """Wraps apply_unitary_bmm / check_all_close to capture what a test does."""
 
@@ -356,3 +410,4 @@ if __name__ == "__main__":
     make_circuits(np.random.default_rng(2))
     make_config1(np.random.default_rng(3))
     make_known_answers()
+    make_hea(np.random.default_rng(4))
