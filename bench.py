@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--depth", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the baseline sample")
+    ap.add_argument("--fuse", default="auto", help="fused block width 1..6 or auto (autotuner)")
     ap.add_argument("--quick", action="store_true", help="skip e2e/roofline/baseline (profiling runs)")
     ap.add_argument("--workload", default="random", choices=["random", "c1", "c3", "c4", "c5"],
                     help="random: the headline circuit (default); c1: small encoder+U3+CNOT model (n=4, bsz=32); "
@@ -223,14 +224,19 @@ def run_ours(args):
 
     def step(theta, method=args.method):
         q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
+        if method == "plain_gate_by_gate":  # the plain method without staged low-qubit runs
+            q.stage_low = False
         if method == "fused":
             q.method = "fused"
-            q.fuse_wires = 6
+            q.fuse_wires = args.fuse if args.fuse == "auto" else int(args.fuse)
         W.apply_circuit(q, gates, theta)
         pr = tq.probs(q)
         ev = tq.expval_joint_analytical_batch(q, paulis)
         (ev * pw).sum().backward()
+        last["q"] = q
         return ev, pr
+
+    last = {}
 
     barrier = R.barrier
 
@@ -252,33 +258,46 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     launches = _lib.LAUNCHES[0] - launches0
+    fusion_info = None
+    if args.method == "fused":
+        segs = last["q"]._tape
+        fusion_info = {"width": [getattr(sg, "fuse_width", None) for sg in segs],
+                       "passes": sum(len(sg.exec_ops) for sg in segs),
+                       "tensor_core_passes": sum(1 for sg in segs for op in sg.exec_ops if getattr(op, "tc", False)),
+                       "chosen_by": "autotuner (measured pass costs)" if args.fuse == "auto" else f"fixed k={args.fuse}"}
+    last.clear()
     ms = R.max_over_ranks(e0.elapsed_time(e1), dev)
     value = R.job_throughput(bsz * args.steps, world, ms / 1e3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": _config(args, args.method),
             "clocks": clk.summary(), "gpu_launches": launches}
+    if fusion_info:
+        line["config"]["fusion"] = fusion_info
     if world > 1:
         line["config"]["parallelism"] = f"replicas x{world} (batch sharding, no collective in the step)"
 
     _lib.check_status(dev)
     if args.method == "fused" and not args.quick and not args.no_plain:
-        # ---------------- the plain gate-by-gate method on the same workload
-        for _ in range(2):
-            th.grad = None
-            step(th, "plain")
-        torch.cuda.synchronize()
-        barrier()
-        e0.record(stream)
-        for _ in range(args.steps):
-            th.grad = None
-            step(th, "plain")
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms_plain = R.max_over_ranks(e0.elapsed_time(e1), dev)
-        v_plain = R.job_throughput(bsz * args.steps, world, ms_plain / 1e3)
-        line["plain_method"] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps}
-        line["fused_speedup_vs_plain"] = value / v_plain
+        # ---------------- the plain method on the same workload: with staged low-qubit
+        # runs (its default) and strictly gate by gate
+        for variant, key in (("plain", "plain_method"), ("plain_gate_by_gate", "plain_gate_by_gate")):
+            for _ in range(2):
+                th.grad = None
+                step(th, variant)
+            torch.cuda.synchronize()
+            barrier()
+            e0.record(stream)
+            for _ in range(args.steps):
+                th.grad = None
+                step(th, variant)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_plain = R.max_over_ranks(e0.elapsed_time(e1), dev)
+            v_plain = R.job_throughput(bsz * args.steps, world, ms_plain / 1e3)
+            line[key] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps}
+        line["fused_speedup_vs_plain"] = value / line["plain_gate_by_gate"]["value"]
+        line["fused_speedup_vs_plain_staged"] = value / line["plain_method"]["value"]
     if not args.quick:
         # ---------------- end to end through the public API with host buffers
         pin_theta = torch.from_numpy(theta_host).pin_memory()
@@ -359,6 +378,22 @@ def roofline(args, dev):
         "cnot_fwd": (lambda i: _lib.apply_mcx(psi, n, [pairs[i][0]], 1, pairs[i][1]), S),
         "cz_fwd": (lambda i: _lib.apply_phase(psi, n, list(pairs[i]), mat[:, 0, 0].contiguous(), bsz), S // 2),
     }
+    # a staged run of 8 dense one-qubit gates on the low wires: one pass (2S / 4S)
+    sdescs = []
+    for j in range(8):
+        d = _lib.StagedOp()
+        d.kind, d.nwires, d.batch, d.operand = _lib.S_DENSE1, 1, bsz, mat.data_ptr()
+        d.wires[0] = n - 1 - j
+        sdescs.append(d)
+    gstage = torch.zeros(8, bsz * 8, dtype=torch.float64, device=dev)
+    sdescs_g = []
+    for j, d in enumerate(sdescs):
+        e = _lib.StagedOp.from_buffer_copy(d)
+        e.grad = gstage[j].data_ptr()
+        sdescs_g.append(e)
+    tb = min(n, _lib.STAGED_MAX_TILE_BITS)
+    kernels["staged8_fwd"] = (lambda i: _lib.staged_apply(psi, n, sdescs, tb), 2 * S)
+    kernels["staged8_adj"] = (lambda i: _lib.staged_adjoint(psi, lam, n, sdescs_g, tb), 4 * S)
     for name, (fn, nbytes) in kernels.items():
         t = timeit(fn)
         gbs = nbytes / t / 1e9
@@ -561,9 +596,11 @@ def run_c5(args):
 def run_c4(args):
     """Uneven batching: 256 independent circuits, n ~ U{8..20}, L ~ U{2..40} layers of
     (RY, RZ on every wire, angles ~ U[-pi, pi); CZ ladder), output <Z_0> of each, run as
-    one persistent batch (tqk_batch_run).  value = circuits/s of the launch; e2e adds the
-    host compile (IR + plan) and the host<->device copies; latency = each circuit's
-    completion time after the launch started."""
+    one persistent kernel (tqk_batch_run) with the launch shape picked by the autotuner
+    and captured in a CUDA graph.  value = circuits/s of graph replays (device time);
+    e2e = new angles from the host every step (set_matrices: pinned host -> device),
+    replay, and <Z> + latencies read back; latency = each circuit's completion time
+    after the launch started."""
     import torch
 
     import torchquantum_gb300 as tq
@@ -573,24 +610,44 @@ def run_c4(args):
     rng = np.random.default_rng(0)
     specs = [(int(rng.integers(8, 21)), int(rng.integers(2, 41))) for _ in range(256)]
     angles = [(rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n))) for n, L in specs]
-
-    def build():
-        cb = B.CircuitBatch()
-        for (n, _), (ry, rz) in zip(specs, angles):
-            cb.add_layered(n, ry, rz)
-        return cb
-
+    cb = B.CircuitBatch()
+    for (n, _), (ry, rz) in zip(specs, angles):
+        cb.add_layered(n, ry, rz)
+    t0 = time.perf_counter()
+    pb = cb.prepare(dev, config="auto")
+    t_tune = time.perf_counter() - t0
+    pb.capture()
     for _ in range(args.warmup):
-        build().run(dev)
-    kms, wall, res = [], [], None
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = build().run(dev)
-        torch.cuda.synchronize()
-        wall.append(time.perf_counter() - t0)
-        kms.append(res.kernel_ms)
-    ms = float(np.sum(kms))
+        pb.launch()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for i in range(args.steps):
+        pb.graph.replay()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[-1])
+    pb.launch()
+    res = pb.result()
+    # end to end: new angles every step from the host, replay, read back
+    new_mats = [np.concatenate([B.layered_matrices(n, rng.uniform(-np.pi, np.pi, (L, n)),
+                                                   rng.uniform(-np.pi, np.pi, (L, n))) for n, L in specs])
+                for _ in range(2)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        pb.set_matrices(new_mats[i % 2])
+        pb.launch()
+        pb.result()
+    e2e_s = time.perf_counter() - t0
+    h2d = int(new_mats[0].size * 8)  # complex64 matrices
+    # default launch shape (no tuning, no graph) for comparison
+    cb0 = B.CircuitBatch()
+    for (n, _), (ry, rz) in zip(specs, angles):
+        cb0.add_layered(n, ry, rz)
+    pd = cb0.prepare(dev, config=B.DEFAULT_CONFIG)
+    dms, _ = _timed(pd.launch, args.steps, args.warmup, dev)
     # the same circuits one at a time through the engine (fused method), on a sample
     sample = list(range(0, 256, 16))
     torch.cuda.synchronize()
@@ -608,13 +665,20 @@ def run_c4(args):
         tq.expval_joint_analytical(q, "Z" + "I" * (n - 1))
     torch.cuda.synchronize()
     per_circuit_engine = (time.perf_counter() - t0) / len(sample)
+    cfg = pb.config
     _line(args, {"workload": "256 circuits, n~U{8..20}, L~U{2..40} x (RY, RZ per wire; CZ ladder), <Z_0> each, one "
-                             "persistent batch", "circuits": 256, "n_range": [8, 20], "layers_range": [2, 40]},
+                             "persistent kernel in a CUDA graph", "circuits": 256, "n_range": [8, 20],
+                 "layers_range": [2, 40],
+                 "launch_shape": {"tile_bits": cfg.tile_bits, "threads": cfg.threads, "ctas_per_sm": cfg.ctas_per_sm,
+                                  "chosen_by": "autotuner (measured candidates)", "tuning_s": t_tune}},
           256 * args.steps / (ms / 1e3), ms,
-          {"e2e": {"value": 256 * args.steps / float(np.sum(wall)), "unit": UNIT, "includes": "host IR build + plan + "
-                   "copies + launch + read-back"},
+          {"e2e": {"value": 256 * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": 256 * 8 + 257 * 8,
+                   "includes": "new angles host->device, graph replay, <Z> and latencies device->host"},
            "latency_ms": {"p50": float(np.percentile(res.latency_ms, 50)), "p99": float(np.percentile(res.latency_ms, 99)),
                           "max": float(res.latency_ms.max())},
+           "default_launch_shape": {"circuits_per_s": 256 * args.steps / (dms / 1e3), "tile_bits": 14, "threads": 512,
+                                    "ctas_per_sm": 1, "graph": False},
            "engine_one_circuit_at_a_time": {"circuits_per_s": 1.0 / per_circuit_engine,
                                             "sample": f"{len(sample)} of the 256 circuits, fused method, sequential"}})
 

@@ -88,6 +88,15 @@ int tqk_reset(void* state, int64_t bsz, int n, const int32_t* wires, int k, void
  * |psi|^2 as float32 [bsz, 2^n] (the probabilities read by measurements.py:297-299). */
 int tqk_probs(const void* state, int64_t bsz, int n, float* out, void* stream);
 
+/* Computational-basis sampling (upstream tq.measure, measurement/measurements.py:37-74,
+ * draws on the host with random.choices).  For every row b and shot s, out[b*shots + s]
+ * is the first index i with sum_{j<=i} |psi_j|^2 > uniforms[b*shots + s] * sum_j |psi_j|^2
+ * (inverse CDF in float64; uniforms in [0, 1) from the caller).  scratch: at least
+ * tqk_sample_scratch_bytes(bsz, n) bytes of device memory. */
+int64_t tqk_sample_scratch_bytes(int64_t bsz, int n);
+int tqk_sample(const void* state, int64_t bsz, int n, const double* uniforms, int64_t shots, int64_t* out,
+               void* scratch, int64_t scratch_bytes, void* stream);
+
 /* Expectation values of m Pauli strings, out[b*m + j] = Re <psi_b| P_j |psi_b> (float64).
  * P_j is given by bit masks over the in-row index (bit n-1-w <-> wire w):
  * xmask = X|Y positions, zmask = Z|Y positions; the i^(#Y) factor is applied.
@@ -231,11 +240,47 @@ int tqk_block_build(const tqk_block_desc* blocks, int nblocks, int max_batch, co
 int tqk_block_unbuild(const tqk_block_desc* blocks, int nblocks, int max_batch,
                       const tqk_block_op* ops, void* stream);
 
+/* ---------------------------------------------------------------------------------
+ * Staged low-qubit runs (plain method).  Upstream applies every gate as its own
+ * permute + bmm pass (functional/gate_wrapper.py:96-140); tqk_staged_apply applies a run
+ * of up to TQK_STAGED_MAX_OPS consecutive ops whose targets lie in the lowest tile_bits
+ * bits of the amplitude index (wires n - tile_bits .. n - 1) in ONE pass: each CTA loads
+ * contiguous tiles of 2^tile_bits amplitudes of a batch row into shared memory (128-bit
+ * loads), applies the ops in order there, and writes the tiles back.  Controls, phase
+ * wires and diagonal wires may be anywhere.  tqk_staged_adjoint is the matching reverse
+ * step of the adjoint method on (psi, lam): ops in reverse order, psi <- U^H psi,
+ * lam <- U^H lam, and for every op with a grad slot the operand cotangent
+ * sum lam_in conj(psi_out) added in float64 (as tqk_adjoint_matrix / _phase / _diagonal
+ * do for one op).  Ops whose uncompute is not U^H (non-unitary) must not be staged. */
+enum { TQK_S_DENSE1 = 0, TQK_S_X = 1, TQK_S_PHASE = 2, TQK_S_DIAG = 3 };
+enum { TQK_STAGED_MAX_OPS = 64, TQK_STAGED_MAX_TILE_BITS = 12, TQK_STAGED_MAX_WIRES = 8 };
+
+typedef struct {
+  int32_t kind;        /* TQK_S_DENSE1: 2x2 on wires[nwires-1] where every control wires[0..nwires-1)
+                          is 1;  TQK_S_X: flip wires[nwires-1] where every control equals ctrl_val;
+                          TQK_S_PHASE: multiply by a phase where every wire is 1;
+                          TQK_S_DIAG: diagonal (2^nwires entries, nwires <= 2, wires[0] = MSB) */
+  int32_t nwires;      /* 1..TQK_STAGED_MAX_WIRES */
+  int32_t wires[TQK_STAGED_MAX_WIRES];
+  int32_t ctrl_val;    /* X only: 1 or 0 */
+  int32_t pad;
+  const void* operand; /* complex64: DENSE1 [batch][2][2], PHASE [batch], DIAG [batch][2^nwires]; X: NULL */
+  int64_t batch;       /* 1 (shared by every row) or bsz */
+  double* grad;        /* adjoint only: complex128 cotangent of the operand (interleaved, same shape
+                          as the operand), or NULL */
+} tqk_staged_op; /* 72 bytes */
+
+int tqk_staged_apply(void* state, int64_t bsz, int n, const tqk_staged_op* ops, int nops, int tile_bits,
+                     void* stream);
+int tqk_staged_adjoint(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op* ops, int nops,
+                       int tile_bits, void* stream);
+
 /* ---------------------------------------------------------------- persistent circuit batches
  * Many independent circuits of different sizes (n <= 24) in one launch.  tqk_batch_plan
- * splits each circuit into passes whose target bits fit a tile of 2^14 amplitudes held in
- * shared memory (circuits with n <= 14: one pass, one tile, never touching HBM; larger
- * ones stream their state, states + state_off, once per pass).  tqk_batch_items lists the
+ * splits each circuit into passes whose target bits fit a tile of 2^tile_bits amplitudes
+ * (tile_bits 10..14) held in shared memory (circuits with n <= tile_bits: one pass, one
+ * tile, never touching HBM; larger ones stream their state, states + state_off, once per
+ * pass).  tqk_batch_items lists the
  * work: one item per (circuit, pass, tile), in waves of pass index, so a pass's tiles run
  * on many SMs at once.  One persistent CTA per SM takes items in order; an item of pass
  * p > 0 first waits (bounded) until every tile of pass p - 1 of its circuit is done.
@@ -267,7 +312,7 @@ typedef struct {
 typedef struct {
   int32_t first_op;   /* into the planned op array */
   int32_t num_ops;
-  uint32_t tile_mask; /* amplitude-index bits inside the tile (min(n, 14) of them) */
+  uint32_t tile_mask; /* amplitude-index bits inside the tile (min(n, tile_bits) of them) */
   int32_t flags;      /* 1: first pass (starts from |0..0>), 2: last pass (reduces <Z>) */
 } tqk_batch_pass; /* 16 bytes */
 
@@ -278,13 +323,20 @@ typedef struct {
   int32_t pad;
 } tqk_batch_item; /* 16 bytes */
 
+typedef struct {
+  int32_t tile_bits;   /* 10..14: tile of 2^tile_bits amplitudes; must equal the plan's */
+  int32_t threads;     /* threads per CTA: 128, 256 or 512 */
+  int32_t ctas_per_sm; /* persistent CTAs per SM, 1..8 (clamped to what fits) */
+  int32_t pad;
+} tqk_batch_config; /* 16 bytes; NULL = {14, 512, 1} */
+
 /* Host only (no GPU work): validate `circuits` and their ops (matrix indices < n_mats),
  * write each circuit's passes into passes[0 .. return value) and its ops, regrouped by
  * pass (ops that commute may move across passes), into ops_out at the same positions;
  * fills first_pass/num_passes.  Returns the number of passes, or -TQK_* on error
  * (-TQK_SCRATCH_TOO_SMALL if more than max_passes are needed). */
 int tqk_batch_plan(tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops_in, int n_mats,
-                   tqk_batch_op* ops_out, tqk_batch_pass* passes, int max_passes);
+                   tqk_batch_op* ops_out, tqk_batch_pass* passes, int max_passes, int tile_bits);
 /* Host only: the work items of planned circuits in dispatch order (wave w = every
  * circuit's w-th pass, circuits in array order, tiles ascending); returns their number,
  * or -TQK_SCRATCH_TOO_SMALL if more than max_items. */
@@ -294,11 +346,16 @@ int64_t tqk_batch_items(const tqk_batch_circuit* circuits, int ncirc, const tqk_
  * (complex64 [*, 2, 2]), states (complex64; may be NULL if no circuit needs one),
  * z_out[ncirc], pass_done[npasses] and counter (one int) all zeroed by the caller before
  * each launch, t_done[ncirc + 1] or NULL, status (device int; TQK_TIMEOUT if a wait gave
- * up).  write_states != 0 stores every final state. */
+ * up, TQK_BAD_SHAPE if a pass is wider than config->tile_bits).  write_states != 0 stores
+ * every final state.  config: tile size (the one the plan used), CTA shape and CTAs per
+ * SM (host-side autotuning picks them); NULL for the defaults.  The launch is a single
+ * kernel on `stream` with no host synchronisation, so it can be captured in a CUDA
+ * graph once a first launch of the same variant has run on the device uncaptured. */
 int tqk_batch_run(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops,
                   const tqk_batch_pass* passes, const tqk_batch_item* items, int64_t n_items,
                   const void* mats, void* states, int write_states, double* z_out, int* pass_done,
-                  uint64_t* t_done, int* counter, int* status, void* stream);
+                  uint64_t* t_done, int* counter, int* status, const tqk_batch_config* config,
+                  void* stream);
 
 #ifdef __cplusplus
 }

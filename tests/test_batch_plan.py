@@ -4,8 +4,9 @@ planner (tqk_batch_plan, host code in libtqk.so) checked with the oracle.
 * the IR a gate list compiles to (fused one-qubit matrices, controlled blocks, CZ)
   simulates to the oracle's state;
 * the planner only regroups ops of one circuit, keeps every pass's targets inside its
-  tile of 2^14 amplitudes (with address bits 0-4, for coalescing), flags the first and
-  last passes, and its regrouped order simulates to the same state as the original;
+  tile of 2^tile_bits amplitudes (tile_bits 10, 12, 14; with address bits 0-4, for
+  coalescing), flags the first and last passes, and its regrouped order simulates to
+  the same state as the original;
 * invalid circuits are rejected with the library's status codes.
 """
 import numpy as np
@@ -80,17 +81,19 @@ def test_layered_ir_matches_gate_list():
     np.testing.assert_allclose(got, O.run(n, 1, gates)[0], atol=1e-6)
 
 
-def test_plan_regroups_legally():
+@pytest.mark.parametrize("tile_bits", [10, 12, 14])
+def test_plan_regroups_legally(tile_bits):
+    T = tile_bits
     rng = np.random.default_rng(3)
     cb = B.CircuitBatch()
-    sizes = [15, 4, 16, 12, 17]
+    sizes = [15, 4, 16, 12, 17, 11]
     for n in sizes:
         if n % 2:
             L = int(rng.integers(2, 5))
             cb.add_layered(n, rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n)), z_wire=n - 1)
         else:
             cb.add_gates(n, _random_gates(rng, n, 40))
-    circ, ops, passes, items, mats, order, state_amps = cb.compile()
+    circ, ops, passes, items, mats, order, state_amps = cb.compile(tile_bits=T)
     # work items: one per (circuit, pass, tile); a pass's items come after all items of
     # the circuit's previous pass
     seen = {}
@@ -106,7 +109,7 @@ def test_plan_regroups_legally():
             if w:
                 assert min(ks) > max(seen[pi - 1])
     assert sorted(order) == list(range(len(sizes)))
-    assert state_amps == sum(1 << n for n in sizes if n > B.TILE_BITS)
+    assert state_amps == sum(1 << n for n in sizes if n > T)
     for slot, i in enumerate(order):
         c = circ[slot]
         n = int(c["n"])
@@ -120,8 +123,8 @@ def test_plan_regroups_legally():
         covered = 0
         for p in ps:
             tm = int(p["tile_mask"])
-            assert bin(tm).count("1") == min(n, B.TILE_BITS) and tm < (1 << n)
-            if n > B.TILE_BITS:
+            assert bin(tm).count("1") == min(n, T) and tm < (1 << n)
+            if n > T:
                 assert tm & 0x1F == 0x1F
             for op in ops[p["first_op"]:p["first_op"] + p["num_ops"]]:
                 k = int(op["kind"])
@@ -161,5 +164,10 @@ def test_plan_rejects_invalid():
         cb.compile()
     with pytest.raises(ValueError):
         B.CircuitBatch().add_ops(25, np.zeros(0, B.OP_T), np.zeros((0, 2, 2)))
+    cb = B.CircuitBatch()
+    cb.add_ops(3, np.array([(B.DENSE1, 0, 0, 0)], dtype=B.OP_T), np.eye(2)[None])
+    for bad in (9, 15):
+        with pytest.raises(_lib.TQKError, match="BAD_SHAPE"):
+            cb.compile(tile_bits=bad)
     with pytest.raises(ValueError, match="not supported"):
         B.CircuitBatch().add_gates(3, [{"name": "swap", "wires": [0, 1], "params": None}])

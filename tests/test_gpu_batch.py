@@ -64,3 +64,75 @@ def test_uneven_batch_vs_oracle():
             gates += [{"name": "cz", "wires": [w, w + 1], "params": None} for w in range(n - 1)]
         assert abs(z - _z(O.run(n, 1, gates)[0], n, 0)) < 2e-5
     assert res.kernel_ms > 0 and np.isfinite(res.latency_ms).all()
+
+
+def _layered_ref(n, ry, rz):
+    gates = []
+    for l in range(ry.shape[0]):
+        gates += [{"name": "ry", "wires": [w], "params": np.array([[ry[l, w]]])} for w in range(n)]
+        gates += [{"name": "rz", "wires": [w], "params": np.array([[rz[l, w]]])} for w in range(n)]
+        gates += [{"name": "cz", "wires": [w, w + 1], "params": None} for w in range(n - 1)]
+    return O.run(n, 1, gates)[0]
+
+
+def _layered_batch(rng, sizes, L):
+    from torchquantum_gb300 import batch as B
+
+    cb = B.CircuitBatch()
+    spec = []
+    for n in sizes:
+        ry, rz = rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n))
+        cb.add_layered(n, ry, rz)
+        spec.append((n, ry, rz))
+    return cb, spec
+
+
+@pytest.mark.parametrize("cfg_idx", range(6))
+def test_every_launch_shape_vs_oracle(cfg_idx):
+    """Each candidate the autotuner may pick (tile 2^11..2^14, 128..512 threads, 1..8 CTAs
+    per SM) gives the oracle's states: tiles narrower than a circuit split it into more
+    passes."""
+    from torchquantum_gb300 import autotune as A
+
+    cands = A.batch_candidates(17)
+    if cfg_idx >= len(cands):
+        pytest.skip("fewer candidates")
+    cfg = cands[cfg_idx]
+    rng = np.random.default_rng(20 + cfg_idx)
+    cb, spec = _layered_batch(rng, [5, 9, 11, 12, 13, 15, 17], 3)
+    res = cb.run(return_states=True, config=cfg)
+    for (n, ry, rz), z, st in zip(spec, res.z, res.states):
+        ref = _layered_ref(n, ry, rz)
+        np.testing.assert_allclose(st.cpu().numpy(), ref, atol=2e-5)
+        assert abs(z - _z(ref, n, 0)) < 2e-5
+
+
+def test_graph_replay_autotuned_and_new_angles(tmp_path, monkeypatch):
+    """config="auto" picks a launch shape by timing the candidates; the batch is captured
+    in a CUDA graph; replays give the same <Z>; set_matrices + replay gives the oracle's
+    values for new angles."""
+    from torchquantum_gb300 import autotune as A
+    from torchquantum_gb300 import batch as B
+
+    monkeypatch.setenv("TQ_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    A.clear()
+    rng = np.random.default_rng(7)
+    sizes = [int(rng.integers(8, 17)) for _ in range(24)]
+    cb, spec = _layered_batch(rng, sizes, 4)
+    pb = cb.prepare(config="auto").capture()
+    assert A.lookup(next(k for k in A._MEM if k.startswith("batch|")))["config"]["tile_bits"] == pb.config.tile_bits
+    pb.launch()
+    z1 = pb.result().z
+    pb.launch()
+    r2 = pb.result()
+    np.testing.assert_allclose(z1, r2.z, atol=1e-12)  # multi-tile circuits add partials atomically
+    for (n, ry, rz), z in zip(spec, z1):
+        assert abs(z - _z(_layered_ref(n, ry, rz), n, 0)) < 2e-5
+    new = [(n, rng.uniform(-np.pi, np.pi, (4, n)), rng.uniform(-np.pi, np.pi, (4, n))) for n in sizes]
+    pb.set_matrices(np.concatenate([B.layered_matrices(n, ry, rz) for n, ry, rz in new]))
+    pb.launch()
+    r3 = pb.result()
+    for (n, ry, rz), z in zip(new, r3.z):
+        assert abs(z - _z(_layered_ref(n, ry, rz), n, 0)) < 2e-5
+    assert r3.kernel_ms > 0 and (r3.latency_ms > 0).all()
+    A.clear()

@@ -223,3 +223,36 @@ def test_fused_tensor_core_gradients_vs_plain():
     assert np.abs(evs["fused"] - evs["plain"]).max() < 1e-5
     for gp, gf in zip(grads["plain"], grads["fused"]):
         assert np.abs(gf - gp).max() < 1e-5
+
+
+def test_autotuned_fusion_vs_oracle(tmp_path, monkeypatch):
+    """fuse_wires="auto": the width / planner / kernel choice made from measured pass
+    costs gives the oracle's state and the plain method's gradients."""
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import autotune as A
+    from torchquantum_gb300 import workloads as W
+
+    monkeypatch.setenv("TQ_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    A.clear()
+    dev = torch.device("cuda")
+    n, bsz = 14, 3
+    gates, ncols = W.random_circuit(n, 120, seed=3)
+    theta = W.random_params(bsz, ncols, seed=4)
+    paulis = W.random_paulis(n, 4, seed=5)
+    res = {}
+    for method in ("fused", "plain"):
+        th = torch.tensor(theta, device=dev, requires_grad=True)
+        q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
+        q.method = method
+        W.apply_circuit(q, gates, th)
+        ev = tq.expval_joint_analytical_batch(q, paulis)
+        ev.sum().backward()
+        res[method] = (q.get_states_1d().detach().cpu().numpy(), th.grad.cpu().numpy())
+        if method == "fused":
+            seg = q._tape[0]
+            assert seg.fuse_width in (4, 5, 6) and any(getattr(op, "members", None) for op in seg.exec_ops)
+    ref = O.run(n, bsz, W.oracle_gates(gates, theta))
+    assert np.abs(res["fused"][0] - ref).max() < 1e-5
+    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-4
+    assert any(k.startswith("fusion|") for k in A._MEM)
+    A.clear()

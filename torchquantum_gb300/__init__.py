@@ -18,6 +18,8 @@ from . import layers as layer  # noqa: F401
 from .layers import *  # noqa: F401,F403
 from .encoding import GeneralEncoder, StateEncoder, Encoder  # noqa: F401
 from .measurement import expval_joint_analytical, expval_joint_analytical_batch, expval, MeasureAll, probs  # noqa
+from .measurement import measure, gen_bitstrings, MeasureMultipleTimes, MeasureMultiPauliSum, \
+    MeasureMultiQubitPauliSum  # noqa: F401
 from . import measurement  # noqa: F401
 
 _bind_gate_methods()

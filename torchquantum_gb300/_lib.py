@@ -57,9 +57,13 @@ _SIGS = {
     "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_fused_image_bytes": (_i64, [_i64]),
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp, _vp]),
-    "tqk_batch_plan": (_int, [_vp, _int, _vp, _int, _vp, _vp, _int]),
+    "tqk_sample_scratch_bytes": (_i64, [_i64, _int]),
+    "tqk_sample": (_int, [_vp, _i64, _int, _vp, _i64, _vp, _vp, _i64, _vp]),
+    "tqk_staged_apply": (_int, [_vp, _i64, _int, _vp, _int, _int, _vp]),
+    "tqk_staged_adjoint": (_int, [_vp, _vp, _i64, _int, _vp, _int, _int, _vp]),
+    "tqk_batch_plan": (_int, [_vp, _int, _vp, _int, _vp, _vp, _int, _int]),
     "tqk_batch_items": (_i64, [_vp, _int, _vp, _vp, _i64]),
-    "tqk_batch_run": (_int, [_vp, _int, _vp, _vp, _vp, _i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "tqk_batch_run": (_int, [_vp, _int, _vp, _vp, _vp, _i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
     "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
     "tqk_pauli_expval_noalloc_capacity": (_i64, []),
@@ -224,6 +228,44 @@ def adjoint_phase(psi, lam, n, wires, phase, phase_batch, grad):
                                     phase.data_ptr(), phase_batch, _ptr(grad), _stream(psi)))
 
 
+def sample(state, n, uniforms):
+    """Inverse-CDF draws: state [bsz, 2^n] complex64, uniforms [bsz, shots] float64 in
+    [0, 1) -> outcome indices [bsz, shots] int64 (wire 0 = most significant bit)."""
+    lib = load()
+    bsz, shots = uniforms.shape
+    out = torch.empty(bsz, shots, dtype=torch.int64, device=state.device)
+    nbytes = lib.tqk_sample_scratch_bytes(bsz, n)
+    scratch = torch.empty(max(1, nbytes // 8), dtype=torch.float64, device=state.device)
+    _check(lib.tqk_sample(state.data_ptr(), bsz, n, uniforms.data_ptr(), shots, out.data_ptr(), scratch.data_ptr(),
+                          nbytes, _stream(state)), launches=3)
+    return out
+
+
+class StagedOp(ctypes.Structure):
+    """``tqk_staged_op``: one op of a staged low-qubit run."""
+    _fields_ = [("kind", ctypes.c_int32), ("nwires", ctypes.c_int32), ("wires", ctypes.c_int32 * 8),
+                ("ctrl_val", ctypes.c_int32), ("pad", ctypes.c_int32), ("operand", ctypes.c_void_p),
+                ("batch", ctypes.c_int64), ("grad", ctypes.c_void_p)]
+
+
+assert ctypes.sizeof(StagedOp) == 72
+S_DENSE1, S_X, S_PHASE, S_DIAG = 0, 1, 2, 3
+STAGED_MAX_OPS, STAGED_MAX_TILE_BITS, STAGED_MAX_WIRES = 64, 12, 8
+
+
+def staged_apply(state, n, ops, tile_bits):
+    """Apply a run of ``StagedOp`` (sequence) in one shared-memory pass."""
+    arr = (StagedOp * max(1, len(ops)))(*ops)
+    _check(load().tqk_staged_apply(state.data_ptr(), state.shape[0], n, arr, len(ops), tile_bits, _stream(state)))
+
+
+def staged_adjoint(psi, lam, n, ops, tile_bits):
+    """Reverse step of a staged run on (psi, lam); ops carry their cotangent slots."""
+    arr = (StagedOp * max(1, len(ops)))(*ops)
+    _check(load().tqk_staged_adjoint(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, arr, len(ops), tile_bits,
+                                     _stream(psi)))
+
+
 def adjoint_diagonal(psi, lam, n, wires, diag, diag_batch, grad):
     _check(load().tqk_adjoint_diagonal(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, _i32(wires), len(wires),
                                        diag.data_ptr(), diag_batch, _ptr(grad), _stream(psi)))
@@ -234,7 +276,9 @@ _STATUS = {}
 
 
 def status_word(device) -> torch.Tensor:
-    """Per-device int32 the tensor-core kernels write TQK_TIMEOUT into on a bounded-wait timeout."""
+    """Per-device int32 that kernels with device-side checks write a status code into
+    (TQK_TIMEOUT when a bounded wait gave up, TQK_BAD_SHAPE when a batch work item does
+    not fit the launch's tile)."""
     key = str(device)
     t = _STATUS.get(key)
     if t is None:
@@ -249,7 +293,9 @@ def check_status(device) -> None:
     v = int(t.item())
     if v != 0:
         t.zero_()
-        raise TQKError(v, "a tensor-core kernel gave up waiting on its pipeline (bounded wait timed out)")
+        why = {6: "a kernel gave up waiting on its pipeline or a dependency (bounded wait timed out)",
+               2: "a circuit-batch work item was wider than the launch's tile (plan/config mismatch)"}
+        raise TQKError(v, why.get(v, "a kernel reported a device-side error"))
 
 
 def fused_prepare(u128: torch.Tensor, wires: Sequence[int]) -> torch.Tensor:

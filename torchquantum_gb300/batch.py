@@ -26,10 +26,28 @@ CIRC_T = np.dtype([("n", "<i4"), ("z_wire", "<i4"), ("first_op", "<i4"), ("num_o
                    ("first_pass", "<i4"), ("num_passes", "<i4")])
 PASS_T = np.dtype([("first_op", "<i4"), ("num_ops", "<i4"), ("tile_mask", "<u4"), ("flags", "<i4")])
 ITEM_T = np.dtype([("circuit", "<i4"), ("pass", "<i4"), ("tile", "<i4"), ("pad", "<i4")])
+CONFIG_T = np.dtype([("tile_bits", "<i4"), ("threads", "<i4"), ("ctas_per_sm", "<i4"), ("pad", "<i4")])
 DENSE1, CTRL1, CZ, CZ_LADDER = 0, 1, 2, 3
-TILE_BITS = 14
+TILE_BITS = 14            # default (and largest) tile: 2^14 amplitudes = 128 KB of shared memory
+MIN_TILE_BITS = 10
 MAX_QUBITS = 24
 _X = np.array([[0, 1], [1, 0]], dtype=np.complex128)
+
+
+@dataclass(frozen=True)
+class BatchConfig:
+    """Launch shape of a circuit batch: shared-memory tile of 2^tile_bits amplitudes
+    (circuits with n <= tile_bits run in one tile), threads per CTA and persistent CTAs
+    per SM.  Chosen by ``autotune.tune_batch`` or given explicitly."""
+    tile_bits: int = TILE_BITS
+    threads: int = 512
+    ctas_per_sm: int = 1
+
+    def as_struct(self) -> np.ndarray:
+        return np.array([(self.tile_bits, self.threads, self.ctas_per_sm, 0)], dtype=CONFIG_T)
+
+
+DEFAULT_CONFIG = BatchConfig()
 
 
 @dataclass
@@ -38,6 +56,19 @@ class BatchResult:
     latency_ms: np.ndarray               # completion time of each circuit after the launch started
     kernel_ms: float                     # device time of the launch (CUDA events)
     states: Optional[List[torch.Tensor]]  # final states (complex64 [2^n]) if requested
+
+
+def layered_matrices(n: int, ry: np.ndarray, rz: np.ndarray) -> np.ndarray:
+    """The [L * n, 2, 2] matrices RZ(rz[l, w]) RY(ry[l, w]) of ``add_layered`` (row-major
+    over (layer, wire)); also what ``PreparedBatch.set_matrices`` takes for new angles."""
+    ry = np.asarray(ry, np.float64).reshape(-1, n)
+    rz = np.asarray(rz, np.float64).reshape(-1, n)
+    c, s = np.cos(ry / 2), np.sin(ry / 2)
+    em, ep = np.exp(-0.5j * rz), np.exp(0.5j * rz)
+    m = np.empty(ry.shape + (2, 2), dtype=np.complex128)
+    m[..., 0, 0], m[..., 0, 1] = em * c, -em * s
+    m[..., 1, 0], m[..., 1, 1] = ep * s, ep * c
+    return m.reshape(-1, 2, 2)
 
 
 class CircuitBatch:
@@ -115,14 +146,8 @@ class CircuitBatch:
     def add_layered(self, n: int, ry: np.ndarray, rz: np.ndarray, z_wire: int = 0) -> int:
         """L layers of (RY(ry[l, w]), RZ(rz[l, w]) on every wire w, then CZ(w, w+1) for
         w = 0..n-2): one fused 2x2 per (layer, wire) and one CZ-ladder op per layer."""
-        ry = np.asarray(ry, np.float64).reshape(-1, n)
-        rz = np.asarray(rz, np.float64).reshape(-1, n)
-        L = ry.shape[0]
-        c, s = np.cos(ry / 2), np.sin(ry / 2)
-        em, ep = np.exp(-0.5j * rz), np.exp(0.5j * rz)
-        m = np.empty((L, n, 2, 2), dtype=np.complex128)  # RZ(b) RY(a)
-        m[..., 0, 0], m[..., 0, 1] = em * c, -em * s
-        m[..., 1, 0], m[..., 1, 1] = ep * s, ep * c
+        m = layered_matrices(n, ry, rz)
+        L = m.shape[0] // n
         per = n + (1 if n >= 2 else 0)
         ops = np.zeros(L * per, dtype=OP_T)
         ops = ops.reshape(L, per)
@@ -134,12 +159,26 @@ class CircuitBatch:
             ops["w0"][:, n] = 0
             ops["w1"][:, n] = n - 1
             ops["mat"][:, n] = -1
-        return self.add_ops(n, ops.reshape(-1), m.reshape(-1, 2, 2), z_wire)
+        return self.add_ops(n, ops.reshape(-1), m, z_wire)
 
     # ------------------------------------------------------------------ execution
-    def compile(self, return_states: bool = False):
+    def signature(self) -> tuple:
+        """Coarse shape of the batch (for the autotuner's cache): circuit count and
+        per-width-band counts and work, bucketed by powers of two."""
+        def b2(x):
+            return int(np.log2(max(1, x)))
+        bands = [(1, 10), (11, 12), (13, 14), (15, 17), (18, 20), (21, 24)]
+        sig = [b2(len(self._n))]
+        for lo, hi in bands:
+            idx = [i for i, n in enumerate(self._n) if lo <= n <= hi]
+            work = sum(len(self._ops[i]) << self._n[i] for i in idx)
+            sig += [b2(len(idx) + 1), b2(work + 1)]
+        return tuple(sig)
+
+    def compile(self, return_states: bool = False, tile_bits: int = TILE_BITS):
         """Host tables in execution order (costly circuits first): circuits, planned ops,
-        passes, matrices, the execution order and the state buffer size (amplitudes)."""
+        passes, work items, matrices, the execution order and the state buffer size
+        (amplitudes), for tiles of 2^tile_bits amplitudes."""
         nc = len(self._n)
         cost = [len(o) * (1 << n) for o, n in zip(self._ops, self._n)]
         order = sorted(range(nc), key=lambda i: -cost[i])
@@ -152,7 +191,7 @@ class CircuitBatch:
             o = self._ops[i].copy()
             o["mat"] = np.where(o["mat"] >= 0, o["mat"] + nmats, -1)
             circ[slot] = (n, self._z[i], nops, len(o), -1, 0, 0)
-            if return_states or n > TILE_BITS:
+            if return_states or n > tile_bits:
                 circ[slot]["state_off"] = state_amps
                 state_amps += 1 << n
             ops_l.append(o)
@@ -166,7 +205,8 @@ class CircuitBatch:
         passes = np.zeros(max(1, max_passes), dtype=PASS_T)
         lib = _lib.load()
         npass = lib.tqk_batch_plan(circ.ctypes.data, nc, ops_in.ctypes.data if len(ops_in) else None, len(mats),
-                                   ops_out.ctypes.data if len(ops_out) else None, passes.ctypes.data, max_passes)
+                                   ops_out.ctypes.data if len(ops_out) else None, passes.ctypes.data, max_passes,
+                                   int(tile_bits))
         if npass < 0:
             raise _lib.TQKError(-npass, lib.tqk_last_error().decode())
         passes = passes[:npass]
@@ -178,48 +218,132 @@ class CircuitBatch:
             raise _lib.TQKError(-got, lib.tqk_last_error().decode())
         return circ, ops_out, passes, items[:got], mats, order, state_amps
 
-    def run(self, device=None, return_states: bool = False) -> BatchResult:
+    def prepare(self, device=None, return_states: bool = False, config=None) -> "PreparedBatch":
+        """Compile and upload the batch once; the result launches (or replays a CUDA graph
+        of) the persistent kernel any number of times.  ``config``: a ``BatchConfig``,
+        ``"auto"`` (the autotuner's choice, measured on this device and cached) or None
+        (defaults)."""
         dev = torch.device(device if device is not None else "cuda")
         if dev.type != "cuda":
             raise _lib.TQKError(8, "circuit batches run on a CUDA device only")
-        nc = len(self._n)
-        if nc == 0:
+        if isinstance(config, str):
+            if config != "auto":
+                raise ValueError(f"config must be a BatchConfig, 'auto' or None (got {config!r})")
+            from . import autotune
+
+            config = autotune.tune_batch(self, dev, return_states)
+        return PreparedBatch(self, dev, return_states, config or DEFAULT_CONFIG)
+
+    def run(self, device=None, return_states: bool = False, config=None) -> BatchResult:
+        """Compile, upload and launch once (see ``prepare`` for repeated launches)."""
+        if len(self._n) == 0:
             return BatchResult(np.zeros(0), np.zeros(0), 0.0, [] if return_states else None)
-        circ, ops, passes, items, mats, order, state_amps = self.compile(return_states)
+        pb = self.prepare(device, return_states, config)
+        pb.launch()
+        return pb.result()
+
+
+class PreparedBatch:
+    """A compiled batch resident on the device: tables, matrices, state and output
+    buffers.  ``launch`` zeroes the per-launch counters and starts the persistent kernel
+    on the current stream; ``capture`` records that into a CUDA graph which ``replay``
+    re-launches with one call; ``set_matrices`` rewrites the gate matrices in place
+    (same circuit structure, new angles) between launches."""
+
+    def __init__(self, cb: CircuitBatch, dev: torch.device, return_states: bool, config: BatchConfig):
+        self.n = list(cb._n)
+        self.ncirc = len(self.n)
+        self.device = dev
+        self.config = config
+        self.return_states = return_states
+        circ, ops, passes, items, mats, order, state_amps = cb.compile(return_states, config.tile_bits)
+        self.circ, self.order, self.n_items = circ, order, len(items)
+        self.mat_counts = [len(cb._mats[i]) for i in order]
 
         def up(a):
-            return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).pin_memory().to(dev, non_blocking=True)
+            return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).to(dev)
 
-        d_circ, d_ops, d_pass = up(circ), up(ops if len(ops) else np.zeros(1, OP_T)), up(passes)
-        d_items = up(items)
-        d_mats = up(mats if len(mats) else np.zeros((1, 2, 2), np.complex64))
-        states = torch.empty(max(1, state_amps), dtype=torch.complex64, device=dev)
-        z = torch.zeros(nc, dtype=torch.float64, device=dev)
-        pass_done = torch.zeros(len(passes), dtype=torch.int32, device=dev)
-        t_done = torch.empty(nc + 1, dtype=torch.int64, device=dev)
-        counter = torch.zeros(1, dtype=torch.int32, device=dev)
-        stream = torch.cuda.current_stream(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        _lib._check(_lib.load().tqk_batch_run(d_circ.data_ptr(), nc, d_ops.data_ptr(), d_pass.data_ptr(),
-                                              d_items.data_ptr(), len(items), d_mats.data_ptr(), states.data_ptr(),
-                                              int(return_states), z.data_ptr(), pass_done.data_ptr(),
-                                              t_done.data_ptr(), counter.data_ptr(),
-                                              _lib.status_word(dev).data_ptr(), stream.cuda_stream))
-        e1.record(stream)
-        zh = z.cpu().numpy()
-        th = t_done.cpu().numpy()
-        _lib.check_status(dev)
-        kernel_ms = e0.elapsed_time(e1)
+        self.d_circ, self.d_pass, self.d_items = up(circ), up(passes), up(items)
+        self.d_ops = up(ops if len(ops) else np.zeros(1, OP_T))
+        self.d_mats = up(mats if len(mats) else np.zeros((1, 2, 2), np.complex64))
+        self.d_cfg = config.as_struct()  # host struct, read by the launch call
+        self.states = torch.empty(max(1, state_amps), dtype=torch.complex64, device=dev)
+        self.z = torch.zeros(self.ncirc, dtype=torch.float64, device=dev)
+        self.pass_done = torch.zeros(max(1, len(passes)), dtype=torch.int32, device=dev)
+        self.t_done = torch.zeros(self.ncirc + 1, dtype=torch.int64, device=dev)
+        self.counter = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.status = _lib.status_word(dev)
+        self.graph = None
+        self.kernel_ms = 0.0
+        self._ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+
+    def _enqueue(self, stream) -> None:
+        self.z.zero_()
+        self.pass_done.zero_()
+        self.counter.zero_()
+        _lib._check(_lib.load().tqk_batch_run(
+            self.d_circ.data_ptr(), self.ncirc, self.d_ops.data_ptr(), self.d_pass.data_ptr(),
+            self.d_items.data_ptr(), self.n_items, self.d_mats.data_ptr(), self.states.data_ptr(),
+            int(self.return_states), self.z.data_ptr(), self.pass_done.data_ptr(), self.t_done.data_ptr(),
+            self.counter.data_ptr(), self.status.data_ptr(), self.d_cfg.ctypes.data, stream.cuda_stream))
+
+    def launch(self) -> None:
+        """Zero the counters and launch the persistent kernel (device-timed)."""
+        stream = torch.cuda.current_stream(self.device)
+        self._ev[0].record(stream)
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._enqueue(stream)
+        self._ev[1].record(stream)
+
+    def capture(self) -> "PreparedBatch":
+        """Record the counter resets and the kernel launch into a CUDA graph; later
+        ``launch`` calls replay it.  A first uncaptured launch is made here so that the
+        kernel's one-time device setup happens outside the capture."""
+        if self.graph is not None:
+            return self
+        with torch.cuda.device(self.device):
+            self.launch()
+            torch.cuda.synchronize(self.device)
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(self.device)
+            side.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side):
+                    self._enqueue(side)
+            torch.cuda.current_stream(self.device).wait_stream(side)
+            self.graph = g
+        return self
+
+    def set_matrices(self, mats: np.ndarray) -> None:
+        """New 2x2 matrices for every circuit, in the order the circuits were added
+        (the concatenation of each circuit's matrix list, same counts as before)."""
+        mats = np.asarray(mats, dtype=np.complex64).reshape(-1, 2, 2)
+        if len(mats) != sum(self.mat_counts):
+            raise ValueError(f"expected {sum(self.mat_counts)} matrices, got {len(mats)}")
+        starts = np.concatenate([[0], np.cumsum([self.mat_counts[self.order.index(i)] for i in range(self.ncirc)])])
+        parts = [mats[starts[i]:starts[i + 1]] for i in self.order]
+        flat = np.concatenate(parts) if parts else mats
+        src = torch.from_numpy(np.ascontiguousarray(flat).view(np.uint8).reshape(-1))
+        self.d_mats[:src.numel()].copy_(src.pin_memory(), non_blocking=True)
+
+    def result(self) -> BatchResult:
+        """Wait for the last launch and gather <Z>, latencies and (optionally) states."""
+        zh = self.z.cpu().numpy()
+        th = self.t_done.cpu().numpy()
+        _lib.check_status(self.device)
+        self.kernel_ms = self._ev[0].elapsed_time(self._ev[1])
+        nc = self.ncirc
         out_z = np.empty(nc)
         lat = np.empty(nc)
-        for slot, i in enumerate(order):
+        for slot, i in enumerate(self.order):
             out_z[i] = zh[slot]
             lat[i] = (th[slot] - th[nc]) / 1e6
         out_states = None
-        if return_states:
+        if self.return_states:
             out_states = [None] * nc
-            for slot, i in enumerate(order):
-                off = int(circ[slot]["state_off"])
-                out_states[i] = states[off:off + (1 << self._n[i])].clone()
-        return BatchResult(out_z, lat, kernel_ms, out_states)
+            for slot, i in enumerate(self.order):
+                off = int(self.circ[slot]["state_off"])
+                out_states[i] = self.states[off:off + (1 << self.n[i])].clone()
+        return BatchResult(out_z, lat, self.kernel_ms, out_states)

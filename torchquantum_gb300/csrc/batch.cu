@@ -25,8 +25,8 @@
 namespace tqk {
 namespace batch {
 
-constexpr int kTileBits = TQK_BATCH_TILE_BITS;
-constexpr int kThreads = 512;
+constexpr int kMaxTileBits = TQK_BATCH_TILE_BITS;
+constexpr int kMinTileBits = 10;
 constexpr int kLowReserve = 5;  // address bits 0-4 stay in every tile: warps read 256-byte runs
 constexpr int kFirst = 1, kLast = 2;
 
@@ -45,10 +45,11 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // a * b
 }
 
 // 2x2 matrix m on local bit lb of the tile; if lc >= 0 only where local bit lc is set.
+template <int THREADS>
 __device__ __forceinline__ void apply_1q(float2* amp, int tb, int lb, int lc, const float2* m) {
   const float2 m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
   const int half = 1 << (tb - 1);
-  for (int p = threadIdx.x; p < half; p += blockDim.x) {
+  for (int p = threadIdx.x; p < half; p += THREADS) {
     const int i0 = ((p >> lb) << (lb + 1)) | (p & ((1 << lb) - 1));
     if (lc >= 0 && !((i0 >> lc) & 1)) continue;
     const int i1 = i0 | (1 << lb);
@@ -58,28 +59,29 @@ __device__ __forceinline__ void apply_1q(float2* amp, int tb, int lb, int lc, co
   }
 }
 
+template <int THREADS>
 __device__ void apply_op(const tqk_batch_op& op, float2* amp, int n, int tb, uint32_t tmask, uint32_t base,
                          const Tabs& tabs, const float2* mats) {
   const int tsz = 1 << tb;
   switch (op.kind) {
     case TQK_B_DENSE1: {
       const int b = n - 1 - op.w0;
-      apply_1q(amp, tb, __popc(tmask & ((1u << b) - 1u)), -1, mats + 4 * op.mat);
+      apply_1q<THREADS>(amp, tb, __popc(tmask & ((1u << b) - 1u)), -1, mats + 4 * op.mat);
       break;
     }
     case TQK_B_CTRL1: {
       const int cb = n - 1 - op.w0, b = n - 1 - op.w1;
       const int lb = __popc(tmask & ((1u << b) - 1u));
       if ((tmask >> cb) & 1u) {
-        apply_1q(amp, tb, lb, __popc(tmask & ((1u << cb) - 1u)), mats + 4 * op.mat);
+        apply_1q<THREADS>(amp, tb, lb, __popc(tmask & ((1u << cb) - 1u)), mats + 4 * op.mat);
       } else if ((base >> cb) & 1u) {  // control outside the tile: set for the whole tile
-        apply_1q(amp, tb, lb, -1, mats + 4 * op.mat);
+        apply_1q<THREADS>(amp, tb, lb, -1, mats + 4 * op.mat);
       }
       break;
     }
     case TQK_B_CZ: {
       const int b0 = n - 1 - op.w0, b1 = n - 1 - op.w1;
-      for (int l = threadIdx.x; l < tsz; l += blockDim.x) {
+      for (int l = threadIdx.x; l < tsz; l += THREADS) {
         const uint32_t g = base + dep(tabs, l);
         if ((g >> b0) & (g >> b1) & 1u) amp[l] = make_float2(-amp[l].x, -amp[l].y);
       }
@@ -88,7 +90,7 @@ __device__ void apply_op(const tqk_batch_op& op, float2* amp, int n, int tb, uin
     case TQK_B_CZ_LADDER: {
       uint32_t m = 0;  // bit of wire w+1 for every pair (w, w+1); the pair's other bit is one above
       for (int w = op.w0; w < op.w1; ++w) m |= 1u << (n - 2 - w);
-      for (int l = threadIdx.x; l < tsz; l += blockDim.x) {
+      for (int l = threadIdx.x; l < tsz; l += THREADS) {
         const uint32_t g = base + dep(tabs, l);
         if (__popc(g & (g >> 1) & m) & 1) amp[l] = make_float2(-amp[l].x, -amp[l].y);
       }
@@ -107,14 +109,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
-__global__ void __launch_bounds__(kThreads, 1)
+// THREADS threads per CTA, MINB CTAs per SM for the register budget; the tile holds up
+// to 2^max_tb amplitudes (dynamic shared memory).
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_batch(const tqk_batch_circuit* circ, int ncirc, const tqk_batch_op* ops, const tqk_batch_pass* passes,
             const tqk_batch_item* items, long long n_items, const float2* mats, float2* states, int write_states,
-            double* z_out, int* pass_done, unsigned long long* t_done, int* counter, int* status) {
+            double* z_out, int* pass_done, unsigned long long* t_done, int* counter, int* status, int max_tb) {
   extern __shared__ float2 amp[];
   __shared__ Tabs tabs;
   __shared__ long long s_i;
-  __shared__ double red[kThreads / 32];
+  __shared__ double red[THREADS / 32];
   if (t_done != nullptr && blockIdx.x == 0 && threadIdx.x == 0) t_done[ncirc] = global_ns();
   for (;;) {
     if (threadIdx.x == 0) s_i = atomicAdd(counter, 1);
@@ -128,6 +133,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int n = C.n;
     const uint32_t tmask = P.tile_mask;
     const int tb = __popc(tmask);
+    if (tb > max_tb || tb < 1) {  // a plan made for a larger tile: record and skip the item
+      if (threadIdx.x == 0) {
+        atomicExch(status, TQK_BAD_SHAPE);
+        atomicAdd(pass_done + it.pass, 1);
+      }
+      __syncthreads();
+      continue;
+    }
     const int tsz = 1 << tb;
     const int ntiles = 1 << (n - tb);
     const uint32_t omask = (n >= 32 ? 0xffffffffu : ((1u << n) - 1u)) & ~tmask;
@@ -144,8 +157,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __threadfence();
     }
-    if (threadIdx.x < 256) {  // deposit tables of the tile bits
-      const int part = threadIdx.x >> 7, x = threadIdx.x & 127;
+    for (int t = threadIdx.x; t < 256; t += THREADS) {  // deposit tables of the tile bits
+      const int part = t >> 7, x = t & 127;
       uint32_t v = 0;
       int j = 0;
       for (int b = 0; b < n; ++b) {
@@ -163,21 +176,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     if (P.flags & kFirst) {
-      for (int l = threadIdx.x; l < tsz; l += blockDim.x)
+      for (int l = threadIdx.x; l < tsz; l += THREADS)
         amp[l] = make_float2((base == 0u && l == 0) ? 1.f : 0.f, 0.f);
     } else {
 #pragma unroll 4
-      for (int l = threadIdx.x; l < tsz; l += blockDim.x) amp[l] = __ldcg(st + base + dep(tabs, l));
+      for (int l = threadIdx.x; l < tsz; l += THREADS) amp[l] = __ldcg(st + base + dep(tabs, l));
     }
     __syncthreads();
     for (int oi = 0; oi < P.num_ops; ++oi) {
-      apply_op(ops[P.first_op + oi], amp, n, tb, tmask, base, tabs, mats);
+      apply_op<THREADS>(ops[P.first_op + oi], amp, n, tb, tmask, base, tabs, mats);
       __syncthreads();
     }
     if (P.flags & kLast) {
       const int zbit = n - 1 - C.z_wire;
       double zacc = 0.0;
-      for (int l = threadIdx.x; l < tsz; l += blockDim.x) {
+      for (int l = threadIdx.x; l < tsz; l += THREADS) {
         const float2 a = amp[l];
         const double p2 = static_cast<double>(a.x) * a.x + static_cast<double>(a.y) * a.y;
         zacc += (((base + dep(tabs, l)) >> zbit) & 1u) ? -p2 : p2;
@@ -187,14 +200,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     if (((P.flags & kLast) == 0 || write_states) && C.state_off >= 0) {
 #pragma unroll 4
-      for (int l = threadIdx.x; l < tsz; l += blockDim.x) __stcg(st + base + dep(tabs, l), amp[l]);
+      for (int l = threadIdx.x; l < tsz; l += THREADS) __stcg(st + base + dep(tabs, l), amp[l]);
     }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
       if (P.flags & kLast) {
         double sum = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) sum += red[w];
+        for (int w = 0; w < THREADS / 32; ++w) sum += red[w];
         atomicAdd(z_out + it.circuit, sum);
         __threadfence();
       }
@@ -235,11 +248,14 @@ void op_bits(const tqk_batch_op& op, int n, uint32_t* wires, uint32_t* targets) 
 using namespace tqk;
 
 extern "C" int tqk_batch_plan(tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops_in, int n_mats,
-                              tqk_batch_op* ops_out, tqk_batch_pass* passes, int max_passes) {
+                              tqk_batch_op* ops_out, tqk_batch_pass* passes, int max_passes, int tile_bits) {
   const char* what = "tqk_batch_plan";
   if (ncirc < 0) return -fail(TQK_BAD_SHAPE, "%s: ncirc %d", what, ncirc);
   if (ncirc > 0 && (!circuits || !passes || !ops_out)) return -fail(TQK_BAD_POINTER, "%s: null pointer", what);
-  constexpr int T = batch::kTileBits;
+  if (tile_bits < batch::kMinTileBits || tile_bits > batch::kMaxTileBits)
+    return -fail(TQK_BAD_SHAPE, "%s: tile_bits %d outside %d..%d", what, tile_bits, batch::kMinTileBits,
+                 batch::kMaxTileBits);
+  const int T = tile_bits;
   int np = 0;
   for (int ci = 0; ci < ncirc; ++ci) {
     tqk_batch_circuit& c = circuits[ci];
@@ -324,27 +340,68 @@ extern "C" int64_t tqk_batch_items(const tqk_batch_circuit* circuits, int ncirc,
   return k;
 }
 
+namespace {
+// Kernel variants: (threads per CTA, CTAs per SM the register budget is sized for).
+template <int THREADS, int MINB>
+int launch_batch(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops, const tqk_batch_pass* passes,
+                 const tqk_batch_item* items, int64_t n_items, const void* mats, void* states, int write_states,
+                 double* z_out, int* pass_done, uint64_t* t_done, int* counter, int* status, int tile_bits,
+                 int ctas_per_sm, cudaStream_t stream) {
+  auto kern = batch::k_batch<THREADS, MINB>;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = sizeof(float2) << tile_bits;
+  // attributes are set once per device and variant (before any stream capture: the
+  // first launch of a variant on a device must not be captured)
+  static int attr_set[64] = {0};
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(sizeof(float2) << batch::kMaxTileBits));
+    attr_set[dev] = 1;
+  }
+  int fit = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, THREADS, smem) != cudaSuccess || fit < 1) fit = 1;
+  const int per_sm = ctas_per_sm < fit ? ctas_per_sm : fit;
+  const int64_t slots = static_cast<int64_t>(sms) * per_sm;
+  const int grid = static_cast<int>(n_items < slots ? n_items : slots);
+  kern<<<grid, THREADS, smem, stream>>>(circuits, ncirc, ops, passes, items, n_items,
+                                        static_cast<const float2*>(mats), static_cast<float2*>(states), write_states,
+                                        z_out, pass_done, reinterpret_cast<unsigned long long*>(t_done), counter,
+                                        status, tile_bits);
+  return launch_status("tqk_batch_run");
+}
+}  // namespace
+
 extern "C" int tqk_batch_run(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_op* ops,
                              const tqk_batch_pass* passes, const tqk_batch_item* items, int64_t n_items,
                              const void* mats, void* states, int write_states, double* z_out, int* pass_done,
-                             uint64_t* t_done, int* counter, int* status, void* stream) {
+                             uint64_t* t_done, int* counter, int* status, const tqk_batch_config* config,
+                             void* stream) {
   const char* what = "tqk_batch_run";
   if (ncirc <= 0 || n_items <= 0) return TQK_OK;
   if (!circuits || !passes || !items || !z_out || !pass_done || !counter || !status)
     return fail(TQK_BAD_POINTER, "%s: null pointer", what);
   if (n_items > 0x7fffffff) return fail(TQK_BAD_SHAPE, "%s: too many items", what);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = sizeof(float2) << batch::kTileBits;
-  static int attr_dev = -1;
-  if (attr_dev != dev) {
-    cudaFuncSetAttribute(batch::k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    attr_dev = dev;
+  tqk_batch_config cfg = {TQK_BATCH_TILE_BITS, 512, 1, 0};
+  if (config) cfg = *config;
+  if (cfg.tile_bits < batch::kMinTileBits || cfg.tile_bits > batch::kMaxTileBits)
+    return fail(TQK_BAD_SHAPE, "%s: tile_bits %d outside %d..%d", what, cfg.tile_bits, batch::kMinTileBits,
+                batch::kMaxTileBits);
+  if (cfg.ctas_per_sm < 1 || cfg.ctas_per_sm > 8)
+    return fail(TQK_BAD_SHAPE, "%s: ctas_per_sm %d outside 1..8", what, cfg.ctas_per_sm);
+  cudaStream_t s = as_stream(stream);
+#define TQK_BATCH_ARGS circuits, ncirc, ops, passes, items, n_items, mats, states, write_states, z_out, pass_done, \
+                       t_done, counter, status, cfg.tile_bits, cfg.ctas_per_sm, s
+  switch (cfg.threads) {
+    case 512:
+      return launch_batch<512, 1>(TQK_BATCH_ARGS);
+    case 256:
+      return cfg.ctas_per_sm >= 4 ? launch_batch<256, 4>(TQK_BATCH_ARGS) : launch_batch<256, 2>(TQK_BATCH_ARGS);
+    case 128:
+      return launch_batch<128, 8>(TQK_BATCH_ARGS);
+    default:
+      return fail(TQK_BAD_SHAPE, "%s: threads %d (128, 256 or 512)", what, cfg.threads);
   }
-  const int grid = n_items < sms ? static_cast<int>(n_items) : sms;
-  batch::k_batch<<<grid, batch::kThreads, smem, as_stream(stream)>>>(
-      circuits, ncirc, ops, passes, items, n_items, static_cast<const float2*>(mats), static_cast<float2*>(states),
-      write_states, z_out, pass_done, reinterpret_cast<unsigned long long*>(t_done), counter, status);
-  return launch_status(what);
+#undef TQK_BATCH_ARGS
 }

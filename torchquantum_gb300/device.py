@@ -43,8 +43,9 @@ class QuantumDevice(nn.Module):
         self.record_op = record_op
         self.op_history: List[dict] = []
         self.method = "plain"          # "plain" | "fused" (see fusion.py)
-        self.fuse_wires = 6
+        self.fuse_wires = "auto"       # fused block width 1..6, or "auto" (autotune.choose_fusion)
         self.fused_backend = "auto"    # "auto" | "tc" (tensor cores) | "cuda" (CUDA cores)
+        self.stage_low = True          # plain method: runs of low-qubit gates share one pass (program.stage_runs)
         self._tape: List[engine.TapeOp] = []
         self._pending: List[engine.TapeOp] = []   # fused method: recorded, not yet applied
         self._init: Optional[torch.Tensor] = None

@@ -1,11 +1,14 @@
 """Fused method: group gates into k-wire blocks, build each block's unitary in
 complex128, apply it with one pass over the state.
 
-Planner: greedy and linear in the number of gates per block.  A block starts with
-the first pending gate's wires; walking the pending list in order, a gate joins the
-block if none of its wires is blocked by an earlier gate left out and the union of
-wires stays within ``k``; otherwise its wires become blocked (gates on disjoint wires
-commute, so later gates may still join).  Upstream's static mode instead scores every
+Planner: greedy and linear in the number of gates per block.  A block starts from a
+seed (the first pending gate's wires, or, with lookahead, the best of a few front
+gates and pairs of them); walking the pending list in order, a gate joins the block if
+none of its wires is blocked by an earlier gate left out and the union of wires stays
+within ``k``; otherwise its wires become blocked (gates on disjoint wires commute, so
+later gates may still join).  ``plan_beam`` keeps the few best partial plans per block
+instead of one.  The fusion width and planner variant are picked per segment by
+``autotune.choose_fusion`` from measured per-pass costs.  Upstream's static mode instead scores every
 ``C(n, k)`` wire combination per block (``torchquantum/graph/graphs.py:384-532``),
 which is impractical at n = 24..28.
 
@@ -28,8 +31,35 @@ from . import engine
 __all__ = ["plan_blocks", "op_full_matrix", "build_block_unitary", "use_tensor_cores"]
 
 
-def plan_blocks(wire_lists: Sequence[Sequence[int]], k: int) -> List[Tuple[List[int], List[int]]]:
-    """Greedy fusion plan: list of (sorted block wires, gate indices in order)."""
+def _grow(wire_lists, pending, seed, k):
+    """One block from ``seed`` wires: walk ``pending`` in order, take every gate whose
+    wires are unblocked and keep the union within ``k``; a gate left out blocks its
+    wires for the gates after it.  Returns (block wires, taken, rest)."""
+    q = set(seed)
+    blocked = set()
+    take, rest = [], []
+    for gi in pending:
+        w = set(wire_lists[gi])
+        if w & blocked:
+            blocked |= w
+            rest.append(gi)
+            continue
+        if len(q | w) <= k:
+            q |= w
+            take.append(gi)
+        else:
+            blocked |= w
+            rest.append(gi)
+    return q, take, rest
+
+
+def plan_blocks(wire_lists: Sequence[Sequence[int]], k: int, lookahead: int = 0) -> List[Tuple[List[int], List[int]]]:
+    """Greedy fusion plan: list of (sorted block wires, gate indices in order).
+
+    ``lookahead = 0``: each block is seeded with the first pending gate's wires.
+    ``lookahead = m``: the first m gates of the front (pending gates no earlier pending
+    gate shares a wire with) are tried as seeds, alone and in pairs that fit, and the
+    seed whose block takes the most gates wins.  Cost: O(m^2 x pending) per block."""
     pending = list(range(len(wire_lists)))
     blocks = []
     while pending:
@@ -38,26 +68,95 @@ def plan_blocks(wire_lists: Sequence[Sequence[int]], k: int) -> List[Tuple[List[
             blocks.append((sorted(first), [pending[0]]))
             pending = pending[1:]
             continue
-        q = set(first)
-        blocked = set()
-        take, rest = [], []
-        for gi in pending:
-            w = set(wire_lists[gi])
-            if w & blocked:
-                blocked |= w
-                rest.append(gi)
-                continue
-            if len(q | w) <= k:
-                q |= w
-                take.append(gi)
-            else:
-                blocked |= w
-                rest.append(gi)
-            if len(blocked) >= 64 and not rest:
-                break
+        if lookahead <= 0:
+            q, take, rest = _grow(wire_lists, pending, first, k)
+        else:
+            front, seen = [], set()
+            for gi in pending:
+                w = set(wire_lists[gi])
+                if not (w & seen) and len(w) <= k:
+                    front.append(w)
+                seen |= w
+                if len(front) >= lookahead or len(seen) >= 64:
+                    break
+            seeds = list(front) + [a | b for i, a in enumerate(front) for b in front[i + 1:] if len(a | b) <= k]
+            best = None
+            for sd in seeds:
+                cand = _grow(wire_lists, pending, sd, k)
+                if best is None or len(cand[1]) > len(best[1]):
+                    best = cand
+            q, take, rest = best
         blocks.append((sorted(q), take))
         pending = rest
     return blocks
+
+
+def _front_seeds(wire_lists, pending, k, m):
+    front, seen = [], set()
+    for gi in pending:
+        w = set(wire_lists[gi])
+        if not (w & seen) and len(w) <= k:
+            front.append(w)
+        seen |= w
+        if len(front) >= m or len(seen) >= 64:
+            break
+    return front + [a | b for i, a in enumerate(front) for b in front[i + 1:] if len(a | b) <= k]
+
+
+def plan_beam(wire_lists: Sequence[Sequence[int]], k: int, width: int = 4, lookahead: int = 8):
+    """Beam search over block sequences: each step extends every kept partial plan by one
+    block per seed (front gates and pairs, as in ``plan_blocks``) and keeps the ``width``
+    partial plans with the fewest gates left.  Same legality rules as ``plan_blocks``."""
+    states = [([], tuple(range(len(wire_lists))))]
+    while True:
+        done = [st for st in states if not st[1]]
+        if done:
+            return min(done, key=lambda st: len(st[0]))[0]
+        cand = []
+        for blocks, pend in states:
+            pl = list(pend)
+            first = set(wire_lists[pl[0]])
+            if len(first) > k:  # a gate wider than the block size stays on its own
+                cand.append((blocks + [(sorted(first), [pl[0]])], tuple(pl[1:])))
+                continue
+            seen = set()
+            for sd in _front_seeds(wire_lists, pl, k, lookahead):
+                q, take, rest = _grow(wire_lists, pl, sd, k)
+                key = tuple(rest)
+                if key in seen:
+                    continue
+                seen.add(key)
+                cand.append((blocks + [(sorted(q), take)], key))
+        cand.sort(key=lambda st: (len(st[1]), len(st[0])))
+        states, keys = [], set()
+        for st in cand:
+            if st[1] in keys:
+                continue
+            keys.add(st[1])
+            states.append(st)
+            if len(states) >= width:
+                break
+
+
+BEAM_MAX_GATES = 2000  # longer segments plan with the single-pass lookahead only
+_PLAN_CACHE: dict = {}
+
+
+def plan_cached(wire_lists: Sequence[Sequence[int]], k: int, lookahead: int = 0, beam: int = 0):
+    """Fusion plan memoised on the wire lists (a circuit re-recorded every step plans
+    once): ``beam > 1`` runs ``plan_beam`` (segments up to ``BEAM_MAX_GATES`` gates),
+    otherwise ``plan_blocks``."""
+    key = (tuple(tuple(w) for w in wire_lists), k, lookahead, beam)
+    hit = _PLAN_CACHE.get(key)
+    if hit is None:
+        if len(_PLAN_CACHE) > 256:
+            _PLAN_CACHE.clear()
+        if beam > 1 and len(wire_lists) <= BEAM_MAX_GATES:
+            hit = plan_beam(wire_lists, k, beam, max(lookahead, 1))
+        else:
+            hit = plan_blocks(wire_lists, k, lookahead)
+        _PLAN_CACHE[key] = hit
+    return hit
 
 
 def op_full_matrix(op: engine.TapeOp, dtype=torch.complex128, device=None) -> torch.Tensor:

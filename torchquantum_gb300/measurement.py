@@ -10,11 +10,21 @@ are float64 with a fixed order.  The backward of an expval is ``2 g P psi``
 observables' diagonalizing gates are applied to the device in place, then each wire's
 eigenvalue-weighted marginal is read -- here as a Z-string expectation value,
 ``e0 P(0) + e1 P(1) = (e0+e1)/2 + (e0-e1)/2 <Z>``.
+
+``MeasureMultipleTimes`` / ``MeasureMultiPauliSum`` / ``MeasureMultiQubitPauliSum``
+(measurements.py:346-456) measure a copy of the state per layer of per-wire
+observables; Pauli layers become single-site strings evaluated in one fused pass.
+
+``measure`` (measurements.py:37-74) samples bitstrings on the GPU (``tqk_sample``:
+inverse-CDF draws against device-side prefix sums) instead of copying |psi|^2 to the
+host for ``random.choices``.
 """
 from __future__ import annotations
 
-from typing import List, Sequence, Union
+from collections import OrderedDict
+from typing import List, Optional, Sequence, Union
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -22,7 +32,8 @@ from .engine import kernel_operand
 from .module import QuantumModule
 
 __all__ = ["expval_joint_analytical", "expval_joint_analytical_batch", "expval", "MeasureAll", "probs",
-           "pauli_masks"]
+           "pauli_masks", "measure", "gen_bitstrings", "MeasureMultipleTimes", "MeasureMultiPauliSum",
+           "MeasureMultiQubitPauliSum"]
 
 
 def pauli_masks(observable: str, n: int):
@@ -122,3 +133,124 @@ def probs(qdev) -> torch.Tensor:
     """|psi|^2 as [bsz, 2^n] float32 (no autograd; use ``get_states_1d().abs()**2`` for gradients)."""
     st = kernel_operand(_state_2d(qdev))
     return _lib.probs(st, qdev.n_wires)
+
+
+# ------------------------------------------------------------------ sampling
+def gen_bitstrings(n_wires: int) -> List[str]:
+    """All n-bit strings, qubit 0 first (measurements.py:33-34)."""
+    return ["{:0{}b}".format(k, n_wires) for k in range(2 ** n_wires)]
+
+
+FULL_DICT_MAX_WIRES = 20
+
+
+def measure(qdev, n_shots: int = 1024, draw_id: Optional[int] = None, generator: Optional[torch.Generator] = None):
+    """Sample ``n_shots`` bitstrings per batch row (measurements.py:37-74): a list of
+    OrderedDicts bitstring -> count, sorted by bitstring, qubit 0 first.  Up to
+    ``FULL_DICT_MAX_WIRES`` wires every bitstring is a key (zero counts included, as
+    upstream); above that only observed bitstrings are (upstream would build 2^n keys).
+    ``generator``: a CUDA torch.Generator for reproducible draws.  ``draw_id`` plots
+    that row's histogram when matplotlib is installed."""
+    n = qdev.n_wires
+    st = kernel_operand(_state_2d(qdev))
+    bsz = st.shape[0]
+    u = torch.rand(bsz, int(n_shots), dtype=torch.float64, device=st.device, generator=generator)
+    idx = _lib.sample(st, n, u)
+    out = []
+    if n <= FULL_DICT_MAX_WIRES:
+        flat = idx + (torch.arange(bsz, device=idx.device, dtype=torch.int64) << n)[:, None]
+        counts = torch.bincount(flat.reshape(-1), minlength=bsz << n).view(bsz, 1 << n).cpu().numpy()
+        keys = gen_bitstrings(n)
+        for b in range(bsz):
+            out.append(OrderedDict(zip(keys, counts[b].tolist())))
+    else:
+        for b in range(bsz):
+            vals, cnt = torch.unique(idx[b], return_counts=True)
+            out.append(OrderedDict(("{:0{}b}".format(int(v), n), int(c)) for v, c in
+                                   zip(vals.cpu().tolist(), cnt.cpu().tolist())))
+    if draw_id is not None:
+        try:
+            import matplotlib.pyplot as plt
+        except ImportError:
+            plt = None
+        if plt is not None:
+            plt.bar(out[draw_id].keys(), out[draw_id].values())
+            plt.xticks(rotation="vertical")
+            plt.xlabel("bitstring [qubit0, qubit1, ..., qubitN]")
+            plt.title("distribution of measured bitstrings")
+            plt.show()
+    return out
+
+
+# ------------------------------------------------------------------ multi-observable layers
+_PAULI_CHAR = {"x": "X", "paulix": "X", "y": "Y", "pauliy": "Y", "z": "Z", "pauliz": "Z", "i": "I"}
+
+
+class MeasureMultipleTimes(QuantumModule):
+    """Per layer ``{'wires': [...], 'observables': [...]}``: each wire's expectation value
+    of its observable (identity on unlisted wires) on a copy of the state; layers
+    concatenated along the batch dimension, [layers * bsz, n_wires]
+    (measurements.py:346-400)."""
+
+    def __init__(self, obs_list, v_c_reg_mapping=None):
+        super().__init__()
+        self.obs_list = obs_list
+        self.v_c_reg_mapping = v_c_reg_mapping
+
+    def forward(self, qdev):
+        from .device import QuantumDevice
+        from .operators import op_name_dict
+
+        n = qdev.n_wires
+        res_all = []
+        for layer in self.obs_list:
+            names = ["i"] * n
+            for wire, ob in zip(layer["wires"], layer["observables"]):
+                names[wire] = ob.lower()
+            if all(nm in _PAULI_CHAR for nm in names):
+                # single-site Pauli strings, one fused pass per distinct X pattern
+                strings = ["".join(_PAULI_CHAR[nm] if w == j else "I" for j in range(n)) for w, nm in enumerate(names)]
+                res = expval_joint_analytical_batch(qdev, strings)
+            else:
+                qnew = QuantumDevice(n_wires=n, bsz=qdev.bsz, device=qdev.device)
+                qnew.set_states(qdev.get_states_1d())
+                res = expval(qnew, list(range(n)), [op_name_dict[nm]() for nm in names])
+            if self.v_c_reg_mapping is not None:
+                c2v = self.v_c_reg_mapping["c2v"]
+                perm = [c2v[k] for k in range(res.shape[-1]) if k in c2v.keys()]
+                res = res[:, perm]
+            res_all.append(res)
+        return torch.cat(res_all)
+
+    def set_v_c_reg_mapping(self, mapping):
+        self.v_c_reg_mapping = mapping
+
+
+class MeasureMultiPauliSum(QuantumModule):
+    """Sum over wires of ``MeasureMultipleTimes`` (measurements.py:403-432; upstream does
+    not apply the coefficients here, and neither does this)."""
+
+    def __init__(self, obs_list, v_c_reg_mapping=None):
+        super().__init__()
+        self.obs_list = obs_list
+        self.v_c_reg_mapping = v_c_reg_mapping
+        self.measure_multiple_times = MeasureMultipleTimes(obs_list=obs_list, v_c_reg_mapping=v_c_reg_mapping)
+
+    def forward(self, qdev):
+        return self.measure_multiple_times(qdev).sum(-1)
+
+
+class MeasureMultiQubitPauliSum(QuantumModule):
+    """``obs_list[0]['coefficient']`` times ``MeasureMultipleTimes(obs_list[1:])``, summed
+    over the last dimension (measurements.py:435-456)."""
+
+    def __init__(self, obs_list, v_c_reg_mapping=None):
+        super().__init__()
+        self.obs_list = obs_list
+        self.v_c_reg_mapping = v_c_reg_mapping
+        self.measure_multiple_times = MeasureMultipleTimes(obs_list=obs_list[1:], v_c_reg_mapping=v_c_reg_mapping)
+
+    def forward(self, qdev):
+        res_all = self.measure_multiple_times(qdev)
+        coef = torch.as_tensor(self.obs_list[0]["coefficient"], dtype=res_all.dtype, device=res_all.device)
+        return (res_all * coef).sum(-1)

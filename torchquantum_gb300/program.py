@@ -7,9 +7,11 @@ the state is read:
   on the GPU by one ``tqk_gate_operands`` launch for the whole segment, reading its
   parameters in place through their strides (no per-gate torch ops);
 * the plain method then applies each op with its kernel; the fused method plans
-  blocks of up to 6 wires (``fusion.plan_blocks``), builds every block unitary in
-  float64 with one ``tqk_block_build`` launch, and applies each block with the
-  tensor-core kernel (or the CUDA-core dense kernel on small states);
+  blocks of up to 6 wires (``fusion.plan_blocks``; width, planner variant and kernel
+  per block chosen by ``autotune.choose_fusion`` from measured pass costs when
+  ``fuse_wires == "auto"``), builds every block unitary in float64 with one
+  ``tqk_block_build`` launch, and applies each block with the tensor-core kernel or
+  the CUDA-core dense kernel;
 * the backward walks the segment in reverse with the adjoint kernels, turns block
   cotangents into gate-operand cotangents with ``tqk_block_unbuild``, and gate-operand
   cotangents into parameter gradients with ``tqk_param_grads`` (analytic
@@ -176,20 +178,34 @@ class Segment:
         # ---- plan
         self.blocks = []
         if method == "fused":
-            k = max(1, min(qdev.fuse_wires, n, 6))
             wl = [op.wires if fusable(op) else list(range(n)) for op in ops]
-            plan = fusion.plan_blocks(wl, k)
+            fw = qdev.fuse_wires
+            backend = getattr(qdev, "fused_backend", "auto")
+            tc_ok = backend != "cuda" and n >= fusion.TC_MIN_WIRES
+            if fw == "auto" and self.device.type == "cuda":
+                from . import autotune
+
+                with_adj = any(isinstance(r, NativeGate) and r.params.requires_grad for r in records) or \
+                    any(not isinstance(r, NativeGate) and r.needs_grad for r in records)
+                plan, tc_flags, k, _ = autotune.choose_fusion(wl, n, self.bsz, dev, tc_ok, with_adj)
+                if backend == "tc":
+                    tc_flags = [tc_ok for _ in plan]
+            else:
+                k = max(1, min(6 if fw == "auto" else int(fw), n, 6))
+                plan = fusion.plan_cached(wl, k, 8, 4)
+                tc_flags = [fusion.use_tensor_cores(qdev, len(bw)) for bw, _ in plan]
+            self.fuse_width = k
             exec_ops = []
-            for bwires, idxs in plan:
+            for (bwires, idxs), tc in zip(plan, tc_flags):
                 members = [ops[i] for i in idxs]
                 if len(members) == 1:  # a lone gate is cheapest on its own kernel
                     exec_ops.append(members[0])
                     continue
-                exec_ops.append(self._make_block(qdev, members, bwires))
+                exec_ops.append(self._make_block(qdev, members, bwires, tc))
             self.exec_ops = exec_ops
             self._build_blocks()
         else:
-            self.exec_ops = ops
+            self.exec_ops = stage_runs(ops, n) if getattr(qdev, "stage_low", True) else ops
         # ---- differentiable inputs
         self.bases: Dict[int, tuple] = {}
         for g in natives:
@@ -200,10 +216,9 @@ class Segment:
         self.diff_inputs = [b for b, _ in self.bases.values()] + [op.source for op in self.generic_sources]
 
     # -------------------------------------------------------------- blocks
-    def _make_block(self, qdev, members, bwires):
+    def _make_block(self, qdev, members, bwires, tc):
         from . import fusion
 
-        tc = fusion.use_tensor_cores(qdev, len(bwires))
         if tc:
             bwires = fusion._pad_wires(bwires, self.n)
         k = len(bwires)
@@ -278,7 +293,9 @@ class Segment:
     # -------------------------------------------------------------- forward
     def apply(self, buf: torch.Tensor) -> None:
         for op in self.exec_ops:
-            if getattr(op, "members", None) is not None:
+            if isinstance(op, StagedRun):
+                _lib.staged_apply(buf, self.n, op.descs(), op.tile_bits)
+            elif getattr(op, "members", None) is not None:
                 if op.tc:
                     _lib.fused_apply(buf, self.n, op.wires, op.image, op.block_batch)
                 else:
@@ -297,6 +314,18 @@ class Segment:
             gslots[id(op)] = torch.zeros(op.operand.shape, dtype=torch.complex128, device=dev)
         gu = torch.zeros_like(self.u128) if (need_grads and self.blocks) else None
         for op in reversed(self.exec_ops):
+            if isinstance(op, StagedRun):
+                slots = []
+                for m in op.ops:
+                    slot = None
+                    if need_grads:
+                        if hasattr(m, "native") and m.native.params.requires_grad:
+                            slot = _as_real(opg, m.op128, self.op128)
+                        elif id(m) in gslots:
+                            slot = torch.view_as_real(gslots[id(m)]).view(-1)
+                    slots.append(slot)
+                _lib.staged_adjoint(psi, lam, n, op.descs(slots), op.tile_bits)
+                continue
             if getattr(op, "members", None) is not None:
                 slot = None
                 if gu is not None and _block_needs_grad(op):
@@ -366,6 +395,94 @@ class Segment:
         for op in self.generic_sources:
             grads.append(gslots[id(op)].to(op.source.dtype).view(op.source.shape))
         return grads
+
+
+# ---------------------------------------------------------------- staged low-qubit runs
+class StagedRun:
+    """Consecutive ops whose targets lie in the lowest ``tile_bits`` index bits, applied
+    in one shared-memory pass (``tqk_staged_apply``) and reversed in one adjoint pass."""
+
+    def __init__(self, ops, tile_bits):
+        self.ops = ops
+        self.tile_bits = tile_bits
+        self.wires = sorted({w for o in ops for w in o.wires})
+
+    def descs(self, grads=None):
+        out = []
+        for i, o in enumerate(self.ops):
+            d = _lib.StagedOp()
+            if o.kind == engine.KIND_X:
+                ws, d.kind, d.ctrl_val = o.controls + o.targets, _lib.S_X, o.ctrl_val
+            elif o.kind in (engine.KIND_DENSE, engine.KIND_CTRL):
+                ws, d.kind = (o.controls + o.targets) if o.kind == engine.KIND_CTRL else o.wires, _lib.S_DENSE1
+            elif o.kind == engine.KIND_PHASE:
+                ws, d.kind = o.wires, _lib.S_PHASE
+            else:
+                ws, d.kind = o.wires, _lib.S_DIAG
+            d.nwires = len(ws)
+            for j, w in enumerate(ws):
+                d.wires[j] = w
+            if o.kind != engine.KIND_X:
+                d.operand = o.operand.data_ptr()
+                d.batch = int(o.operand.shape[0])
+            else:
+                d.batch = 1
+            g = grads[i] if grads is not None else None
+            d.grad = g.data_ptr() if g is not None else None
+            out.append(d)
+        return out
+
+
+def stageable(op, n: int, tile_bits: int) -> bool:
+    """Ops ``tqk_staged_apply`` can run: one target inside the low tile (dense, controlled,
+    controlled-X), or diagonal ops anywhere (phase on any wires, diagonal on <= 2)."""
+    if getattr(op, "uncompute", None) is not None or getattr(op, "image", None) is not None:
+        return False
+    if not op.wires or len(op.wires) > _lib.STAGED_MAX_WIRES:
+        return False
+    low = n - tile_bits  # wires >= low have their bit inside the tile
+    k = op.kind
+    if k == engine.KIND_DENSE:
+        return len(op.wires) == 1 and op.wires[0] >= low and _mat2(op)
+    if k == engine.KIND_CTRL:
+        return len(op.targets) == 1 and op.targets[0] >= low and _mat2(op)
+    if k == engine.KIND_X:
+        return len(op.targets) == 1 and op.targets[0] >= low
+    if k == engine.KIND_PHASE:
+        return op.operand is not None and op.operand.numel() == int(op.operand.shape[0])
+    if k == engine.KIND_DIAG:
+        return len(op.wires) <= 2 and op.operand is not None and op.operand.shape[-1] == (1 << len(op.wires))
+    return False
+
+
+def _mat2(op) -> bool:
+    t = op.operand
+    return t is not None and t.dtype == torch.complex64 and tuple(t.shape[1:]) == (2, 2) and t.is_contiguous()
+
+
+def stage_runs(ops, n: int, min_run: int = 2):
+    """Group maximal runs of consecutive stageable ops into ``StagedRun`` passes (tile of
+    2^min(n, 12) amplitudes; at most ``STAGED_MAX_OPS`` ops per pass)."""
+    tb = min(n, _lib.STAGED_MAX_TILE_BITS)
+    out, run = [], []
+
+    def close():
+        if len(run) >= min_run:
+            out.append(StagedRun(list(run), tb))
+        else:
+            out.extend(run)
+        run.clear()
+
+    for op in ops:
+        if stageable(op, n, tb):
+            run.append(op)
+            if len(run) == _lib.STAGED_MAX_OPS:
+                close()
+        else:
+            close()
+            out.append(op)
+    close()
+    return out
 
 
 def _operand_shape(r: NativeGate, sz: int):
