@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the baseline sample")
     ap.add_argument("--fuse", default="auto", help="fused block width 1..6 or auto (autotuner)")
+    ap.add_argument("--kernels", action="store_true",
+                    help="only time the hot kernels alone at --n/--bsz (roofline table; for profiling)")
     ap.add_argument("--quick", action="store_true", help="skip e2e/roofline/baseline (profiling runs)")
     ap.add_argument("--workload", default="random", choices=["random", "c1", "c3", "c4", "c5"],
                     help="random: the headline circuit (default); c1: small encoder+U3+CNOT model (n=4, bsz=32); "
@@ -82,17 +84,23 @@ def cpu_sample(args, seconds: float):
     theta = W.random_params(1, ncols, seed=1)
     og = W.oracle_gates(gates, theta)
 
+    cpu = {}
+
     def run(g):
-        t0 = time.perf_counter()
+        t0, c0 = time.perf_counter(), time.process_time()
         s, saved, mats = O.forward_saving(args.n, 1, og[:g], np.complex64)
         O.backward_sweep(args.n, og[:g], saved, mats, s.copy())
-        return time.perf_counter() - t0
+        wall = time.perf_counter() - t0
+        cpu["cores"] = (time.process_time() - c0) / max(wall, 1e-9)
+        return wall
 
     t1 = run(2) / 2
     g = int(max(2, min(args.depth, seconds / max(t1, 1e-6))))
     t = run(g)
     per_circuit = t / g * args.depth
-    threads = os.cpu_count() or 1
+    # cores actually used: process CPU time / wall time of the sample (numpy runs the
+    # permute copies on one thread; BLAS may thread the matmuls)
+    threads = round(cpu["cores"], 2)
     desc = (f"oracle (numpy complex64) fwd keeping per-gate states + reverse sweep, n={args.n}, 1 circuit, "
             f"first {g} of {args.depth} gates in {t:.1f} s, extrapolated to the full depth")
     return 1.0 / per_circuit, desc, threads, g, t
@@ -114,7 +122,9 @@ def run_reference(args):
         s, saved, mats = O.forward_saving(args.n, 1, og[:g], np.complex64)
         O.backward_sweep(args.n, og[:g], saved, mats, s.copy())
 
-    t0 = time.perf_counter()
+    c_start = time.process_time()
+
+    t0 = t_run0 = time.perf_counter()
     one(1)
     t1 = time.perf_counter() - t0
     # each step is a bounded sample sized so steps+warmup fit in ~3 minutes
@@ -129,7 +139,8 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
     per_step = sum(times) / len(times)
     value = 1.0 / (per_step / g * args.depth)
-    threads = os.cpu_count() or 1
+    # cores actually used: process CPU time over the whole run / its wall time
+    threads = round((time.process_time() - c_start) / max(time.perf_counter() - t_run0, 1e-9), 2)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -687,6 +698,12 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.kernels:
+        import torch
+
+        dev = torch.device("cuda")
+        roof, res = roofline(args, dev)
+        print(json.dumps({"kernels": res, "n_wires": args.n, "bsz": args.bsz}), flush=True)
     elif args.workload == "c1":
         run_c1(args)
     elif args.workload == "c3":

@@ -276,6 +276,32 @@ def run(n: int, bsz: int, gates: List[Dict], state: Optional[np.ndarray] = None)
     return s
 
 
+# ----------------------------------------------------------------------- density matrices
+def density_run(n: int, bsz: int, gates: List[Dict], rho: Optional[np.ndarray] = None,
+                upstream_bmm: bool = False) -> np.ndarray:
+    """rho [bsz, 2^n, 2^n] evolved by a gate list from |0..0><0..0| (or ``rho``).
+
+    Default: rho -> U rho U^H.  ``upstream_bmm``: upstream's density bmm
+    (``functional/gate_wrapper.py:265-321``), which multiplies the bra wires by conj(U)
+    without transposing -- rho -> U rho conj(U) in the same index convention -- equal to
+    U rho U^H only for symmetric U."""
+    d = 1 << n
+    if rho is None:
+        rho = np.zeros((bsz, d, d), C)
+        rho[:, 0, 0] = 1
+    v = np.array(rho, C).reshape(bsz, d * d)  # vec(rho): ket wires 0..n-1, bra wires n..2n-1
+    for g in gates:
+        wires = [g["wires"]] if isinstance(g["wires"], int) else list(g["wires"])
+        m = np.asarray(gate_matrix(g["name"], g.get("params"), g.get("n_wires") or len(wires),
+                                   g.get("inverse", False)), C)
+        m3 = m if m.ndim == 3 else m[None]
+        v = apply(v, m3, wires, 2 * n)
+        # bra side: rho U^H acts on the bra index as conj(U); upstream applies conj(U)^T
+        right = np.conj(m3) if not upstream_bmm else np.conj(np.swapaxes(m3, -1, -2))
+        v = apply(v, right, [w + n for w in wires], 2 * n)
+    return v.reshape(bsz, d, d)
+
+
 def pauli_masks(pauli: str, n: int):
     """(xmask, zmask, number of Y) with P[0] on wire 0 = bit n-1."""
     x = z = ny = 0

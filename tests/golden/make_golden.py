@@ -22,6 +22,8 @@ Outputs (all small ``.npz`` files, committed):
   ladder with shared parameters, optional per-sample RY input layer, weighted sum of
   Pauli-string expvals): expvals and autograd gradients for the shared angles and the
   inputs, complex64 and complex128.
+* ``density.npz`` -- upstream's density-matrix device on circuits of symmetric gates,
+  plus one circuit with RY that records upstream's rho conj(U) defect.
 * ``known_answers.npz`` -- the upstream known-answer tests (``test/device/test_init.py:32``,
   ``test/functional/test_controlled_unitary.py:30``, ``test/functional/test_func_mat_exp.py:30``,
   ``test/operator/test_ControlledU.py:40``, ``test/operator/test_op_hamil_exp.py:32``) and the
@@ -263,6 +265,43 @@ def make_config1(rng):
     print("config1: done")
 
 
+def make_density(rng):
+    """Upstream's density-matrix device (device/noisedevices.py:36-105, gate_wrapper.py
+    bmm branch :434-440 -> apply_unitary_density_bmm :265-321), complex128 mode: circuits of
+    symmetric gates (where upstream's rho conj(U) equals rho U^H), and one circuit with a
+    non-symmetric gate (RY) recording upstream's output as a documented defect.  Gate
+    parameters have one row (upstream's density bmm fails on per-row matrices)."""
+    import contextlib
+    import io
+
+    out, index = {}, []
+    sym = [("rx", 1, 1), ("rz", 1, 1), ("hadamard", 0, 1), ("sx", 0, 1), ("s", 0, 1), ("t", 0, 1),
+           ("cnot", 0, 2), ("cz", 0, 2), ("crx", 1, 2), ("swap", 0, 2), ("rxx", 1, 2), ("rzz", 1, 2)]
+    cases = [(3, 2, 25, sym), (4, 1, 30, sym), (3, 1, 6, [("ry", 1, 1), ("hadamard", 0, 1)])]
+    refimport.set_reference_precision(True)
+    for ci, (n, bsz, depth, pool) in enumerate(cases):
+        gates = []
+        for _ in range(depth):
+            name, npar, k = pool[rng.integers(len(pool))]
+            wires = [int(w) for w in rng.permutation(n)[:k]]
+            # one parameter row: upstream's density bmm reshapes with matdag.shape[0], which is
+            # the batch size for a per-row matrix (gate_wrapper.py:308), and fails
+            p = rng.uniform(-np.pi, np.pi, size=(1, npar)).tolist() if npar else None
+            gates.append({"name": name, "wires": wires, "params": p})
+        q = tq.NoiseDevice(n_wires=n, bsz=bsz)
+        q.densities = q.densities.to(torch.complex128)
+        with contextlib.redirect_stdout(io.StringIO()):  # upstream prints the density shape per gate
+            for g in gates:
+                p = None if g["params"] is None else torch.tensor(g["params"], dtype=torch.float64)
+                tqf.func_name_dict[g["name"]](q, wires=g["wires"], params=p)
+        out[f"d{ci}__rho"] = q.densities.reshape(bsz, 1 << n, 1 << n).detach().numpy()
+        index.append({"key": f"d{ci}", "n": n, "bsz": bsz, "gates": gates, "symmetric": pool is sym})
+    refimport.set_reference_precision(False)
+    out["__meta__"] = np.array(json.dumps(index))
+    np.savez_compressed(os.path.join(HERE, "density.npz"), **out)
+    print(f"density: {len(index)} cases")
+
+
 def make_hea(rng):
     """Differentiation workload at reduced size: optional per-sample RY(x) input layer,
     then L layers of (RY on every wire, RZ on every wire, CZ ladder (i, i+1)) with one
@@ -411,3 +450,4 @@ if __name__ == "__main__":
     make_config1(np.random.default_rng(3))
     make_known_answers()
     make_hea(np.random.default_rng(4))
+    make_density(np.random.default_rng(5))

@@ -171,3 +171,24 @@ def test_plan_rejects_invalid():
             cb.compile(tile_bits=bad)
     with pytest.raises(ValueError, match="not supported"):
         B.CircuitBatch().add_gates(3, [{"name": "swap", "wires": [0, 1], "params": None}])
+
+
+def test_op_history_ingestion():
+    """A device's op_history (scalar wires for one-qubit gates, scalar or list params,
+    inverse flags) compiles to a batch circuit with the oracle's state."""
+    n = 4
+    hist = [{"name": "u3", "wires": 2, "params": [0.3, -0.7, 1.1], "inverse": False, "trainable": True},
+            {"name": "rx", "wires": 0, "params": 0.4, "inverse": True, "trainable": False},
+            {"name": "crx", "wires": [0, 3], "params": 1.3, "inverse": True, "trainable": True},
+            {"name": "cnot", "wires": [3, 1], "params": None, "inverse": False, "trainable": False},
+            {"name": "sx", "wires": 1, "params": None, "inverse": True, "trainable": False},
+            {"name": "cz", "wires": [1, 2], "params": None, "inverse": False, "trainable": False}]
+    cb = B.CircuitBatch()
+    cb.add_gates(n, hist)
+    got = _simulate_ir(n, cb._ops[0], cb._mats[0].astype(np.complex128))
+    og = [{"name": h["name"], "wires": list(np.atleast_1d(h["wires"])), "inverse": h["inverse"],
+           "params": None if h["params"] is None else np.atleast_1d(np.asarray(h["params"], np.float64))[None]}
+          for h in hist]
+    np.testing.assert_allclose(got, O.run(n, 1, og)[0], atol=1e-6)
+    with pytest.raises(ValueError, match="one parameter row"):
+        B.CircuitBatch().add_gates(2, [{"name": "rx", "wires": 0, "params": [[0.1], [0.2]]}])

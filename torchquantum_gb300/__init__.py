@@ -21,6 +21,7 @@ from .measurement import expval_joint_analytical, expval_joint_analytical_batch,
 from .measurement import measure, gen_bitstrings, MeasureMultipleTimes, MeasureMultiPauliSum, \
     MeasureMultiQubitPauliSum  # noqa: F401
 from . import measurement  # noqa: F401
+from .density import NoiseDevice  # noqa: F401
 
 _bind_gate_methods()
 

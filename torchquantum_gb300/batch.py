@@ -96,10 +96,12 @@ class CircuitBatch:
         return len(self._n) - 1
 
     def add_gates(self, n: int, gates: Sequence[Dict], z_wire: int = 0) -> int:
-        """A circuit as a gate list ``{name, wires, params}`` (params: P reals or None).
-        Consecutive one-qubit gates on a wire are fused into one 2x2 matrix; controlled
-        one-qubit gates, CNOT and controlled phases use their lower-right 2x2 block; CZ
-        becomes a diagonal op."""
+        """A circuit as a gate list ``{name, wires, params[, inverse]}`` (params: P reals,
+        a scalar or None; wires: a list or one int) -- the format of a device's
+        ``op_history`` (upstream functional/gate_wrapper.py:380-391), so a recorded
+        circuit can be replayed in a batch.  Consecutive one-qubit gates on a wire are
+        fused into one 2x2 matrix; controlled one-qubit gates, CNOT and controlled
+        phases use their lower-right 2x2 block; CZ becomes a diagonal op."""
         pending: Dict[int, np.ndarray] = {}
         ops, mats = [], []
 
@@ -117,11 +119,15 @@ class CircuitBatch:
 
         for g in gates:
             name = G.canonical_name(g["name"])
-            wires = [int(w) for w in g["wires"]]
+            wires = [int(w) for w in np.atleast_1d(g["wires"])]
             gd = G.GATES[name]
             p = g.get("params")
+            if p is not None and np.asarray(p).ndim > 1 and np.asarray(p).shape[0] > 1:
+                raise ValueError(f"gate {name}: a batch circuit takes one parameter row (got {np.asarray(p).shape})")
             pt = None if p is None else torch.tensor(np.asarray(p, np.float64).reshape(1, -1))
             mat = G.gate_matrix(name, pt, len(wires), dtype=torch.complex128)[0].numpy()
+            if g.get("inverse"):
+                mat = mat.conj().T
             if len(wires) == 1:
                 pending[wires[0]] = mat @ pending.get(wires[0], np.eye(2))
                 continue

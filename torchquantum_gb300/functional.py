@@ -139,7 +139,9 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
                               inverse=inverse)
         return
     cname = G.canonical_name(name)
-    if mat is None and cname in program.NATIVE and isinstance(params, torch.Tensor) and not params.is_complex():
+    density = getattr(q_device, "is_density", False)
+    if mat is None and cname in program.NATIVE and isinstance(params, torch.Tensor) and not params.is_complex() \
+            and not density:
         nat = _native_record(cname, wires, params, inverse, q_device)
         if nat is not None:
             q_device._apply(nat)
@@ -166,6 +168,10 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
         matrix = matrix.permute(0, 2, 1) if matrix.dim() == 3 else matrix.permute(1, 0)
     dim = matrix.shape[-1]
     assert int(round(math.log2(dim))) == len(wires), f"{name}: matrix of dim {dim} on wires {wires}"
+    if density:  # rho -> U rho U^H (density.NoiseDevice; a global phase cancels)
+        if len(wires):
+            q_device._apply_matrix(matrix, wires)
+        return
     if len(wires) == 0:  # globalphase: a phase on every amplitude
         ph = matrix.reshape(-1).to(q_device.device)
         q_device._apply(engine.TapeOp(engine.KIND_PHASE, [], operand=engine.kernel_operand(ph.to(torch.complex64)),

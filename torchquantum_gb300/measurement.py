@@ -152,7 +152,11 @@ def measure(qdev, n_shots: int = 1024, draw_id: Optional[int] = None, generator:
     ``generator``: a CUDA torch.Generator for reproducible draws.  ``draw_id`` plots
     that row's histogram when matplotlib is installed."""
     n = qdev.n_wires
-    st = kernel_operand(_state_2d(qdev))
+    if getattr(qdev, "is_density", False):  # sample the diagonal of rho (measurements.py:51-55)
+        p = qdev.get_probs_1d().detach().real.clamp_min(0)
+        st = torch.sqrt(p).to(torch.complex64).contiguous()
+    else:
+        st = kernel_operand(_state_2d(qdev))
     bsz = st.shape[0]
     u = torch.rand(bsz, int(n_shots), dtype=torch.float64, device=st.device, generator=generator)
     idx = _lib.sample(st, n, u)
