@@ -141,3 +141,33 @@ def test_staged_abi_rejects_target_outside_tile():
     _lib.staged_apply(psi, n, [d], 12)
     with pytest.raises(_lib.TQKError, match="tile_bits"):
         _lib.staged_apply(psi, n, [d], 13)
+
+
+def _pair_base(q, lb):
+    """Host model of staged.cu's pair_base (index of the first pair of pair-pair q)."""
+    if lb == 0:
+        return q << 1
+    lowm = (1 << (lb - 1)) - 1
+    return ((q >> (lb - 1)) << (lb + 1)) | ((q & lowm) << 1)
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 5, 8, 12])
+def test_staged_pair_indexing_covers_every_pair_once(m):
+    """The staged kernels visit, for a target bit lb of a 2^m tile, every amplitude pair
+    (i, i | 2^lb) with bit lb of i clear exactly once, through 16-byte-aligned float4
+    accesses inside the tile (checked on the CPU before any launch)."""
+    tsz = 1 << m
+    for lb in range(m):
+        nq = tsz >> 1 if lb == 0 else tsz >> 2
+        seen = []
+        for q in range(nq):
+            i0 = _pair_base(q, lb)
+            assert i0 % 2 == 0 and (i0 >> lb) & 1 == 0
+            if lb == 0:
+                seen.append((i0, i0 + 1))
+            else:
+                i1 = i0 | (1 << lb)
+                assert i1 < tsz and i1 % 2 == 0
+                seen += [(i0, i1), (i0 + 1, i1 + 1)]
+        want = [(i, i | (1 << lb)) for i in range(tsz) if not (i >> lb) & 1]
+        assert sorted(seen) == want

@@ -46,45 +46,127 @@ struct Params {
   SOp ops[TQK_STAGED_MAX_OPS];
 };
 
-__device__ __forceinline__ int diag_index(const SOp& o, uint64_t g) {
-  int d = 0;
-  for (int j = 0; j < o.nd; ++j) d = (d << 1) | (int)((g >> o.dbits[j]) & 1ull);
+// Per-tile view of an op: its control / phase condition split into the bits inside the
+// tile (checked per amplitude, 32-bit) and the bits above it (uniform for the tile).
+struct Local {
+  bool active;      // the condition on the bits above the tile holds
+  uint32_t lmask;   // condition bits inside the tile
+  uint32_t lval;    // their required values
+  int dsh[2];       // DIAG: local bit of diag-index bit j, or -1 (then dconst)
+  int dconst;       // DIAG: diag-index bits that come from above the tile
+};
+
+__device__ __forceinline__ Local localise(const SOp& o, int m, uint64_t base) {
+  Local L;
+  const uint64_t lo = (1ull << m) - 1ull;
+  if (o.kind == TQK_S_DIAG) {
+    L.active = true;
+    L.lmask = L.lval = 0;
+    L.dconst = 0;
+    for (int j = 0; j < 2; ++j) {
+      L.dsh[j] = -1;
+      if (j >= o.nd) continue;
+      const int bit = o.dbits[j];
+      const int place = o.nd - 1 - j;  // dbits[0] is the most significant diag-index bit
+      if (bit < m) L.dsh[j] = bit;
+      else if ((base >> bit) & 1ull) L.dconst |= 1 << place;
+    }
+    return L;
+  }
+  const uint64_t val = o.kind == TQK_S_PHASE ? o.cmask : o.cval;
+  L.active = (base & (o.cmask & ~lo)) == (val & ~lo);
+  L.lmask = static_cast<uint32_t>(o.cmask & lo);
+  L.lval = static_cast<uint32_t>(val & lo);
+  return L;
+}
+
+__device__ __forceinline__ int diag_local(const SOp& o, const Local& L, uint32_t l) {
+  int d = L.dconst;
+  if (L.dsh[0] >= 0) d |= static_cast<int>((l >> L.dsh[0]) & 1u) << (o.nd - 1);
+  if (L.dsh[1] >= 0) d |= static_cast<int>((l >> L.dsh[1]) & 1u);
   return d;
+}
+
+// First index i0 (target bit lb clear) of pair-pair q: two adjacent pairs (i0, i0 + 2^lb)
+// and (i0 + 1, i0 + 1 + 2^lb) when lb >= 1; one pair (2q, 2q + 1) when lb == 0.
+__device__ __forceinline__ uint32_t pair_base(uint32_t q, int lb) {
+  if (lb == 0) return q << 1;
+  const uint32_t lowm = (1u << (lb - 1)) - 1u;
+  return ((q >> (lb - 1)) << (lb + 1)) | ((q & lowm) << 1);
+}
+
+__device__ __forceinline__ void mat2(const float2 (&M)[4], float2& a0, float2& a1) {
+  const float2 y0 = cfma(M[0], a0, cmul(M[1], a1));
+  a1 = cfma(M[2], a0, cmul(M[3], a1));
+  a0 = y0;
 }
 
 // Forward application of one op to the tile (amp, 2^m amplitudes at global index base).
 __device__ __forceinline__ void apply_fwd(const SOp& o, float2* amp, int m, uint64_t base, int64_t b) {
+  const Local L = localise(o, m, base);
+  if (!L.active) return;  // uniform for the tile
   const int tsz = 1 << m;
+  float4* amp4 = reinterpret_cast<float4*>(amp);
   if (o.kind == TQK_S_DENSE1 || o.kind == TQK_S_X) {
     const int lb = o.lb;
-    float2 m00, m01, m10, m11;
-    if (o.kind == TQK_S_DENSE1) {
-      const float2* M = o.operand + b * o.op_stride;
-      m00 = __ldg(M);
-      m01 = __ldg(M + 1);
-      m10 = __ldg(M + 2);
-      m11 = __ldg(M + 3);
+    const bool x = o.kind == TQK_S_X;
+    float2 M[4];
+    if (!x) {
+      const float2* src = o.operand + b * o.op_stride;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) M[e] = __ldg(src + e);
     }
-    for (int p = threadIdx.x; p < (tsz >> 1); p += kThreads) {
-      const int i0 = ((p >> lb) << (lb + 1)) | (p & ((1 << lb) - 1));
-      const int i1 = i0 | (1 << lb);
-      if (((base | (uint64_t)i0) & o.cmask) != o.cval) continue;
-      const float2 a0 = amp[i0], a1 = amp[i1];
-      if (o.kind == TQK_S_X) {
-        amp[i0] = a1;
-        amp[i1] = a0;
-      } else {
-        amp[i0] = cfma(m00, a0, cmul(m01, a1));
-        amp[i1] = cfma(m10, a0, cmul(m11, a1));
+    const uint32_t nq = lb == 0 ? static_cast<uint32_t>(tsz >> 1) : static_cast<uint32_t>(tsz >> 2);
+    for (uint32_t q = threadIdx.x; q < nq; q += kThreads) {
+      const uint32_t i0 = pair_base(q, lb);
+      if (lb == 0) {
+        if ((i0 & L.lmask) != L.lval) continue;
+        float4 v = amp4[i0 >> 1];
+        float2 a0 = lo2(v), a1 = hi2(v);
+        if (x) amp4[i0 >> 1] = pack4(a1, a0);
+        else {
+          mat2(M, a0, a1);
+          amp4[i0 >> 1] = pack4(a0, a1);
+        }
+        continue;
       }
+      const uint32_t i1 = i0 | (1u << lb);
+      const bool ok0 = (i0 & L.lmask) == L.lval, ok1 = ((i0 | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 va = amp4[i0 >> 1], vb = amp4[i1 >> 1];
+      float2 a0 = lo2(va), b0 = lo2(vb), a1 = hi2(va), b1 = hi2(vb);  // pairs (a0, b0), (a1, b1)
+      if (x) {
+        if (ok0) { const float2 t = a0; a0 = b0; b0 = t; }
+        if (ok1) { const float2 t = a1; a1 = b1; b1 = t; }
+      } else {
+        if (ok0) mat2(M, a0, b0);
+        if (ok1) mat2(M, a1, b1);
+      }
+      amp4[i0 >> 1] = pack4(a0, a1);
+      amp4[i1 >> 1] = pack4(b0, b1);
     }
   } else if (o.kind == TQK_S_PHASE) {
     const float2 ph = __ldg(o.operand + b * o.op_stride);
-    for (int l = threadIdx.x; l < tsz; l += kThreads)
-      if (((base | (uint64_t)l) & o.cmask) == o.cmask) amp[l] = cmul(ph, amp[l]);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      const bool ok0 = (l & L.lmask) == L.lval, ok1 = ((l | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 v = amp4[q];
+      float2 a0 = lo2(v), a1 = hi2(v);
+      if (ok0) a0 = cmul(ph, a0);
+      if (ok1) a1 = cmul(ph, a1);
+      amp4[q] = pack4(a0, a1);
+    }
   } else {  // DIAG
     const float2* dv = o.operand + b * o.op_stride;
-    for (int l = threadIdx.x; l < tsz; l += kThreads) amp[l] = cmul(__ldg(dv + diag_index(o, base | (uint64_t)l)), amp[l]);
+    float2 D[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) D[e] = e < (1 << o.nd) ? __ldg(dv + e) : make_float2(0.f, 0.f);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      float4 v = amp4[q];
+      amp4[q] = pack4(cmul(D[diag_local(o, L, l)], lo2(v)), cmul(D[diag_local(o, L, l | 1u)], hi2(v)));
+    }
   }
 }
 
@@ -130,85 +212,128 @@ __device__ __forceinline__ void block_accumulate(float (&v)[NV], float (*red)[8]
   }
 }
 
+__device__ __forceinline__ void acc_c(float (&g)[8], int slot, float2 l, float2 y) {  // g[slot] += l conj(y)
+  const float2 v = cfma_bconj(l, y, make_float2(g[2 * slot], g[2 * slot + 1]));
+  g[2 * slot] = v.x;
+  g[2 * slot + 1] = v.y;
+}
+
+// Reverse step of a dense 2x2 on one pair: psi (a0, a1) <- U^H, lam (l0, l1) <- U^H, and
+// the cotangent g[r][c] += lam_in_r conj(psi_out_c).
+__device__ __forceinline__ void adj_pair(const float2 (&M)[4], float2& a0, float2& a1, float2& l0, float2& l1,
+                                         bool grad, float (&g)[8]) {
+  const float2 y0 = cfma_conj(M[0], a0, cfma_conj(M[2], a1, make_float2(0.f, 0.f)));
+  const float2 y1 = cfma_conj(M[1], a0, cfma_conj(M[3], a1, make_float2(0.f, 0.f)));
+  if (grad) {
+    acc_c(g, 0, l0, y0);
+    acc_c(g, 1, l0, y1);
+    acc_c(g, 2, l1, y0);
+    acc_c(g, 3, l1, y1);
+  }
+  const float2 z0 = cfma_conj(M[0], l0, cfma_conj(M[2], l1, make_float2(0.f, 0.f)));
+  l1 = cfma_conj(M[1], l0, cfma_conj(M[3], l1, make_float2(0.f, 0.f)));
+  l0 = z0;
+  a0 = y0;
+  a1 = y1;
+}
+
 // One reverse step of op o on the psi / lam tiles; cotangent partials into acc (8 doubles).
 __device__ __forceinline__ void apply_adj(const SOp& o, float2* ps, float2* ls, int m, uint64_t base, int64_t b,
                                           float (*red)[8], double* acc) {
+  const Local L = localise(o, m, base);
+  if (!L.active) return;  // uniform for the tile
   const int tsz = 1 << m;
   const bool grad = o.grad != nullptr;
-  if (o.kind == TQK_S_X) {
-    const int lb = o.lb;
-    for (int p = threadIdx.x; p < (tsz >> 1); p += kThreads) {
-      const int i0 = ((p >> lb) << (lb + 1)) | (p & ((1 << lb) - 1));
-      const int i1 = i0 | (1 << lb);
-      if (((base | (uint64_t)i0) & o.cmask) != o.cval) continue;
-      float2 t = ps[i0];
-      ps[i0] = ps[i1];
-      ps[i1] = t;
-      t = ls[i0];
-      ls[i0] = ls[i1];
-      ls[i1] = t;
-    }
-    return;
-  }
+  float4* p4 = reinterpret_cast<float4*>(ps);
+  float4* l4 = reinterpret_cast<float4*>(ls);
   float g[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) g[j] = 0.f;
-  if (o.kind == TQK_S_DENSE1) {
+  if (o.kind == TQK_S_DENSE1 || o.kind == TQK_S_X) {
     const int lb = o.lb;
-    const float2* M = o.operand + b * o.op_stride;
-    const float2 m00 = __ldg(M), m01 = __ldg(M + 1), m10 = __ldg(M + 2), m11 = __ldg(M + 3);
-    for (int p = threadIdx.x; p < (tsz >> 1); p += kThreads) {
-      const int i0 = ((p >> lb) << (lb + 1)) | (p & ((1 << lb) - 1));
-      const int i1 = i0 | (1 << lb);
-      if (((base | (uint64_t)i0) & o.cmask) != o.cval) continue;
-      const float2 a0 = ps[i0], a1 = ps[i1], l0 = ls[i0], l1 = ls[i1];
-      // U^H: [conj m00, conj m10; conj m01, conj m11]
-      const float2 y0 = cfma_conj(m00, a0, cfma_conj(m10, a1, make_float2(0.f, 0.f)));
-      const float2 y1 = cfma_conj(m01, a0, cfma_conj(m11, a1, make_float2(0.f, 0.f)));
-      ps[i0] = y0;
-      ps[i1] = y1;
-      ls[i0] = cfma_conj(m00, l0, cfma_conj(m10, l1, make_float2(0.f, 0.f)));
-      ls[i1] = cfma_conj(m01, l0, cfma_conj(m11, l1, make_float2(0.f, 0.f)));
-      if (grad) {  // g[r][c] += l_r conj(y_c)
-        float2 v;
-        v = cfma_bconj(l0, y0, make_float2(g[0], g[1]));
-        g[0] = v.x, g[1] = v.y;
-        v = cfma_bconj(l0, y1, make_float2(g[2], g[3]));
-        g[2] = v.x, g[3] = v.y;
-        v = cfma_bconj(l1, y0, make_float2(g[4], g[5]));
-        g[4] = v.x, g[5] = v.y;
-        v = cfma_bconj(l1, y1, make_float2(g[6], g[7]));
-        g[6] = v.x, g[7] = v.y;
-      }
+    const bool x = o.kind == TQK_S_X;
+    float2 M[4];
+    if (!x) {
+      const float2* src = o.operand + b * o.op_stride;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) M[e] = __ldg(src + e);
     }
+    const uint32_t nq = lb == 0 ? static_cast<uint32_t>(tsz >> 1) : static_cast<uint32_t>(tsz >> 2);
+    for (uint32_t q = threadIdx.x; q < nq; q += kThreads) {
+      const uint32_t i0 = pair_base(q, lb);
+      if (lb == 0) {
+        if ((i0 & L.lmask) != L.lval) continue;
+        float4 va = p4[i0 >> 1], vl = l4[i0 >> 1];
+        float2 a0 = lo2(va), a1 = hi2(va), l0 = lo2(vl), l1 = hi2(vl);
+        if (x) {
+          p4[i0 >> 1] = pack4(a1, a0);
+          l4[i0 >> 1] = pack4(l1, l0);
+        } else {
+          adj_pair(M, a0, a1, l0, l1, grad, g);
+          p4[i0 >> 1] = pack4(a0, a1);
+          l4[i0 >> 1] = pack4(l0, l1);
+        }
+        continue;
+      }
+      const uint32_t i1 = i0 | (1u << lb);
+      const bool ok0 = (i0 & L.lmask) == L.lval, ok1 = ((i0 | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 pa = p4[i0 >> 1], pb = p4[i1 >> 1], la = l4[i0 >> 1], lb4 = l4[i1 >> 1];
+      float2 a0 = lo2(pa), b0 = lo2(pb), a1 = hi2(pa), b1 = hi2(pb);
+      float2 c0 = lo2(la), d0 = lo2(lb4), c1 = hi2(la), d1 = hi2(lb4);
+      if (x) {
+        if (ok0) { float2 t = a0; a0 = b0; b0 = t; t = c0; c0 = d0; d0 = t; }
+        if (ok1) { float2 t = a1; a1 = b1; b1 = t; t = c1; c1 = d1; d1 = t; }
+      } else {
+        if (ok0) adj_pair(M, a0, b0, c0, d0, grad, g);
+        if (ok1) adj_pair(M, a1, b1, c1, d1, grad, g);
+      }
+      p4[i0 >> 1] = pack4(a0, a1);
+      p4[i1 >> 1] = pack4(b0, b1);
+      l4[i0 >> 1] = pack4(c0, c1);
+      l4[i1 >> 1] = pack4(d0, d1);
+    }
+    if (x) return;
   } else if (o.kind == TQK_S_PHASE) {
     const float2 phc = cconj(__ldg(o.operand + b * o.op_stride));
-    for (int l = threadIdx.x; l < tsz; l += kThreads) {
-      if (((base | (uint64_t)l) & o.cmask) != o.cmask) continue;
-      const float2 y = cmul(phc, ps[l]), lv = ls[l];
-      ps[l] = y;
-      ls[l] = cmul(phc, lv);
-      if (grad) {
-        const float2 v = cfma_bconj(lv, y, make_float2(g[0], g[1]));
-        g[0] = v.x, g[1] = v.y;
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      const bool ok0 = (l & L.lmask) == L.lval, ok1 = ((l | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 vp = p4[q], vl = l4[q];
+      float2 a0 = lo2(vp), a1 = hi2(vp), c0 = lo2(vl), c1 = hi2(vl);
+      if (ok0) {
+        a0 = cmul(phc, a0);
+        if (grad) acc_c(g, 0, c0, a0);
+        c0 = cmul(phc, c0);
       }
+      if (ok1) {
+        a1 = cmul(phc, a1);
+        if (grad) acc_c(g, 0, c1, a1);
+        c1 = cmul(phc, c1);
+      }
+      p4[q] = pack4(a0, a1);
+      l4[q] = pack4(c0, c1);
     }
   } else {  // DIAG (nd <= 2)
     const float2* dv = o.operand + b * o.op_stride;
-    for (int l = threadIdx.x; l < tsz; l += kThreads) {
-      const int d = diag_index(o, base | (uint64_t)l);
-      const float2 c = cconj(__ldg(dv + d));
-      const float2 y = cmul(c, ps[l]), lv = ls[l];
-      ps[l] = y;
-      ls[l] = cmul(c, lv);
+    float2 D[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) D[e] = e < (1 << o.nd) ? cconj(__ldg(dv + e)) : make_float2(0.f, 0.f);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      const int d0 = diag_local(o, L, l), d1 = diag_local(o, L, l | 1u);
+      float4 vp = p4[q], vl = l4[q];
+      const float2 y0 = cmul(D[d0], lo2(vp)), y1 = cmul(D[d1], hi2(vp));
       if (grad) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (j == d) {
-            const float2 v = cfma_bconj(lv, y, make_float2(g[2 * j], g[2 * j + 1]));
-            g[2 * j] = v.x, g[2 * j + 1] = v.y;
-          }
+        for (int j = 0; j < 4; ++j) {
+          if (j == d0) acc_c(g, j, lo2(vl), y0);
+          if (j == d1) acc_c(g, j, hi2(vl), y1);
+        }
       }
+      p4[q] = pack4(y0, y1);
+      l4[q] = pack4(cmul(D[d0], lo2(vl)), cmul(D[d1], hi2(vl)));
     }
   }
   if (grad) block_accumulate<8>(g, red, acc);
