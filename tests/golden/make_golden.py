@@ -24,6 +24,8 @@ Outputs (all small ``.npz`` files, committed):
   inputs, complex64 and complex128.
 * ``density.npz`` -- upstream's density-matrix device on circuits of symmetric gates,
   plus one circuit with RY that records upstream's rho conj(U) defect.
+* ``random_layers.npz`` -- seeded upstream ``RandomLayer`` / ``RandomLayerAllTypes`` op
+  lists, parameters and states, and ``find_observable_groups`` on seeded observable lists.
 * ``known_answers.npz`` -- the upstream known-answer tests (``test/device/test_init.py:32``,
   ``test/functional/test_controlled_unitary.py:30``, ``test/functional/test_func_mat_exp.py:30``,
   ``test/operator/test_ControlledU.py:40``, ``test/operator/test_op_hamil_exp.py:32``) and the
@@ -302,6 +304,49 @@ def make_density(rng):
     print(f"density: {len(index)} cases")
 
 
+def make_random_layers_and_groups(rng):
+    """Upstream ``RandomLayer`` / ``RandomLayerAllTypes`` (layer/layers/random_layers.py:80-298)
+    built with a seed after ``torch.manual_seed``: op names, wires, parameters and the
+    complex128 state they produce; and upstream ``find_observable_groups``
+    (measurement/measurements.py:77-111) on seeded observable lists."""
+    from torchquantum.measurement import find_observable_groups
+
+    out, index = {}, []
+    specs = [("RandomLayer", 4, 30, 11), ("RandomLayer", 6, 50, 12), ("RandomLayerAllTypes", 5, 40, 13)]
+    for ci, (cls, n, n_ops, seed) in enumerate(specs):
+        # built in upstream's default precision: float32 parameters draw from torch's
+        # generator like the engine's operators do
+        refimport.set_reference_precision(False)
+        torch.manual_seed(seed)
+        layer = getattr(tq, cls)(n_ops=n_ops, wires=list(range(n)), seed=seed)
+        refimport.set_reference_precision(True)
+        ops_meta = []
+        for o in layer.op_list:
+            p = o.params.detach().numpy().tolist() if getattr(o, "params", None) is not None else None
+            ops_meta.append({"name": o.name, "wires": [int(w) for w in np.atleast_1d(o.wires)], "params": p})
+        q = tq.QuantumDevice(n_wires=n, bsz=1)
+        q.states = q.states.to(torch.complex128)
+        try:
+            layer(q)
+            out[f"r{ci}__state"] = q.get_states_1d().detach().numpy()
+            ok = True
+        except NameError:  # upstream gates with the mat_dict NameError (u1, u2, ...)
+            ok = False
+        index.append({"key": f"r{ci}", "cls": cls, "n": n, "n_ops": n_ops, "seed": seed, "ops": ops_meta,
+                      "state": ok})
+    refimport.set_reference_precision(False)
+    groups = []
+    for gi in range(6):
+        n = int(rng.integers(3, 7))
+        m = int(rng.integers(4, 20))
+        obs = sorted({random_pauli(rng, n) for _ in range(m)})
+        rng.shuffle(obs)
+        groups.append({"observables": list(obs), "groups": find_observable_groups(list(obs))})
+    out["__meta__"] = np.array(json.dumps({"layers": index, "groups": groups}))
+    np.savez_compressed(os.path.join(HERE, "random_layers.npz"), **out)
+    print(f"random layers: {len(index)}, observable groupings: {len(groups)}")
+
+
 def make_hea(rng):
     """Differentiation workload at reduced size: optional per-sample RY(x) input layer,
     then L layers of (RY on every wire, RZ on every wire, CZ ladder (i, i+1)) with one
@@ -451,3 +496,4 @@ if __name__ == "__main__":
     make_known_answers()
     make_hea(np.random.default_rng(4))
     make_density(np.random.default_rng(5))
+    make_random_layers_and_groups(np.random.default_rng(6))

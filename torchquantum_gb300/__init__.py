@@ -19,7 +19,8 @@ from .layers import *  # noqa: F401,F403
 from .encoding import GeneralEncoder, StateEncoder, Encoder  # noqa: F401
 from .measurement import expval_joint_analytical, expval_joint_analytical_batch, expval, MeasureAll, probs  # noqa
 from .measurement import measure, gen_bitstrings, MeasureMultipleTimes, MeasureMultiPauliSum, \
-    MeasureMultiQubitPauliSum  # noqa: F401
+    MeasureMultiQubitPauliSum, find_observable_groups, expval_joint_sampling, \
+    expval_joint_sampling_grouping  # noqa: F401
 from . import measurement  # noqa: F401
 from .density import NoiseDevice  # noqa: F401
 

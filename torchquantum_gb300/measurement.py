@@ -22,7 +22,7 @@ host for ``random.choices``.
 from __future__ import annotations
 
 from collections import OrderedDict
-from typing import List, Optional, Sequence, Union
+from typing import Dict, List, Optional, Sequence, Union
 
 import numpy as np
 import torch
@@ -33,7 +33,8 @@ from .module import QuantumModule
 
 __all__ = ["expval_joint_analytical", "expval_joint_analytical_batch", "expval", "MeasureAll", "probs",
            "pauli_masks", "measure", "gen_bitstrings", "MeasureMultipleTimes", "MeasureMultiPauliSum",
-           "MeasureMultiQubitPauliSum"]
+           "MeasureMultiQubitPauliSum", "find_observable_groups", "expval_joint_sampling",
+           "expval_joint_sampling_grouping"]
 
 
 def pauli_masks(observable: str, n: int):
@@ -183,6 +184,93 @@ def measure(qdev, n_shots: int = 1024, draw_id: Optional[int] = None, generator:
             plt.xlabel("bitstring [qubit0, qubit1, ..., qubitN]")
             plt.title("distribution of measured bitstrings")
             plt.show()
+    return out
+
+
+# ------------------------------------------------------------------ sampled expectation values
+def find_observable_groups(observables: Sequence[str]) -> Dict[str, List[str]]:
+    """Group Pauli strings that one measurement basis serves (measurements.py:77-111):
+    each string joins the first group, in insertion order, whose basis agrees with it on
+    every non-identity site (the group's identity sites take the string's Pauli); the
+    grown group moves to the end of the dict.  Otherwise it starts a new group."""
+    groups: Dict[str, List[str]] = {}
+    for ob in observables:
+        hit = None
+        for g in groups:
+            grown = list(g)
+            ok = True
+            for k, ch in enumerate(ob):
+                if ch == "I" or ch == g[k]:
+                    continue
+                if g[k] == "I":
+                    grown[k] = ch
+                    continue
+                ok = False
+                break
+            if ok:
+                hit = (g, "".join(grown))
+                break
+        if hit is None:
+            groups[ob] = [ob]
+        else:
+            members = groups.pop(hit[0])
+            members.append(ob)
+            groups[hit[1]] = members
+    return groups
+
+
+def _parity64(v: torch.Tensor) -> torch.Tensor:
+    for sh in (32, 16, 8, 4, 2, 1):
+        v = v ^ (v >> sh)
+    return v & 1
+
+
+def _rotated_samples(qdev, basis: str, n_shots: int, generator=None) -> torch.Tensor:
+    """Outcome indices [bsz, n_shots] after rotating a copy of the state into ``basis``."""
+    from .device import QuantumDevice
+    from .operators import op_name_dict
+
+    n = qdev.n_wires
+    qc = QuantumDevice(n_wires=n, bsz=qdev.bsz, device=qdev.device)
+    qc.set_states(qdev.get_states_1d().detach())
+    names = {"X": "paulix", "Y": "pauliy", "Z": "pauliz", "I": "i"}
+    for w, ch in enumerate(basis):
+        for rot in op_name_dict[names[ch]]().diagonalizing_gates():
+            rot(qc, wires=w)
+    st = kernel_operand(_state_2d(qc))
+    u = torch.rand(st.shape[0], int(n_shots), dtype=torch.float64, device=st.device, generator=generator)
+    return _lib.sample(st, n, u)
+
+
+def _sampled_expval(idx: torch.Tensor, observable: str, n: int) -> torch.Tensor:
+    mask = 0
+    for w, ch in enumerate(observable):
+        if ch != "I":
+            mask |= 1 << (n - 1 - w)
+    par = _parity64(idx & mask)
+    return (1.0 - 2.0 * par.to(torch.float64)).mean(dim=1).to(torch.float32)
+
+
+def expval_joint_sampling(qdev, observable: str, n_shots: int = 1024, generator=None) -> torch.Tensor:
+    """<P> estimated from ``n_shots`` basis-rotated samples per row (measurements.py:169-229),
+    [bsz] float32: the share of shots with even parity on the non-identity sites minus the
+    share with odd parity, counted on the GPU."""
+    observable = observable.upper()
+    idx = _rotated_samples(qdev, observable, n_shots, generator)
+    return _sampled_expval(idx, observable, qdev.n_wires)
+
+
+def expval_joint_sampling_grouping(qdev, observables: Sequence[str], n_shots_per_group: int = 1024,
+                                   generator=None) -> Dict[str, torch.Tensor]:
+    """Sampled <P> for several strings, one set of shots per group of
+    ``find_observable_groups`` (measurements.py:114-166): {string: [bsz] float32}."""
+    assert len(observables) == len(set(observables)), "each observable should be unique"
+    obs = [o.upper() for o in observables]
+    out = {}
+    for basis, members in find_observable_groups(obs).items():
+        idx = _rotated_samples(qdev, basis, n_shots_per_group, generator)
+        for ob in members:
+            out[ob] = _sampled_expval(idx, ob, qdev.n_wires)
     return out
 
 
