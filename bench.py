@@ -285,6 +285,9 @@ def run_ours(args):
             "clocks": clk.summary(), "gpu_launches": launches}
     if fusion_info:
         line["config"]["fusion"] = fusion_info
+    # gate applications per second (each circuit applies `depth` gates forward and
+    # reverses them in the adjoint sweep)
+    line["gate_applications_per_s"] = value * args.depth
     if world > 1:
         line["config"]["parallelism"] = f"replicas x{world} (batch sharding, no collective in the step)"
 
@@ -306,7 +309,8 @@ def run_ours(args):
             torch.cuda.synchronize()
             ms_plain = R.max_over_ranks(e0.elapsed_time(e1), dev)
             v_plain = R.job_throughput(bsz * args.steps, world, ms_plain / 1e3)
-            line[key] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps}
+            line[key] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
+                         "gate_applications_per_s": v_plain * args.depth}
         line["fused_speedup_vs_plain"] = value / line["plain_gate_by_gate"]["value"]
         line["fused_speedup_vs_plain_staged"] = value / line["plain_method"]["value"]
     if not args.quick:

@@ -192,3 +192,67 @@ def test_op_history_ingestion():
     np.testing.assert_allclose(got, O.run(n, 1, og)[0], atol=1e-6)
     with pytest.raises(ValueError, match="one parameter row"):
         B.CircuitBatch().add_gates(2, [{"name": "rx", "wires": 0, "params": [[0.1], [0.2]]}])
+
+
+def _local_pos(tmask, b):
+    return bin(tmask & ((1 << b) - 1)).count("1")
+
+
+def _cz_terms(tmask, base, b0, b1, st):
+    """Host model of batch.cu's cz_terms: split a CZ's sign into tile-local terms."""
+    in0, in1 = (tmask >> b0) & 1, (tmask >> b1) & 1
+    if in0 and in1:
+        p0, p1 = _local_pos(tmask, b0), _local_pos(tmask, b1)
+        lo, hi = min(p0, p1), max(p0, p1)
+        if hi == lo + 1:
+            st["quad"] |= 1 << lo
+        else:
+            st["pairs"] |= (1 << lo) | (1 << hi)
+    elif in0:
+        if (base >> b1) & 1:
+            st["lin"] ^= 1 << _local_pos(tmask, b0)
+    elif in1:
+        if (base >> b0) & 1:
+            st["lin"] ^= 1 << _local_pos(tmask, b1)
+    else:
+        st["c0"] ^= (base >> b0) & (base >> b1) & 1
+
+
+def test_cz_sign_split_matches_global_index():
+    """The batch kernel's CZ / CZ-ladder signs, computed from the tile-local index with
+    per-tile constants, equal the signs computed from each amplitude's global index."""
+    rng = np.random.default_rng(0)
+    for _ in range(60):
+        n = int(rng.integers(3, 16))
+        tb = int(rng.integers(1, n + 1))
+        bits = sorted(rng.choice(n, size=tb, replace=False))
+        tmask = sum(1 << int(b) for b in bits)
+        other = [b for b in range(n) if not (tmask >> b) & 1]
+        base = sum(1 << b for b in other if rng.random() < 0.5)
+        locs = np.arange(1 << tb)
+        glob = np.full(1 << tb, base)
+        for j, b in enumerate(bits):
+            glob |= ((locs >> j) & 1) << int(b)
+        # a ladder over wires w0..w1 and a single CZ
+        w0 = int(rng.integers(0, n - 1))
+        w1 = int(rng.integers(w0 + 1, n))
+        st = {"c0": 0, "lin": 0, "quad": 0, "pairs": 0}
+        for w in range(w0, w1):
+            _cz_terms(tmask, base, n - 1 - w, n - 2 - w, st)
+        assert st["pairs"] == 0
+        got = (st["c0"] + np.array([bin(l & st["lin"]).count("1") + bin(l & (l >> 1) & st["quad"]).count("1")
+                                    for l in locs])) & 1
+        want = np.zeros(1 << tb, dtype=int)
+        for w in range(w0, w1):
+            want ^= ((glob >> (n - 1 - w)) & (glob >> (n - 2 - w)) & 1)
+        assert (got == want).all()
+        a, c = [int(x) for x in rng.choice(n, 2, replace=False)]
+        st = {"c0": 0, "lin": 0, "quad": 0, "pairs": 0}
+        _cz_terms(tmask, base, n - 1 - a, n - 1 - c, st)
+        if st["pairs"]:
+            got = np.array([(l & st["pairs"]) == st["pairs"] for l in locs]).astype(int)
+        else:
+            got = (st["c0"] + np.array([bin(l & st["lin"]).count("1") + bin(l & (l >> 1) & st["quad"]).count("1")
+                                        for l in locs])) & 1
+        want = (glob >> (n - 1 - a)) & (glob >> (n - 1 - c)) & 1
+        assert (got == want).all()

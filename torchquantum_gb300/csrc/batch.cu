@@ -45,55 +45,130 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // a * b
 }
 
 // 2x2 matrix m on local bit lb of the tile; if lc >= 0 only where local bit lc is set.
+// Two adjacent pairs (i0, i0 + 2^lb), (i0 + 1, i0 + 1 + 2^lb) per 16-byte access when
+// lb >= 1, one pair (2q, 2q + 1) per access when lb == 0.
 template <int THREADS>
 __device__ __forceinline__ void apply_1q(float2* amp, int tb, int lb, int lc, const float2* m) {
-  const float2 m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
-  const int half = 1 << (tb - 1);
-  for (int p = threadIdx.x; p < half; p += THREADS) {
-    const int i0 = ((p >> lb) << (lb + 1)) | (p & ((1 << lb) - 1));
-    if (lc >= 0 && !((i0 >> lc) & 1)) continue;
-    const int i1 = i0 | (1 << lb);
-    const float2 a0 = amp[i0], a1 = amp[i1];
-    amp[i0] = cfma(m00, a0, cmul(m01, a1));
-    amp[i1] = cfma(m10, a0, cmul(m11, a1));
+  float2 M[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) M[e] = __ldg(m + e);
+  const uint32_t cm = lc >= 0 ? (1u << lc) : 0u;
+  float4* amp4 = reinterpret_cast<float4*>(amp);
+  if (lb == 0) {
+    for (uint32_t q = threadIdx.x; q < (1u << (tb - 1)); q += THREADS) {
+      const uint32_t i0 = q << 1;
+      if ((i0 & cm) != cm) continue;
+      const float4 v = amp4[q];
+      const float2 a0 = lo2(v), a1 = hi2(v);
+      amp4[q] = pack4(cfma(M[0], a0, cmul(M[1], a1)), cfma(M[2], a0, cmul(M[3], a1)));
+    }
+    return;
+  }
+  const uint32_t lowm = (1u << (lb - 1)) - 1u;
+  for (uint32_t q = threadIdx.x; q < (1u << (tb - 2)); q += THREADS) {
+    const uint32_t i0 = ((q >> (lb - 1)) << (lb + 1)) | ((q & lowm) << 1);
+    const uint32_t i1 = i0 | (1u << lb);
+    const bool ok0 = (i0 & cm) == cm, ok1 = ((i0 | 1u) & cm) == cm;
+    if (!ok0 && !ok1) continue;
+    const float4 va = amp4[i0 >> 1], vb = amp4[i1 >> 1];
+    float2 a0 = lo2(va), b0 = lo2(vb), a1 = hi2(va), b1 = hi2(vb);
+    if (ok0) {
+      const float2 y = cfma(M[0], a0, cmul(M[1], b0));
+      b0 = cfma(M[2], a0, cmul(M[3], b0));
+      a0 = y;
+    }
+    if (ok1) {
+      const float2 y = cfma(M[0], a1, cmul(M[1], b1));
+      b1 = cfma(M[2], a1, cmul(M[3], b1));
+      a1 = y;
+    }
+    amp4[i0 >> 1] = pack4(a0, a1);
+    amp4[i1 >> 1] = pack4(b0, b1);
+  }
+}
+
+// Negate the amplitudes whose local index l has odd parity of c0 + popc(l & lin) +
+// popc(l & (l >> 1) & quad) (CZ and CZ ladders split into tile-local terms).
+template <int THREADS>
+__device__ __forceinline__ void apply_sign(float2* amp, int tb, int c0, uint32_t lin, uint32_t quad) {
+  float4* amp4 = reinterpret_cast<float4*>(amp);
+  for (uint32_t q = threadIdx.x; q < (1u << (tb - 1)); q += THREADS) {
+    const uint32_t l0 = q << 1, l1 = l0 | 1u;
+    const int s0 = (c0 + __popc(l0 & lin) + __popc(l0 & (l0 >> 1) & quad)) & 1;
+    const int s1 = (c0 + __popc(l1 & lin) + __popc(l1 & (l1 >> 1) & quad)) & 1;
+    if (!(s0 | s1)) continue;
+    float4 v = amp4[q];
+    if (s0) v.x = -v.x, v.y = -v.y;
+    if (s1) v.z = -v.z, v.w = -v.w;
+    amp4[q] = v;
+  }
+}
+
+__device__ __forceinline__ int local_pos(uint32_t tmask, int b) { return __popc(tmask & ((1u << b) - 1u)); }
+
+// Sign terms of CZ on global bits (bh, bl): both local -> a quadratic term only when the
+// bits are adjacent in the tile (true for ladder neighbours), else handled as lin/const.
+__device__ __forceinline__ void cz_terms(uint32_t tmask, uint32_t base, int b0, int b1, int& c0, uint32_t& lin,
+                                         uint32_t& quad, uint32_t& pairs) {
+  const bool in0 = (tmask >> b0) & 1u, in1 = (tmask >> b1) & 1u;
+  if (in0 && in1) {
+    const int p0 = local_pos(tmask, b0), p1 = local_pos(tmask, b1);
+    const int lo = p0 < p1 ? p0 : p1, hi = p0 < p1 ? p1 : p0;
+    if (hi == lo + 1) quad |= 1u << lo;
+    else pairs |= (1u << lo) | (1u << hi);  // a general local pair (single CZ only)
+  } else if (in0) {
+    if ((base >> b1) & 1u) lin ^= 1u << local_pos(tmask, b0);
+  } else if (in1) {
+    if ((base >> b0) & 1u) lin ^= 1u << local_pos(tmask, b1);
+  } else {
+    c0 ^= static_cast<int>((base >> b0) & (base >> b1) & 1u);
   }
 }
 
 template <int THREADS>
 __device__ void apply_op(const tqk_batch_op& op, float2* amp, int n, int tb, uint32_t tmask, uint32_t base,
                          const Tabs& tabs, const float2* mats) {
-  const int tsz = 1 << tb;
   switch (op.kind) {
     case TQK_B_DENSE1: {
       const int b = n - 1 - op.w0;
-      apply_1q<THREADS>(amp, tb, __popc(tmask & ((1u << b) - 1u)), -1, mats + 4 * op.mat);
+      apply_1q<THREADS>(amp, tb, local_pos(tmask, b), -1, mats + 4 * op.mat);
       break;
     }
     case TQK_B_CTRL1: {
       const int cb = n - 1 - op.w0, b = n - 1 - op.w1;
-      const int lb = __popc(tmask & ((1u << b) - 1u));
+      const int lb = local_pos(tmask, b);
       if ((tmask >> cb) & 1u) {
-        apply_1q<THREADS>(amp, tb, lb, __popc(tmask & ((1u << cb) - 1u)), mats + 4 * op.mat);
+        apply_1q<THREADS>(amp, tb, lb, local_pos(tmask, cb), mats + 4 * op.mat);
       } else if ((base >> cb) & 1u) {  // control outside the tile: set for the whole tile
         apply_1q<THREADS>(amp, tb, lb, -1, mats + 4 * op.mat);
       }
       break;
     }
     case TQK_B_CZ: {
-      const int b0 = n - 1 - op.w0, b1 = n - 1 - op.w1;
-      for (int l = threadIdx.x; l < tsz; l += THREADS) {
-        const uint32_t g = base + dep(tabs, l);
-        if ((g >> b0) & (g >> b1) & 1u) amp[l] = make_float2(-amp[l].x, -amp[l].y);
+      int c0 = 0;
+      uint32_t lin = 0, quad = 0, pairs = 0;
+      cz_terms(tmask, base, n - 1 - op.w0, n - 1 - op.w1, c0, lin, quad, pairs);
+      if (pairs) {  // both bits in the tile but not adjacent: negate where both are set
+        float4* amp4 = reinterpret_cast<float4*>(amp);
+        for (uint32_t q = threadIdx.x; q < (1u << (tb - 1)); q += THREADS) {
+          const uint32_t l0 = q << 1;
+          const bool s0 = (l0 & pairs) == pairs, s1 = ((l0 | 1u) & pairs) == pairs;
+          if (!(s0 || s1)) continue;
+          float4 v = amp4[q];
+          if (s0) v.x = -v.x, v.y = -v.y;
+          if (s1) v.z = -v.z, v.w = -v.w;
+          amp4[q] = v;
+        }
+      } else if (c0 | lin | quad) {
+        apply_sign<THREADS>(amp, tb, c0, lin, quad);
       }
       break;
     }
     case TQK_B_CZ_LADDER: {
-      uint32_t m = 0;  // bit of wire w+1 for every pair (w, w+1); the pair's other bit is one above
-      for (int w = op.w0; w < op.w1; ++w) m |= 1u << (n - 2 - w);
-      for (int l = threadIdx.x; l < tsz; l += THREADS) {
-        const uint32_t g = base + dep(tabs, l);
-        if (__popc(g & (g >> 1) & m) & 1) amp[l] = make_float2(-amp[l].x, -amp[l].y);
-      }
+      int c0 = 0;
+      uint32_t lin = 0, quad = 0, pairs = 0;
+      for (int w = op.w0; w < op.w1; ++w) cz_terms(tmask, base, n - 1 - w, n - 2 - w, c0, lin, quad, pairs);
+      if (c0 | lin | quad) apply_sign<THREADS>(amp, tb, c0, lin, quad);
       break;
     }
     default:
@@ -116,7 +191,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
     k_batch(const tqk_batch_circuit* circ, int ncirc, const tqk_batch_op* ops, const tqk_batch_pass* passes,
             const tqk_batch_item* items, long long n_items, const float2* mats, float2* states, int write_states,
             double* z_out, int* pass_done, unsigned long long* t_done, int* counter, int* status, int max_tb) {
-  extern __shared__ float2 amp[];
+  extern __shared__ float4 amp_raw[];  // 16-byte aligned: ops use float4 accesses
+  float2* amp = reinterpret_cast<float2*>(amp_raw);
   __shared__ Tabs tabs;
   __shared__ long long s_i;
   __shared__ double red[THREADS / 32];

@@ -485,8 +485,10 @@ int launch_staged(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op*
     fit = 1;
   // enough CTAs to fill the GPU (each loops over tiles of its row); the adjoint flushes
   // its cotangents once per CTA, so it stops at one wave
+  // (the adjoint grid is rounded down so every CTA is resident at once: a CTA past the
+  // first wave would run its whole tile loop after the others)
   const int64_t want = static_cast<int64_t>(sms) * fit * (adjoint ? 1 : 4);
-  int64_t gx = (want + bsz - 1) / bsz;
+  int64_t gx = adjoint ? want / bsz : (want + bsz - 1) / bsz;
   if (gx > p.tiles) gx = p.tiles;
   if (gx < 1) gx = 1;
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(bsz), 1);
