@@ -31,8 +31,19 @@ class GeneralEncoder(Encoder):
     @static_support
     def forward(self, qdev, x):
         for info in self.func_list:
-            params = x[:, info["input_idx"]] if op_name_dict[info["func"]].num_params > 0 else None
+            params = None
+            if op_name_dict[info["func"]].num_params > 0:
+                idx = info["input_idx"]
+                if _consecutive(idx):  # a view: the engine reads the angles in place
+                    params = x[:, idx[0]:idx[-1] + 1]
+                else:
+                    params = x[:, idx]
             func_name_dict[info["func"]](qdev, wires=info["wires"], params=params)
+
+
+def _consecutive(idx) -> bool:
+    return isinstance(idx, (list, tuple)) and len(idx) > 0 and all(isinstance(i, int) for i in idx) and \
+        list(idx) == list(range(idx[0], idx[0] + len(idx)))
 
 
 class StateEncoder(Encoder):

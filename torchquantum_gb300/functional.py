@@ -124,6 +124,29 @@ def _native_record(cname, wires, params, inverse, q_device):
     return program.NativeGate(cname, wires, params, inverse, kind, nctrl)
 
 
+# parameter-free gates: the engine op is built once per (gate, width, inverse, method,
+# device) and reused with the call's wires (no per-call matrix work or copies)
+_CONST_NAMES = frozenset(n for n, g in G.GATES.items()
+                         if g.num_params == 0 and g.builder is None and n not in _QU and n != "globalphase")
+_CONST_OPS: dict = {}
+
+
+def _const_op(cname, k, wires, inverse, fused, device) -> engine.TapeOp:
+    key = (cname, k, bool(inverse), bool(fused), str(device))
+    tpl = _CONST_OPS.get(key)
+    if tpl is None:
+        matrix = G.gate_matrix(cname, None, k, dtype=torch.complex128 if fused else torch.complex64, device=device)
+        if inverse:
+            matrix = matrix.conj().permute(0, 2, 1)
+        assert int(round(math.log2(matrix.shape[-1]))) == len(wires), f"{cname}: matrix on wires {wires}"
+        tpl = _op_from_matrix(cname, matrix, list(range(len(wires))), device)
+        _CONST_OPS[key] = tpl
+    op = engine.TapeOp(tpl.kind, wires, controls=[wires[i] for i in tpl.controls],
+                       targets=[wires[i] for i in tpl.targets], ctrl_val=tpl.ctrl_val, operand=tpl.operand,
+                       source=tpl.source, uncompute=tpl.uncompute)
+    return op
+
+
 def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, static=False, parent_graph=None,
                  inverse=False):
     """Apply gate ``name`` to ``q_device`` (upstream gate_wrapper.py:324-446)."""
@@ -140,6 +163,10 @@ def gate_wrapper(name, mat, method, q_device, wires, params=None, n_wires=None, 
         return
     cname = G.canonical_name(name)
     density = getattr(q_device, "is_density", False)
+    if mat is None and params is None and not density and cname in _CONST_NAMES:
+        q_device._apply(_const_op(cname, n_wires if n_wires is not None else len(wires), wires, inverse, fused,
+                                  q_device.device))
+        return
     if mat is None and cname in program.NATIVE and isinstance(params, torch.Tensor) and not params.is_complex() \
             and not density:
         nat = _native_record(cname, wires, params, inverse, q_device)

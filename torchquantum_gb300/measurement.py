@@ -103,11 +103,19 @@ def expval(qdev, wires: Union[int, List[int]], observables) -> torch.Tensor:
     n = qdev.n_wires
     strings = ["".join("Z" if w == wire else "I" for w in range(n)) for wire in wires]
     z = expval_joint_analytical_batch(qdev, strings)  # [bsz, len(wires)]
-    cols = []
-    for j, obs in enumerate(observables):
-        ev = obs.eigvals.real.to(z.device, torch.float32)
-        cols.append((ev[0] + ev[1]) / 2 + (ev[0] - ev[1]) / 2 * z[:, j])
-    return torch.stack(cols, dim=-1)
+    evs = tuple(tuple(complex(v).real for v in obs.eigvals.reshape(-1).tolist()) for obs in observables)
+    if all(e == (1.0, -1.0) for e in evs):  # Pauli eigenvalues: the Z-string values themselves
+        return z
+    key = (evs, str(z.device))
+    ab = _EIG_CACHE.get(key)
+    if ab is None:
+        ab = torch.tensor([[(e0 + e1) / 2 for e0, e1 in evs], [(e0 - e1) / 2 for e0, e1 in evs]],
+                          dtype=torch.float32, device=z.device)
+        _EIG_CACHE[key] = ab
+    return ab[0] + ab[1] * z
+
+
+_EIG_CACHE: dict = {}
 
 
 class MeasureAll(QuantumModule):

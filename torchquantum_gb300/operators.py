@@ -98,14 +98,17 @@ class Operator(QuantumModule):
             torch.nn.init.uniform_(self.params, -np.pi, np.pi)
 
     def forward(self, q_device, wires=None, params=None, inverse=None):
+        # plain attributes are written straight into __dict__: nn.Module.__setattr__ costs
+        # more than the gate itself on small circuits
+        d = self.__dict__
         if inverse is not None:
-            self.inverse = inverse
+            d["inverse"] = inverse
         if params is not None:
             self.params = params
-        if self.params is not None:
-            self.params = self.params.unsqueeze(-1) if self.params.dim() == 1 else self.params
+        if self.params is not None and self.params.dim() == 1:
+            self.params = self.params.unsqueeze(-1)
         if wires is not None:
-            self.wires = [wires] if isinstance(wires, int) else wires
+            d["wires"] = [wires] if isinstance(wires, int) else wires
         if self.params is None:
             if self.n_wires is None:
                 self.func(q_device, self.wires, inverse=self.inverse)
