@@ -102,3 +102,21 @@ def test_batch_candidates_and_signature():
     s1 = cb.signature()
     cb.add_layered(9, rng.uniform(size=(3, 9)), rng.uniform(size=(3, 9)))
     assert len(s1) == 13 and cb.signature() != s1
+
+
+def test_choose_fusion_without_room_for_probes(monkeypatch):
+    """If the cost probes cannot allocate their scratch states, the plan is still chosen
+    (fewest passes, tensor cores for multi-gate blocks when allowed)."""
+    import torch
+
+    def oom(*a, **k):
+        raise torch.cuda.OutOfMemoryError("no room")
+
+    monkeypatch.setattr(A, "pass_costs", oom)
+    gates, _ = W.random_circuit(20, 120, seed=1)
+    wl = [g["wires"] for g in gates]
+    plan, flags, k, costs = A.choose_fusion(wl, 20, 4, None, True, True)
+    assert costs["rows"] == 0 and k in (4, 5, 6)
+    assert all(flags[i] for i, (_, idx) in enumerate(plan) if len(idx) > 1)
+    plan, flags, k, costs = A.choose_fusion(wl, 20, 4, None, False, False)
+    assert not any(flags)

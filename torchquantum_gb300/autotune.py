@@ -224,7 +224,14 @@ def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: to
     cheapest of the candidate plans under the measured per-pass costs."""
     from . import fusion
 
-    costs = pass_costs(n, bsz, dev, tc_ok)
+    try:
+        costs = pass_costs(n, bsz, dev, tc_ok)
+    except torch.cuda.OutOfMemoryError:
+        # no room for the probe states: rank plans by pass count with the static kernel
+        # rule (tensor cores for multi-gate blocks when allowed) instead of measured costs
+        torch.cuda.empty_cache()
+        costs = {"dense": {str(k): (1.0 + 0.25 * k, 2.0 + 0.5 * k) for k in range(1, 7)},
+                 "tc": (1.0, 2.0) if tc_ok else None, "rows": 0}
     best = None
     for k in widths:
         k = max(1, min(k, n, 6))

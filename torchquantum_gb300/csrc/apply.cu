@@ -345,28 +345,63 @@ struct XParams {
   uint64_t setmask, tbit;
 };
 
+// Touched-subset kernels (controlled X, swap, phase) move few bytes per unit, so each
+// thread takes kUnits units (block-strided, so every unit index stays coalesced) and
+// issues all its loads before its stores: more bytes in flight per SM.
+constexpr int kUnits = 4;
+
 template <int MODE>
 __global__ void __launch_bounds__(256) k_mcx(const XParams p) {
   const int64_t b = blockIdx.y;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float2* row = p.state + (b << p.n);
-  if (MODE == MODE_VEC) {  // two adjacent groups per thread
-    if (t * 2 >= p.groups) return;
-    const uint64_t i0 = insert_zero_bits((uint64_t)(t * 2), p.ins) | p.setmask;
-    float4 a = ld4(row + i0), c = ld4(row + (i0 | p.tbit));
-    st4(row + i0, c);
-    st4(row + (i0 | p.tbit), a);
+  const int64_t units = MODE == MODE_VEC ? (p.groups + 1) >> 1 : p.groups;
+  int64_t u[kUnits];
+#pragma unroll
+  for (int r = 0; r < kUnits; ++r) u[r] = ((int64_t)blockIdx.x * kUnits + r) * blockDim.x + threadIdx.x;
+  if (MODE == MODE_VEC) {  // two adjacent groups per unit
+    float4 a[kUnits], c[kUnits];
+    uint64_t i0[kUnits];
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      i0[r] = insert_zero_bits((uint64_t)(u[r] * 2), p.ins) | p.setmask;
+      a[r] = ld4(row + i0[r]);
+      c[r] = ld4(row + (i0[r] | p.tbit));
+    }
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      st4(row + i0[r], c[r]);
+      st4(row + (i0[r] | p.tbit), a[r]);
+    }
   } else if (MODE == MODE_LOW) {  // target is bit 0: swap the lanes of one float4
-    if (t >= p.groups) return;
-    const uint64_t i0 = insert_zero_bits((uint64_t)t, p.ins) | p.setmask;
-    float4 a = ld4(row + i0);
-    st4(row + i0, make_float4(a.z, a.w, a.x, a.y));
+    float4 a[kUnits];
+    uint64_t i0[kUnits];
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      i0[r] = insert_zero_bits((uint64_t)u[r], p.ins) | p.setmask;
+      a[r] = ld4(row + i0[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r)
+      if (u[r] < units) st4(row + i0[r], make_float4(a[r].z, a[r].w, a[r].x, a[r].y));
   } else {
-    if (t >= p.groups) return;
-    const uint64_t i0 = insert_zero_bits((uint64_t)t, p.ins) | p.setmask;
-    float2 a = row[i0], c = row[i0 | p.tbit];
-    row[i0] = c;
-    row[i0 | p.tbit] = a;
+    float2 a[kUnits], c[kUnits];
+    uint64_t i0[kUnits];
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      i0[r] = insert_zero_bits((uint64_t)u[r], p.ins) | p.setmask;
+      a[r] = row[i0[r]];
+      c[r] = row[i0[r] | p.tbit];
+    }
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      row[i0[r]] = c[r];
+      row[i0[r] | p.tbit] = a[r];
+    }
   }
 }
 
@@ -416,18 +451,36 @@ struct PhaseParams {
 template <bool VEC>
 __global__ void __launch_bounds__(256) k_phase(const PhaseParams p) {
   const int64_t b = blockIdx.y;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const float2 ph = __ldg(p.phase + b * p.phase_stride);
   float2* row = p.state + (b << p.n);
+  const int64_t units = VEC ? (p.groups + 1) >> 1 : p.groups;
+  int64_t u[kUnits];
+#pragma unroll
+  for (int r = 0; r < kUnits; ++r) u[r] = ((int64_t)blockIdx.x * kUnits + r) * blockDim.x + threadIdx.x;
   if (VEC) {
-    if (t * 2 >= p.groups) return;
-    const uint64_t i0 = insert_zero_bits((uint64_t)(t * 2), p.ins) | p.setmask;
-    float4 a = ld4(row + i0);
-    st4(row + i0, pack4(cmul(ph, lo2(a)), cmul(ph, hi2(a))));
+    float4 a[kUnits];
+    uint64_t i0[kUnits];
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      i0[r] = insert_zero_bits((uint64_t)(u[r] * 2), p.ins) | p.setmask;
+      a[r] = ld4(row + i0[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r)
+      if (u[r] < units) st4(row + i0[r], pack4(cmul(ph, lo2(a[r])), cmul(ph, hi2(a[r]))));
   } else {
-    if (t >= p.groups) return;
-    const uint64_t i0 = insert_zero_bits((uint64_t)t, p.ins) | p.setmask;
-    row[i0] = cmul(ph, row[i0]);
+    float2 a[kUnits];
+    uint64_t i0[kUnits];
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r) {
+      if (u[r] >= units) continue;
+      i0[r] = insert_zero_bits((uint64_t)u[r], p.ins) | p.setmask;
+      a[r] = row[i0[r]];
+    }
+#pragma unroll
+    for (int r = 0; r < kUnits; ++r)
+      if (u[r] < units) row[i0[r]] = cmul(ph, a[r]);
   }
 }
 
@@ -760,8 +813,9 @@ int phase_entry(void* state, void* lam, int64_t bsz, int n, const int32_t* wires
   dim3 grid = grid_for(work, threads, bsz);
   cudaStream_t st = as_stream(stream);
   if (!adjoint) {
-    if (vec) k_phase<true><<<grid, threads, 0, st>>>(p);
-    else k_phase<false><<<grid, threads, 0, st>>>(p);
+    const dim3 gridu = grid_for(work, threads * kUnits, bsz);  // kUnits units per thread
+    if (vec) k_phase<true><<<gridu, threads, 0, st>>>(p);
+    else k_phase<false><<<gridu, threads, 0, st>>>(p);
   } else if (grad) {
     if (vec) k_phase_adj<true, true><<<grid, threads, 0, st>>>(p);
     else k_phase_adj<false, true><<<grid, threads, 0, st>>>(p);
@@ -869,7 +923,7 @@ extern "C" int tqk_apply_mcx(void* state, int64_t bsz, int n, const int32_t* con
   const int mode = bit0_ctrl ? MODE_SCL : (bit0_tgt ? MODE_LOW : MODE_VEC);
   const int64_t work = mode == MODE_VEC ? p.groups / 2 : p.groups;
   const int threads = threads_for(work);
-  dim3 grid = grid_for(work, threads, bsz);
+  dim3 grid = grid_for(work, threads * kUnits, bsz);  // kUnits units per thread
   cudaStream_t st = as_stream(stream);
   if (mode == MODE_VEC) k_mcx<MODE_VEC><<<grid, threads, 0, st>>>(p);
   else if (mode == MODE_LOW) k_mcx<MODE_LOW><<<grid, threads, 0, st>>>(p);
