@@ -3,12 +3,15 @@
 Upstream runs such a batch as a Python loop over circuits, each gate a torch bmm
 (functional/gate_wrapper.py:96-140).  Here a batch is compiled to a compact op list
 (C ABI ``tqk_batch_op``: dense 1-qubit, controlled 1-qubit, CZ, CZ ladder), planned on
-the host into shared-memory tile passes (``tqk_batch_plan``), listed as (circuit, pass,
-tile) work items (``tqk_batch_items``) and executed by one persistent kernel
-(``tqk_batch_run``): circuits with n <= 14 are one item and live entirely in shared
-memory; the tiles of a larger circuit's pass run on many SMs at once and its state is
-streamed once per pass.  Outputs: <Z> on one wire per circuit, each circuit's completion time (for
-latency percentiles) and, on request, the final states.
+the host into shared-memory tile passes (``tqk_batch_plan``, tiles of 2^tile_bits
+amplitudes), listed as (circuit, pass, tile) work items (``tqk_batch_items``) and
+executed by one persistent kernel (``tqk_batch_run``): circuits with n <= tile_bits are
+one item and live entirely in shared memory; the tiles of a larger circuit's pass run on
+many SMs at once and its state is streamed once per pass.  The launch shape (tile size,
+threads, CTAs per SM) is a ``BatchConfig``, picked by ``autotune.tune_batch`` when
+``config="auto"``; ``PreparedBatch`` keeps a compiled batch on the device and replays it
+from a CUDA graph.  Outputs: <Z> on one wire per circuit, each circuit's completion time
+(for latency percentiles) and, on request, the final states.
 """
 from __future__ import annotations
 

@@ -1,14 +1,15 @@
 // batch.cu -- persistent runner for many independent circuits of different sizes.
 //
 // A circuit is a list of passes (tqk_batch_plan); a pass holds ops whose target bits lie
-// in a tile of 2^14 amplitudes (tile_mask), applied tile by tile in shared memory: gather
-// the tile from the circuit's state, apply every op of the pass, scatter it back.
-// Circuits with n <= 14 are one tile and one pass: their whole life is in shared memory.
-// Diagonal ops (CZ, CZ ladders) and controls need no tile bit -- they read the
-// amplitude's global index -- so the planner gives them to any pass.
+// in a tile of 2^tile_bits amplitudes (tile_mask, tile_bits 10..14 per launch), applied
+// tile by tile in shared memory: gather the tile from the circuit's state, apply every op
+// of the pass, scatter it back.  Circuits with n <= tile_bits are one tile and one pass:
+// their whole life is in shared memory.  Diagonal ops (CZ, CZ ladders) and controls need
+// no tile bit -- their signs split into per-tile constants and tile-local terms -- so the
+// planner gives them to any pass.
 //
 // Work is one item per (circuit, pass, tile) (tqk_batch_items), handed out in waves of
-// pass index by a global counter to one persistent CTA per SM, so the tiles of a large
+// pass index by a global counter to persistent CTAs (1..8 per SM), so the tiles of a large
 // circuit's pass run on many SMs at once.  An item of pass p > 0 waits (bounded) for the
 // completion counter of pass p - 1; every item's dependencies are handed out before it,
 // so the earliest unfinished item can always run.  A tile publishes its stores
