@@ -165,3 +165,20 @@ def test_states_reads_are_snapshots():
     tqf.paulix(q, wires=2)
     assert torch.equal(s1.detach(), snap)
     assert not torch.equal(q.states.detach(), snap)
+
+
+def test_phase_encoders_vs_oracle():
+    """PhaseEncoder (upstream encodings.py:133-160) and MultiPhaseEncoder (:163-205)."""
+    import torchquantum_gb300 as tq
+    import torchquantum_gb300.functional as tqf
+
+    n, bsz = 4, 3
+    x = torch.rand(bsz, 12, device="cuda")
+    q = tq.QuantumDevice(n_wires=n, bsz=bsz, device="cuda")
+    tq.PhaseEncoder(tqf.ry)(q, x)
+    tq.MultiPhaseEncoder(["u3", "rz", "u2", "rx"], wires=[0, 1, 2, 3])(q, x[:, 4:])
+    xh = x.cpu().double().numpy()
+    gates = [{"name": "ry", "wires": [k], "params": xh[:, k:k + 1]} for k in range(n)]
+    gates += [{"name": "u3", "wires": [0], "params": xh[:, 4:7]}, {"name": "rz", "wires": [1], "params": xh[:, 7:8]},
+              {"name": "u2", "wires": [2], "params": xh[:, 8:10]}, {"name": "rx", "wires": [3], "params": xh[:, 10:11]}]
+    assert np.abs(q.get_states_1d().cpu().numpy() - O.run(n, bsz, gates)).max() < 1e-5

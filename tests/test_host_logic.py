@@ -46,3 +46,19 @@ def test_structured_ops_are_consistent_with_matrix():
             nc = gd.struct[1] if gd.struct[1] >= 0 else gd.num_wires - 1
             ref = O.gate_matrix(name, None, gd.num_wires)[0]
             assert np.allclose(m[0].numpy(), ref), name
+
+
+def test_upstream_top_level_names():
+    """Names user code reaches through ``import torchquantum as tq`` on this path."""
+    import torchquantum_gb300 as tq
+
+    for name in ["C_DTYPE", "F_DTYPE", "ABC", "ABC_ARRAY", "INV_SQRT2", "QuantumDevice", "NoiseDevice",
+                 "QuantumModule", "QuantumModuleList", "static_support", "op_name_dict", "func_name_dict",
+                 "mat_dict", "gate_wrapper", "apply_unitary_bmm", "rx", "cnot", "u3", "rx_matrix", "u3_matrix",
+                 "GeneralEncoder", "PhaseEncoder", "MultiPhaseEncoder", "StateEncoder", "AmplitudeEncoder",
+                 "Op1QAllLayer", "Op2QAllLayer", "TwoLocal", "EfficientSU2", "RandomLayer", "RandomLayerAllTypes",
+                 "expval_joint_analytical", "expval_joint_sampling", "expval_joint_sampling_grouping",
+                 "find_observable_groups", "expval", "measure", "gen_bitstrings", "MeasureAll",
+                 "MeasureMultipleTimes", "MeasureMultiPauliSum", "MeasureMultiQubitPauliSum"]:
+        assert hasattr(tq, name), name
+    assert tq.RX is not tq.rx and tq.C_DTYPE == __import__("torch").complex64

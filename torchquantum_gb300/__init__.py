@@ -7,6 +7,7 @@ gives ``tq.QuantumDevice``, the ``tqf`` gate functions, the ``tq.Operator`` clas
 sm_103a CUDA kernels (``libtqk.so``, C ABI in ``include/tqk.h``).  CUDA only: the
 engine raises if its library is missing or the device is not a GPU.
 """
+from .macro import *  # noqa: F401,F403
 from . import gates  # noqa: F401
 from . import functional  # noqa: F401
 from .device import QuantumDevice, _bind_gate_methods
@@ -16,7 +17,8 @@ from .operators import op_name_dict, fixed_ops, parameterized_ops, Operator, Ope
     DiagonalOperation  # noqa: F401
 from . import layers as layer  # noqa: F401
 from .layers import *  # noqa: F401,F403
-from .encoding import GeneralEncoder, StateEncoder, Encoder  # noqa: F401
+from .encoding import GeneralEncoder, StateEncoder, Encoder, PhaseEncoder, MultiPhaseEncoder, AmplitudeEncoder, \
+    MagnitudeEncoder  # noqa: F401
 from .measurement import expval_joint_analytical, expval_joint_analytical_batch, expval, MeasureAll, probs  # noqa
 from .measurement import measure, gen_bitstrings, MeasureMultipleTimes, MeasureMultiPauliSum, \
     MeasureMultiQubitPauliSum, find_observable_groups, expval_joint_sampling, \
@@ -25,5 +27,20 @@ from . import measurement  # noqa: F401
 from .density import NoiseDevice  # noqa: F401
 
 _bind_gate_methods()
+
+
+def _export_functional():
+    """Upstream star-imports its functional package at the top level (``tq.rx``,
+    ``tq.cnot``, ``tq.gate_wrapper``, ``tq.func_name_dict``, ...): the same names here,
+    without shadowing the operator classes and modules already exported."""
+    g = globals()
+    names = list(functional.func_name_dict) + list(functional.__all__) + \
+        [n for n in dir(functional) if n.endswith("_matrix")]
+    for name in names:
+        if name not in g:
+            g[name] = getattr(functional, name)
+
+
+_export_functional()
 
 __version__ = "0.1.0"

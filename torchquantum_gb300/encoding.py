@@ -11,7 +11,8 @@ from .functional import func_name_dict
 from .module import QuantumModule, static_support
 from .operators import op_name_dict
 
-__all__ = ["Encoder", "GeneralEncoder", "StateEncoder"]
+__all__ = ["Encoder", "GeneralEncoder", "PhaseEncoder", "MultiPhaseEncoder", "StateEncoder", "AmplitudeEncoder",
+           "MagnitudeEncoder"]
 
 
 class Encoder(QuantumModule):
@@ -46,6 +47,47 @@ def _consecutive(idx) -> bool:
         list(idx) == list(range(idx[0], idx[0] + len(idx)))
 
 
+class PhaseEncoder(Encoder):
+    """``func`` on every wire k with angle ``x[:, k]`` (upstream encodings.py:133-160)."""
+
+    def __init__(self, func):
+        super().__init__()
+        self.func = func
+
+    @static_support
+    def forward(self, qdev, x):
+        for k in range(qdev.n_wires):
+            self.func(qdev, wires=k, params=x[:, k:k + 1])
+
+
+class MultiPhaseEncoder(Encoder):
+    """``funcs[k]`` on ``wires[k]`` with the next 1 / 2 / 3 columns of ``x`` for
+    rx, ry, rz, u1, phaseshift / u2 / u3 (upstream encodings.py:163-205)."""
+
+    _STRIDE = {"rx": 1, "ry": 1, "rz": 1, "u1": 1, "phaseshift": 1, "u2": 2, "u3": 3}
+
+    def __init__(self, funcs, wires=None):
+        super().__init__()
+        self.funcs = list(funcs) if isinstance(funcs, (list, tuple)) else [funcs]
+        self.wires = wires
+
+    @static_support
+    def forward(self, qdev, x):
+        if self.wires is None:
+            self.wires = list(range(qdev.n_wires)) * (len(self.funcs) // qdev.n_wires)
+        col = 0
+        for k, func in enumerate(self.funcs):
+            if func not in self._STRIDE:
+                raise ValueError(func)
+            step = self._STRIDE[func]
+            func_name_dict[func](qdev, wires=self.wires[k], params=x[:, col:col + step])
+            col += step
+
+
+class MagnitudeEncoder(Encoder):
+    """Placeholder class with upstream's name (encodings.py:243-249 defines no forward)."""
+
+
 class StateEncoder(Encoder):
     """Load a (zero-padded, normalised) state from ``x`` (upstream encodings.py StateEncoder)."""
 
@@ -56,3 +98,6 @@ class StateEncoder(Encoder):
         state = torch.cat([x, torch.zeros(x.shape[0], pad, device=x.device, dtype=x.dtype)], dim=-1)
         state = state / state.abs().pow(2).sum(-1, keepdim=True).sqrt()
         qdev.set_states(state.to(torch.complex64))
+
+
+AmplitudeEncoder = StateEncoder

@@ -229,6 +229,9 @@ class _Builder:
 mat_dict = {name: _Builder(name) for name in G.GATES}
 for _a, _t in G.ALIASES.items():
     mat_dict.setdefault(_a, mat_dict[_t])
+# upstream's per-gate builder names (functional/rx.py rx_matrix, u3.py u3_matrix, ...)
+for _n, _b in list(mat_dict.items()):
+    globals().setdefault(f"{_n}_matrix", _b)
 
 
 def _make_gate(name: str):
