@@ -257,30 +257,3 @@ def test_cz_sign_split_matches_global_index():
         want = (glob >> (n - 1 - a)) & (glob >> (n - 1 - c)) & 1
         assert (got == want).all()
 
-
-def test_group_sweep_indexing_covers_tile_once():
-    """Host model of batch.cu's apply_group: for G = 2, 3 ops on distinct tile bits, the
-    sub-cubes over those bits visit every amplitude of the tile exactly once, and sub-cube
-    entry e maps bit k of e to tile bit lbs[k]."""
-    rng = np.random.default_rng(1)
-    for _ in range(40):
-        tb = int(rng.integers(3, 15))
-        G = int(rng.integers(2, 4))
-        if G > tb:
-            continue
-        lbs = [int(b) for b in rng.choice(tb, size=G, replace=False)]
-        srt = sorted(lbs)
-        seen = []
-        for s in range(1 << (tb - G)):
-            base = s
-            for b in srt:
-                base = ((base >> b) << (b + 1)) | (base & ((1 << b) - 1))
-            for b in lbs:
-                assert not (base >> b) & 1
-            for e in range(1 << G):
-                i = base
-                for k in range(G):
-                    i |= ((e >> k) & 1) << lbs[k]
-                assert i < (1 << tb)
-                seen.append(i)
-        assert sorted(seen) == list(range(1 << tb))
