@@ -270,10 +270,12 @@ typedef struct {
                           as the operand), or NULL */
 } tqk_staged_op; /* 72 bytes */
 
+/* status: device int; TQK_TIMEOUT is written there if a tile's bulk load (TMA) did not
+ * complete within ~2 s (the pass then stops early). */
 int tqk_staged_apply(void* state, int64_t bsz, int n, const tqk_staged_op* ops, int nops, int tile_bits,
-                     void* stream);
+                     int* status, void* stream);
 int tqk_staged_adjoint(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op* ops, int nops,
-                       int tile_bits, void* stream);
+                       int tile_bits, int* status, void* stream);
 
 /* ---------------------------------------------------------------- persistent circuit batches
  * Many independent circuits of different sizes (n <= 24) in one launch.  tqk_batch_plan

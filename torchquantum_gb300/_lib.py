@@ -59,8 +59,8 @@ _SIGS = {
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp, _vp]),
     "tqk_sample_scratch_bytes": (_i64, [_i64, _int]),
     "tqk_sample": (_int, [_vp, _i64, _int, _vp, _i64, _vp, _vp, _i64, _vp]),
-    "tqk_staged_apply": (_int, [_vp, _i64, _int, _vp, _int, _int, _vp]),
-    "tqk_staged_adjoint": (_int, [_vp, _vp, _i64, _int, _vp, _int, _int, _vp]),
+    "tqk_staged_apply": (_int, [_vp, _i64, _int, _vp, _int, _int, _vp, _vp]),
+    "tqk_staged_adjoint": (_int, [_vp, _vp, _i64, _int, _vp, _int, _int, _vp, _vp]),
     "tqk_batch_plan": (_int, [_vp, _int, _vp, _int, _vp, _vp, _int, _int]),
     "tqk_batch_items": (_i64, [_vp, _int, _vp, _vp, _i64]),
     "tqk_batch_run": (_int, [_vp, _int, _vp, _vp, _vp, _i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -256,14 +256,15 @@ STAGED_MAX_OPS, STAGED_MAX_TILE_BITS, STAGED_MAX_WIRES = 64, 12, 8
 def staged_apply(state, n, ops, tile_bits):
     """Apply a run of ``StagedOp`` (sequence) in one shared-memory pass."""
     arr = (StagedOp * max(1, len(ops)))(*ops)
-    _check(load().tqk_staged_apply(state.data_ptr(), state.shape[0], n, arr, len(ops), tile_bits, _stream(state)))
+    _check(load().tqk_staged_apply(state.data_ptr(), state.shape[0], n, arr, len(ops), tile_bits,
+                                   status_word(state.device).data_ptr(), _stream(state)))
 
 
 def staged_adjoint(psi, lam, n, ops, tile_bits):
     """Reverse step of a staged run on (psi, lam); ops carry their cotangent slots."""
     arr = (StagedOp * max(1, len(ops)))(*ops)
     _check(load().tqk_staged_adjoint(psi.data_ptr(), lam.data_ptr(), psi.shape[0], n, arr, len(ops), tile_bits,
-                                     _stream(psi)))
+                                     status_word(psi.device).data_ptr(), _stream(psi)))
 
 
 def adjoint_diagonal(psi, lam, n, wires, diag, diag_batch, grad):

@@ -8,6 +8,10 @@
 // the tile back.  Controls and the wires of diagonal ops may be anywhere: they are read
 // from the amplitude's global index (tile base | local index).
 //
+// Tiles are contiguous, so one thread moves each with the bulk-copy engine (TMA:
+// cp.async.bulk into shared memory on an mbarrier, cp.async.bulk back to HBM); the wait
+// for a load is bounded and reports TQK_TIMEOUT through the caller's status word.
+//
 // The adjoint pass holds the psi and lam tiles of the same amplitudes and walks the run
 // in reverse: psi <- U^H psi, lam <- U^H lam and, for ops with a cotangent slot,
 // sum lam_in conj(psi_out) accumulated per op (warp shuffles, then float64 in shared
@@ -21,6 +25,68 @@ namespace staged {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+// ------------------------------------------------------------------ bulk-copy (TMA) tiles
+// A tile is contiguous in HBM (2^tile_bits amplitudes of one row), so one elected thread
+// moves it with the bulk-copy engine: cp.async.bulk global -> shared completing on an
+// mbarrier, and cp.async.bulk shared -> global in a bulk group.  Sizes are multiples of
+// 16 bytes and both addresses 16-byte aligned (tile_bits >= 1, rows of 2^n amplitudes).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+// Bounded wait on phase `parity`; false if it did not complete within kWaitCycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Thread 0: load `nreg` tile regions (bytes each) for use number `use` of the barrier; the
+// previous tile's bulk stores must have finished reading the buffer first.  Returns false
+// (and records TQK_TIMEOUT) if the load did not land in time.
+__device__ __forceinline__ bool load_tile(uint64_t* bar, uint32_t use, int nreg, void* d0, const void* s0,
+                                          void* d1, const void* s1, uint32_t bytes, int* status) {
+  bulk_wait_read();
+  mbar_expect(bar, bytes * nreg);
+  bulk_load(d0, s0, bytes, bar);
+  if (nreg > 1) bulk_load(d1, s1, bytes, bar);
+  if (mbar_wait(bar, use & 1u)) return true;
+  atomicExch(status, TQK_TIMEOUT);
+  return false;
+}
 
 struct SOp {
   int32_t kind;           // TQK_S_*
@@ -43,6 +109,7 @@ struct Params {
   int m;                  // tile bits
   int nops;
   int64_t tiles;          // tiles per row
+  int* status;            // TQK_TIMEOUT if a tile load did not complete
   SOp ops[TQK_STAGED_MAX_OPS];
 };
 
@@ -172,23 +239,36 @@ __device__ __forceinline__ void apply_fwd(const SOp& o, float2* amp, int m, uint
 
 __global__ void __launch_bounds__(kThreads) k_staged(const __grid_constant__ Params p) {
   extern __shared__ float4 sm4[];
+  __shared__ uint64_t full;
+  __shared__ int abort_flag;
   float2* amp = reinterpret_cast<float2*>(sm4);
   const int64_t b = blockIdx.y;
-  const int half = 1 << (p.m - 1);  // float4 per tile
+  const uint32_t bytes = static_cast<uint32_t>(sizeof(float2)) << p.m;
   float2* row = p.psi + (b << p.n);
-  for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x) {
+  if (threadIdx.x == 0) {
+    mbar_init(&full);
+    abort_flag = 0;
+  }
+  __syncthreads();
+  uint32_t use = 0;
+  for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x, ++use) {
     const uint64_t base = (uint64_t)t << p.m;
-    const float4* src = reinterpret_cast<const float4*>(row + base);
-    for (int i = threadIdx.x; i < half; i += kThreads) sm4[i] = src[i];
+    if (threadIdx.x == 0 && !load_tile(&full, use, 1, amp, row + base, nullptr, nullptr, bytes, p.status))
+      abort_flag = 1;
     __syncthreads();
+    if (abort_flag) break;  // uniform
     for (int j = 0; j < p.nops; ++j) {
       apply_fwd(p.ops[j], amp, p.m, base, b);
       __syncthreads();
     }
-    float4* dst = reinterpret_cast<float4*>(row + base);
-    for (int i = threadIdx.x; i < half; i += kThreads) dst[i] = sm4[i];
+    fence_async_smem();  // the ops' shared-memory writes, visible to the bulk store
     __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_store(row + base, amp, bytes);
+      bulk_commit();
+    }
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // Warp-reduce NV float partials and add the block's sum into acc[0..NV) (float64,
@@ -346,35 +426,39 @@ __global__ void __launch_bounds__(kThreads) k_staged_adj(const __grid_constant__
   float2* ls = ps + tsz;
   __shared__ double gacc[TQK_STAGED_MAX_OPS][8];
   __shared__ float red[kWarps][8];
+  __shared__ uint64_t full;
+  __shared__ int abort_flag;
   for (int i = threadIdx.x; i < TQK_STAGED_MAX_OPS * 8; i += kThreads) gacc[i / 8][i % 8] = 0.0;
   const int64_t b = blockIdx.y;
-  const int half = tsz >> 1;
+  const uint32_t bytes = static_cast<uint32_t>(sizeof(float2)) << p.m;
   float2* prow = p.psi + (b << p.n);
   float2* lrow = p.lam + (b << p.n);
-  float4* ps4 = sm4;
-  float4* ls4 = sm4 + half;
+  if (threadIdx.x == 0) {
+    mbar_init(&full);
+    abort_flag = 0;
+  }
   __syncthreads();
-  for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x) {
+  uint32_t use = 0;
+  for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x, ++use) {
     const uint64_t base = (uint64_t)t << p.m;
-    const float4* sp = reinterpret_cast<const float4*>(prow + base);
-    const float4* sl = reinterpret_cast<const float4*>(lrow + base);
-    for (int i = threadIdx.x; i < half; i += kThreads) {
-      ps4[i] = sp[i];
-      ls4[i] = sl[i];
-    }
+    if (threadIdx.x == 0 && !load_tile(&full, use, 2, ps, prow + base, ls, lrow + base, bytes, p.status))
+      abort_flag = 1;
     __syncthreads();
+    if (abort_flag) break;  // uniform
     for (int j = p.nops - 1; j >= 0; --j) {
       apply_adj(p.ops[j], ps, ls, p.m, base, b, red, gacc[j]);
       __syncthreads();
     }
-    float4* dp = reinterpret_cast<float4*>(prow + base);
-    float4* dl = reinterpret_cast<float4*>(lrow + base);
-    for (int i = threadIdx.x; i < half; i += kThreads) {
-      dp[i] = ps4[i];
-      dl[i] = ls4[i];
-    }
+    fence_async_smem();
     __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_store(prow + base, ps, bytes);
+      bulk_store(lrow + base, ls, bytes);
+      bulk_commit();
+    }
   }
+  if (threadIdx.x == 0) bulk_wait_all();
+  __syncthreads();
   // flush: one atomic per value per op with a cotangent slot
   for (int i = threadIdx.x; i < p.nops * 8; i += kThreads) {
     const SOp& o = p.ops[i / 8];
@@ -460,15 +544,17 @@ int fill_staged(staged::Params& p, int64_t bsz, int n, const tqk_staged_op* ops,
 }
 
 int launch_staged(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op* ops, int nops, int tile_bits,
-                  bool adjoint, void* stream, const char* what) {
+                  int* status, bool adjoint, void* stream, const char* what) {
   int rc = check_state(psi, bsz, n, what);
   if (rc) return rc;
   if (adjoint && (rc = check_state(lam, bsz, n, what))) return rc;
   staged::Params p;
   if ((rc = fill_staged(p, bsz, n, ops, nops, tile_bits, adjoint, what))) return rc;
   if (nops == 0) return TQK_OK;
+  if (status == nullptr) return fail(TQK_BAD_POINTER, "%s: null status word", what);
   p.psi = static_cast<float2*>(psi);
   p.lam = static_cast<float2*>(lam);
+  p.status = status;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -499,11 +585,11 @@ int launch_staged(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op*
 }  // namespace
 
 extern "C" int tqk_staged_apply(void* state, int64_t bsz, int n, const tqk_staged_op* ops, int nops, int tile_bits,
-                                void* stream) {
-  return launch_staged(state, nullptr, bsz, n, ops, nops, tile_bits, false, stream, "tqk_staged_apply");
+                                int* status, void* stream) {
+  return launch_staged(state, nullptr, bsz, n, ops, nops, tile_bits, status, false, stream, "tqk_staged_apply");
 }
 
 extern "C" int tqk_staged_adjoint(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op* ops, int nops,
-                                  int tile_bits, void* stream) {
-  return launch_staged(psi, lam, bsz, n, ops, nops, tile_bits, true, stream, "tqk_staged_adjoint");
+                                  int tile_bits, int* status, void* stream) {
+  return launch_staged(psi, lam, bsz, n, ops, nops, tile_bits, status, true, stream, "tqk_staged_adjoint");
 }
