@@ -205,6 +205,22 @@ __device__ __forceinline__ uint64_t insert6(uint64_t g, const BitInsert& bi) {
   return g;
 }
 
+// U image (2 x 32 KB, contiguous and 1024-byte aligned in shared memory, 16-byte aligned
+// in global memory) moved by the bulk-copy engine, completing on `bar`.
+__device__ __forceinline__ void load_u_image(uint64_t* bar, uint8_t* dst, const uint8_t* src) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(2 * kBImgBytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(2 * kBImgBytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait of a whole warp on the U image; warp-uniform result.
+__device__ __forceinline__ bool wait_u_image(uint64_t* bar, uint32_t parity) {
+  return __all_sync(0xffffffffu, mbar_wait(bar, parity));
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -258,6 +274,7 @@ constexpr int kABufs = 2;
 
 struct Sync {
   uint64_t a_full[kABufs], a_empty[kABufs], d_full[2], d_empty[2], x_full, x_empty;
+  uint64_t u_full;        // bulk-copy (TMA) load of the U image, one use per batch row
   int nat_of_k[128];      // natural row/column of cross-term index 64p + jk
   uint32_t tmem_base;
   int abort;
@@ -414,12 +431,15 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
                  "r"(ncols_tmem)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    // U (or U^H) image of the first row
-    const uint4* src =
-        reinterpret_cast<const uint4*>(p.uimg + (p.u_batch > 1 ? (t_begin >> p.tpr_log2) : 0) * 2 * kBImgBytes);
-    uint4* dstb = reinterpret_cast<uint4*>(bimg);
-    for (int i = lane; i < 2 * kBImgBytes / 16; i += 32) dstb[i] = src[i];
-    fence_proxy_async();
+    // U (or U^H) image of the first row: one bulk-copy (TMA) load of 64 KB on u_full,
+    // initialised here by the warp that uses it
+    if (lane == 0) {
+      mbar_init(&sy->u_full, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      load_u_image(&sy->u_full, bimg, p.uimg + (p.u_batch > 1 ? (t_begin >> p.tpr_log2) : 0) * 2 * kBImgBytes);
+    }
+    __syncwarp();
+    if (!wait_u_image(&sy->u_full, 0u) && lane == 0) atomicExch(&sy->abort, 1);
     tc_fence_before();
   }
   __syncthreads();
@@ -473,6 +493,7 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
     }
   } else {
     // ------------------------------------------------------------ MMA issuer
+    uint32_t u_use = 1;  // uses of u_full so far (the first row's image is use 0)
     int64_t cur_b = t_begin >> p.tpr_log2;
     bool first_cross = true;
     uint32_t xphase = 0;
@@ -490,11 +511,10 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
         }
         if (p.u_batch > 1) {  // reload U once every MMA of the previous row has completed
           if (!wait_or_abort(&sy->d_full[(k - 1) & 1], static_cast<uint32_t>(((k - 1) >> 1) & 1), sy)) break;
-          const uint4* src = reinterpret_cast<const uint4*>(p.uimg + b * 2 * kBImgBytes);
-          uint4* dstb = reinterpret_cast<uint4*>(bimg);
-          for (int i = lane; i < 2 * kBImgBytes / 16; i += 32) dstb[i] = src[i];
-          fence_proxy_async();
+          if (lane == 0) load_u_image(&sy->u_full, bimg, p.uimg + b * 2 * kBImgBytes);
           __syncwarp();
+          if (!wait_or_abort(&sy->u_full, u_use & 1u, sy)) break;
+          ++u_use;
         }
         cur_b = b;
       }
