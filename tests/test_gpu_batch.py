@@ -136,3 +136,46 @@ def test_graph_replay_autotuned_and_new_angles(tmp_path, monkeypatch):
         assert abs(z - _z(_layered_ref(n, ry, rz), n, 0)) < 2e-5
     assert r3.kernel_ms > 0 and (r3.latency_ms > 0).all()
     A.clear()
+
+
+def test_bounded_wait_reports_timeout():
+    """Failure detection without a GPU fault: a work list missing every tile of a
+    circuit's first pass leaves the second pass's tiles waiting on a counter that nothing
+    raises; their bounded waits (~2 s) give up, the kernel finishes, and the host reads
+    TQK_TIMEOUT from the status word."""
+    import torch
+
+    from torchquantum_gb300 import _lib
+    from torchquantum_gb300 import batch as B
+
+    n = 16
+    rng = np.random.default_rng(3)
+    cb = B.CircuitBatch()
+    cb.add_layered(n, rng.uniform(-np.pi, np.pi, (2, n)), rng.uniform(-np.pi, np.pi, (2, n)))
+    circ, ops, passes, items, mats, order, state_amps = cb.compile(tile_bits=14)
+    assert circ[0]["num_passes"] >= 2
+    first = int(circ[0]["first_pass"])
+    kept = items[items["pass"] != first]  # pass 1 waits for tiles that are never run
+    dev = torch.device("cuda")
+
+    def up(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).to(dev)
+
+    d_circ, d_ops, d_pass, d_items, d_mats = up(circ), up(ops), up(passes), up(kept), up(mats)
+    states = torch.zeros(max(1, state_amps), dtype=torch.complex64, device=dev)
+    z = torch.zeros(1, dtype=torch.float64, device=dev)
+    pass_done = torch.zeros(len(passes), dtype=torch.int32, device=dev)
+    counter = torch.zeros(1, dtype=torch.int32, device=dev)
+    status = _lib.status_word(dev)
+    status.zero_()
+    cfg = B.DEFAULT_CONFIG.as_struct()
+    rc = _lib.load().tqk_batch_run(d_circ.data_ptr(), 1, d_ops.data_ptr(), d_pass.data_ptr(), d_items.data_ptr(),
+                                   len(kept), d_mats.data_ptr(), states.data_ptr(), 0, z.data_ptr(),
+                                   pass_done.data_ptr(), None, counter.data_ptr(), status.data_ptr(),
+                                   cfg.ctypes.data, torch.cuda.current_stream().cuda_stream)
+    assert rc == 0
+    with pytest.raises(_lib.TQKError, match="TIMEOUT|bounded wait"):
+        _lib.check_status(dev)
+    assert int(status.item()) == 0  # check_status clears the word; the context stays usable
+    res = cb.run(config=B.DEFAULT_CONFIG)
+    assert np.isfinite(res.z).all()
