@@ -86,3 +86,34 @@ def test_two_ranks_gloo(tmp_path):
     assert infos[0]["rate"] == pytest.approx(5 * 2 / 2.0)
     sharded = np.concatenate([np.load(tmp_path / f"rows{r}.npy") for r in range(world)])
     np.testing.assert_allclose(sharded, _rows(0, total, n), atol=1e-12)
+
+
+def _leaving_worker(rank, world, port, out_dir):
+    import time
+
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    R.init("gloo", timeout_s=20)
+    R.barrier()  # both ranks arrive here
+    if rank == 1:
+        os._exit(0)  # leaves between steps, before the next barrier, with nothing in flight
+    t0 = time.time()
+    err = None
+    try:
+        R.max_over_ranks(1.0)
+    except Exception as e:  # noqa: BLE001 - any error type from the backend is the signal
+        err = type(e).__name__
+    with open(os.path.join(out_dir, "rank0.json"), "w") as f:
+        json.dump({"error": err, "seconds": time.time() - t0}, f)
+
+
+def test_rank_leaving_surfaces_as_error(tmp_path):
+    """Failure detection on the host: a rank that leaves between steps makes the other
+    rank's next collective raise (within the process-group timeout) instead of hanging."""
+    world = 2
+    ctx = mp.start_processes(_leaving_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=False,
+                             start_method="spawn")
+    while not ctx.join(timeout=60):
+        pass
+    info = json.load(open(tmp_path / "rank0.json"))
+    assert info["error"] is not None and info["seconds"] < 30

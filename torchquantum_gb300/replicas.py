@@ -26,15 +26,20 @@ def rank_env() -> Tuple[int, int, int]:
     return rank, world, local
 
 
-def init(backend: str) -> bool:
-    """Join the process group when more than one rank runs; returns True if it did."""
+def init(backend: str, timeout_s: Optional[float] = None) -> bool:
+    """Join the process group when more than one rank runs; returns True if it did.
+    ``timeout_s`` bounds every collective (a rank that leaves or never arrives then
+    surfaces as an error on the others instead of a hang)."""
     _, world, _ = rank_env()
     if world == 1:
         return False
+    import datetime
+
     import torch.distributed as dist
 
     if not dist.is_initialized():
-        dist.init_process_group(backend)
+        kw = {"timeout": datetime.timedelta(seconds=timeout_s)} if timeout_s else {}
+        dist.init_process_group(backend, **kw)
     return True
 
 
