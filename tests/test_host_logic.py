@@ -62,3 +62,20 @@ def test_upstream_top_level_names():
                  "MeasureMultipleTimes", "MeasureMultiPauliSum", "MeasureMultiQubitPauliSum"]:
         assert hasattr(tq, name), name
     assert tq.RX is not tq.rx and tq.C_DTYPE == __import__("torch").complex64
+
+
+def test_engine_defaults_roundtrip():
+    import pytest
+
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import device as D
+
+    prev = tq.set_engine_defaults(method="fused", fuse_wires=5, fused_backend="tc", stage_low=False)
+    try:
+        assert D.ENGINE_DEFAULTS == {"method": "fused", "fuse_wires": 5, "fused_backend": "tc", "stage_low": False}
+        for bad in ({"method": "x"}, {"fuse_wires": 7}, {"fused_backend": "gpu"}):
+            with pytest.raises(ValueError):
+                tq.set_engine_defaults(**bad)
+    finally:
+        tq.set_engine_defaults(**prev)
+    assert D.ENGINE_DEFAULTS == prev

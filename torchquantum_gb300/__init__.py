@@ -10,7 +10,7 @@ engine raises if its library is missing or the device is not a GPU.
 from .macro import *  # noqa: F401,F403
 from . import gates  # noqa: F401
 from . import functional  # noqa: F401
-from .device import QuantumDevice, _bind_gate_methods
+from .device import QuantumDevice, set_engine_defaults, _bind_gate_methods
 from .module import QuantumModule, QuantumModuleList, QuantumModuleDict, static_support
 from .operators import *  # noqa: F401,F403
 from .operators import op_name_dict, fixed_ops, parameterized_ops, Operator, Operation, Observable, \

@@ -80,6 +80,19 @@ _lib: Optional[ctypes.CDLL] = None
 # Kernels launched by this process through the C ABI (bench.py reports the count of
 # its timed region).
 LAUNCHES = [0]
+# NVTX ranges around segment compilation, forward and backward sweeps, batch launches
+# and autotuning probes (for nsys / ncu --nvtx); off unless TQ_GB300_NVTX=1.
+NVTX = os.environ.get("TQ_GB300_NVTX") == "1"
+
+
+def nvtx_push(name: str) -> None:
+    if NVTX:
+        torch.cuda.nvtx.range_push(name)
+
+
+def nvtx_pop() -> None:
+    if NVTX:
+        torch.cuda.nvtx.range_pop()
 
 
 def _count(k: int = 1) -> None:

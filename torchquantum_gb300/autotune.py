@@ -161,6 +161,14 @@ def pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool) -> dict:
     hit = lookup(key)
     if hit is not None:
         return hit
+    _lib.nvtx_push(f"tqk.autotune.pass_costs[n={n},bsz={bsz}]")
+    try:
+        return _pass_costs(n, bsz, dev, tc_ok, key)
+    finally:
+        _lib.nvtx_pop()
+
+
+def _pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool, key: str) -> dict:
     rows = max(1, min(bsz, SCRATCH_AMPS >> n))
     scale = bsz / rows
     psi = torch.zeros(rows, 1 << n, dtype=torch.complex64, device=dev)

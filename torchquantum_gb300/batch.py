@@ -299,12 +299,14 @@ class PreparedBatch:
     def launch(self) -> None:
         """Zero the counters and launch the persistent kernel (device-timed)."""
         stream = torch.cuda.current_stream(self.device)
+        _lib.nvtx_push(f"tqk.batch.launch[{self.ncirc} circuits]")
         self._ev[0].record(stream)
         if self.graph is not None:
             self.graph.replay()
         else:
             self._enqueue(stream)
         self._ev[1].record(stream)
+        _lib.nvtx_pop()
 
     def capture(self) -> "PreparedBatch":
         """Record the counter resets and the kernel launch into a CUDA graph; later

@@ -26,6 +26,33 @@ from . import engine
 __all__ = ["QuantumDevice"]
 
 
+# Engine settings every new QuantumDevice starts with (``set_engine_defaults``).
+ENGINE_DEFAULTS = {"method": "plain", "fuse_wires": "auto", "fused_backend": "auto", "stage_low": True}
+
+
+def set_engine_defaults(method: Optional[str] = None, fuse_wires=None, fused_backend: Optional[str] = None,
+                        stage_low: Optional[bool] = None) -> dict:
+    """Set the engine settings of QuantumDevices created from now on -- e.g. the fused
+    method for models that build their devices inside ``forward`` -- and return the
+    previous defaults (pass them back as keyword arguments to restore them)."""
+    prev = dict(ENGINE_DEFAULTS)
+    if method is not None:
+        if method not in ("plain", "fused"):
+            raise ValueError(f"method must be 'plain' or 'fused' (got {method!r})")
+        ENGINE_DEFAULTS["method"] = method
+    if fuse_wires is not None:
+        if fuse_wires != "auto" and not (isinstance(fuse_wires, int) and 1 <= fuse_wires <= 6):
+            raise ValueError(f"fuse_wires must be 1..6 or 'auto' (got {fuse_wires!r})")
+        ENGINE_DEFAULTS["fuse_wires"] = fuse_wires
+    if fused_backend is not None:
+        if fused_backend not in ("auto", "tc", "cuda"):
+            raise ValueError(f"fused_backend must be 'auto', 'tc' or 'cuda' (got {fused_backend!r})")
+        ENGINE_DEFAULTS["fused_backend"] = fused_backend
+    if stage_low is not None:
+        ENGINE_DEFAULTS["stage_low"] = bool(stage_low)
+    return prev
+
+
 class QuantumDevice(nn.Module):
     def __init__(self, n_wires: int, device_name: str = "default", bsz: int = 1,
                  device: Union[torch.device, str] = "cuda", record_op: bool = False):
@@ -42,10 +69,11 @@ class QuantumDevice(nn.Module):
         self.device = dev
         self.record_op = record_op
         self.op_history: List[dict] = []
-        self.method = "plain"          # "plain" | "fused" (see fusion.py)
-        self.fuse_wires = "auto"       # fused block width 1..6, or "auto" (autotune.choose_fusion)
-        self.fused_backend = "auto"    # "auto" | "tc" (tensor cores) | "cuda" (CUDA cores)
-        self.stage_low = True          # plain method: runs of low-qubit gates share one pass (program.stage_runs)
+        d = ENGINE_DEFAULTS
+        self.method = d["method"]                # "plain" | "fused" (see fusion.py)
+        self.fuse_wires = d["fuse_wires"]        # fused block width 1..6, or "auto" (autotune.choose_fusion)
+        self.fused_backend = d["fused_backend"]  # "auto" | "tc" (tensor cores) | "cuda" (CUDA cores)
+        self.stage_low = d["stage_low"]          # plain method: runs of low-qubit gates share one pass
         self._tape: List[engine.TapeOp] = []
         self._pending: List[engine.TapeOp] = []   # fused method: recorded, not yet applied
         self._init: Optional[torch.Tensor] = None

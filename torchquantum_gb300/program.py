@@ -292,6 +292,11 @@ class Segment:
 
     # -------------------------------------------------------------- forward
     def apply(self, buf: torch.Tensor) -> None:
+        _lib.nvtx_push(f"tqk.segment.forward[{len(self.exec_ops)} passes]")
+        self._apply(buf)
+        _lib.nvtx_pop()
+
+    def _apply(self, buf: torch.Tensor) -> None:
         for op in self.exec_ops:
             if isinstance(op, StagedRun):
                 _lib.staged_apply(buf, self.n, op.descs(), op.tile_bits)
@@ -306,6 +311,13 @@ class Segment:
     # -------------------------------------------------------------- backward
     def backward(self, psi: torch.Tensor, lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
         """Reverse sweep over this segment; returns grads for ``self.diff_inputs``."""
+        _lib.nvtx_push(f"tqk.segment.backward[{len(self.exec_ops)} passes]")
+        try:
+            return self._backward(psi, lam, need_grads)
+        finally:
+            _lib.nvtx_pop()
+
+    def _backward(self, psi: torch.Tensor, lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
         dev = self.device
         n = self.n
         opg = torch.zeros_like(self.op128) if (need_grads and self.natives) else None
