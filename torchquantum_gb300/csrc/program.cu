@@ -20,13 +20,33 @@
 namespace tqk {
 namespace prog {
 
-struct C2 {
-  double x, y;
+// Complex scalars: float64 (C2) for operands and block unitaries; float32 (F2) for the
+// block unbuild sweeps, whose input cotangent carries complex64 accuracy (partial sums
+// go to float64 before any atomic).
+template <typename R>
+struct CT {
+  R x, y;
+  using real = R;
 };
+using C2 = CT<double>;
+using F2 = CT<float>;
 __device__ __forceinline__ C2 mk(double a, double b) { return C2{a, b}; }
-__device__ __forceinline__ C2 cmul2(C2 a, C2 b) { return C2{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
-__device__ __forceinline__ C2 conj2(C2 a) { return C2{a.x, -a.y}; }
-__device__ __forceinline__ C2 cadd2(C2 a, C2 b) { return C2{a.x + b.x, a.y + b.y}; }
+template <typename C>
+__device__ __forceinline__ C mkc(double a, double b) {
+  return C{static_cast<typename C::real>(a), static_cast<typename C::real>(b)};
+}
+template <typename C>
+__device__ __forceinline__ C cmul2(C a, C b) {
+  return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename C>
+__device__ __forceinline__ C conj2(C a) {
+  return C{a.x, -a.y};
+}
+template <typename C>
+__device__ __forceinline__ C cadd2(C a, C b) {
+  return C{a.x + b.x, a.y + b.y};
+}
 __device__ __forceinline__ C2 expi(double t) {
   double s, c;
   sincos(t, &s, &c);
@@ -276,7 +296,8 @@ __global__ void k_param_grads(const tqk_gate_desc* gates, int ngates) {
 // ------------------------------------------------------------------ block build / unbuild
 // Rows of a 2^k x 2^k complex128 matrix in shared memory (row-major, ld = D); block wire
 // i <-> row bit (k-1-i).  apply_op_rows applies op (or its adjoint) to every column.
-__device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double2* opnd, bool adjoint) {
+template <typename C>
+__device__ void apply_op_rows(C* U, int D, const tqk_block_op& op, const double2* opnd, bool adjoint) {
   const int nw = op.nw;
   const int kind = op.kind;
   const int nc = op.nctrl;
@@ -286,7 +307,7 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
   const uint32_t allmask = cmask | tmask;
   const int tid = threadIdx.x, nth = blockDim.x;
   if (kind == TQK_K_PHASE) {
-    C2 ph = mk(opnd[0].x, opnd[0].y);
+    C ph = mkc<C>(opnd[0].x, opnd[0].y);
     if (adjoint) ph = conj2(ph);
     for (int e = tid; e < D * D; e += nth) {
       const int r = e / D;
@@ -297,7 +318,7 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
       const int r = e / D;
       int di = 0;
       for (int j = 0; j < nw; ++j) di = (di << 1) | ((r >> op.pos[j]) & 1);
-      C2 dv = mk(opnd[di].x, opnd[di].y);
+      C dv = mkc<C>(opnd[di].x, opnd[di].y);
       if (adjoint) dv = conj2(dv);
       U[e] = cmul2(dv, U[e]);
     }
@@ -308,7 +329,7 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
       const int r = e / D, c = e % D;
       if ((static_cast<uint32_t>(r) & tb) == 0 && (static_cast<uint32_t>(r) & cmask) == want) {
         const int r2 = r | tb;
-        const C2 a = U[r * D + c], b2 = U[r2 * D + c];
+        const C a = U[r * D + c], b2 = U[r2 * D + c];
         U[r * D + c] = b2;
         U[r2 * D + c] = a;
       }
@@ -319,7 +340,7 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
       const int r = e / D, c = e % D;
       if ((static_cast<uint32_t>(r) & cmask) == cmask && (r & b0) && !(r & b1)) {
         const int r2 = (r & ~b0) | b1;
-        const C2 a = U[r * D + c], b2 = U[r2 * D + c];
+        const C a = U[r * D + c], b2 = U[r2 * D + c];
         U[r * D + c] = b2;
         U[r2 * D + c] = a;
       }
@@ -327,11 +348,11 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
   } else {  // dense (all wires targets) or controlled block on the last nw-nc wires
     const int kt = nw - nc;
     const int dt = 1 << kt;
-    C2 M[16];
+    C M[16];
     for (int a = 0; a < dt; ++a)
       for (int b = 0; b < dt; ++b) {
         const double2 v = adjoint ? opnd[b * dt + a] : opnd[a * dt + b];
-        M[a * dt + b] = adjoint ? conj2(mk(v.x, v.y)) : mk(v.x, v.y);
+        M[a * dt + b] = adjoint ? conj2(mkc<C>(v.x, v.y)) : mkc<C>(v.x, v.y);
       }
     // work item = (column, group of rows sharing all op bits = 0)
     const int groups = D >> nw;
@@ -344,7 +365,7 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
       }
       base |= cmask;
       int rows[4];
-      C2 x[4], y[4];
+      C x[4], y[4];
       for (int a = 0; a < dt; ++a) {
         uint32_t r = base;
         for (int j = 0; j < kt; ++j)
@@ -353,7 +374,7 @@ __device__ void apply_op_rows(C2* U, int D, const tqk_block_op& op, const double
         x[a] = U[r * D + c];
       }
       for (int a = 0; a < dt; ++a) {
-        C2 acc = mk(0, 0);
+        C acc = mkc<C>(0, 0);
         for (int b = 0; b < dt; ++b) acc = cadd2(acc, cmul2(M[a * dt + b], x[b]));
         y[a] = acc;
       }
@@ -384,7 +405,8 @@ __global__ void k_block_build(const tqk_block_desc* blocks, const tqk_block_op* 
 // grad of op (operand cotangent) = sum over rows/cols of X[row][col] conj(W[row'][col]) restricted
 // to the op's structure; W = product of the ops before it, X = (ops after)^H dL/dU.
 // One sweep per entry: ops outside the specialised shapes below.
-__device__ void op_cotangent_generic(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+template <typename C>
+__device__ void op_cotangent_generic(const C* X, const C* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
   const int nw = op.nw, nc = op.nctrl;
   uint32_t cmask = 0, tmask = 0;
   for (int j = 0; j < nc; ++j) cmask |= 1u << op.pos[j];
@@ -421,7 +443,7 @@ __device__ void op_cotangent_generic(const C2* X, const C2* W, int D, const tqk_
         }
       }
       if (rr >= 0) {
-        const C2 xv = X[r * D + c], wv = W[rr * D + c];
+        const C xv = X[r * D + c], wv = W[rr * D + c];
         ax += xv.x * wv.x + xv.y * wv.y;  // x * conj(w)
         ay += xv.y * wv.x - xv.x * wv.y;
       }
@@ -480,8 +502,9 @@ __device__ void block_reduce_entries(double (&acc)[2 * NE], double2* gout, int n
 // columns c, of X[r][c] conj(W[r with target pattern b][c]) (diagonal ops: a = b over
 // all op bits; phase ops: the single all-ones pattern).  One sweep over (row with the op's
 // bits cleared, column) pairs evaluates every entry.
-template <int KT>
-__device__ void cot_dense(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+template <int KT, typename C>
+__device__ void cot_dense(const C* X, const C* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+  using R = typename C::real;
   constexpr int DT = 1 << KT, NE = DT * DT;
   const int nc = op.nctrl;
   uint32_t cmask = 0;
@@ -505,15 +528,15 @@ __device__ void cot_dense(const C2* X, const C2* W, int D, const tqk_block_op& o
       if ((a >> (KT - 1 - j)) & 1) r |= 1 << tbit[j];
     pat[a] = r;
   }
-  double acc[2 * NE];
+  R acc[2 * NE];
 #pragma unroll
-  for (int q = 0; q < 2 * NE; ++q) acc[q] = 0.0;
+  for (int q = 0; q < 2 * NE; ++q) acc[q] = R(0);
   const int nbase = D >> KT;
   for (int w = threadIdx.x; w < nbase * D; w += blockDim.x) {
     const int c = w % D;
     const int r = insert_zeros(w / D, tsorted, KT);
     if ((static_cast<uint32_t>(r) & cmask) != cmask) continue;
-    C2 xs[DT], ws[DT];
+    C xs[DT], ws[DT];
 #pragma unroll
     for (int a = 0; a < DT; ++a) {
       xs[a] = X[(r | pat[a]) * D + c];
@@ -527,13 +550,17 @@ __device__ void cot_dense(const C2* X, const C2* W, int D, const tqk_block_op& o
         acc[2 * (a * DT + b2) + 1] += xs[a].y * ws[b2].x - xs[a].x * ws[b2].y;
       }
   }
-  block_reduce_entries<NE>(acc, gout, NE, accumulate);
+  double accd[2 * NE];
+#pragma unroll
+  for (int q = 0; q < 2 * NE; ++q) accd[q] = static_cast<double>(acc[q]);
+  block_reduce_entries<NE>(accd, gout, NE, accumulate);
 }
 
 // Diagonal ops (entries = pattern over all NW op bits) and phase ops (one entry: all bits set).
-template <int NW>
-__device__ void cot_diag(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate,
+template <int NW, typename C>
+__device__ void cot_diag(const C* X, const C* W, int D, const tqk_block_op& op, double2* gout, bool accumulate,
                          bool phase) {
+  using R = typename C::real;
   constexpr int DT = 1 << NW;
   int bit[NW], srt[NW];
 #pragma unroll
@@ -552,9 +579,9 @@ __device__ void cot_diag(const C2* X, const C2* W, int D, const tqk_block_op& op
       if ((a >> (NW - 1 - j)) & 1) r |= 1 << bit[j];
     pat[a] = r;
   }
-  double acc[2 * DT];
+  R acc[2 * DT];
 #pragma unroll
-  for (int q = 0; q < 2 * DT; ++q) acc[q] = 0.0;
+  for (int q = 0; q < 2 * DT; ++q) acc[q] = R(0);
   const int nbase = D >> NW;
   for (int w = threadIdx.x; w < nbase * D; w += blockDim.x) {
     const int c = w % D;
@@ -562,7 +589,7 @@ __device__ void cot_diag(const C2* X, const C2* W, int D, const tqk_block_op& op
 #pragma unroll
     for (int a = 0; a < DT; ++a) {
       if (phase && a != DT - 1) continue;
-      const C2 xv = X[(r | pat[a]) * D + c], wv = W[(r | pat[a]) * D + c];
+      const C xv = X[(r | pat[a]) * D + c], wv = W[(r | pat[a]) * D + c];
       acc[2 * a] += xv.x * wv.x + xv.y * wv.y;
       acc[2 * a + 1] += xv.y * wv.x - xv.x * wv.y;
     }
@@ -571,24 +598,28 @@ __device__ void cot_diag(const C2* X, const C2* W, int D, const tqk_block_op& op
     acc[0] = acc[2 * (DT - 1)];
     acc[1] = acc[2 * (DT - 1) + 1];
   }
-  block_reduce_entries<DT>(acc, gout, phase ? 1 : DT, accumulate);
+  double accd[2 * DT];
+#pragma unroll
+  for (int q = 0; q < 2 * DT; ++q) accd[q] = static_cast<double>(acc[q]);
+  block_reduce_entries<DT>(accd, gout, phase ? 1 : DT, accumulate);
 }
 
-__device__ void op_cotangent(const C2* X, const C2* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
+template <typename C>
+__device__ void op_cotangent(const C* X, const C* W, int D, const tqk_block_op& op, double2* gout, bool accumulate) {
   const int kt = op.nw - op.nctrl;
   const bool diag = op.kind == TQK_K_PHASE || op.kind == TQK_K_DIAG;
   if ((diag && (op.nw < 1 || op.nw > 4)) || (!diag && (kt < 1 || kt > 2))) {
     op_cotangent_generic(X, W, D, op, gout, accumulate);
   } else if (diag) {
     const bool phase = op.kind == TQK_K_PHASE;
-    if (op.nw == 1) cot_diag<1>(X, W, D, op, gout, accumulate, phase);
-    else if (op.nw == 2) cot_diag<2>(X, W, D, op, gout, accumulate, phase);
-    else if (op.nw == 3) cot_diag<3>(X, W, D, op, gout, accumulate, phase);
-    else cot_diag<4>(X, W, D, op, gout, accumulate, phase);
+    if (op.nw == 1) cot_diag<1, C>(X, W, D, op, gout, accumulate, phase);
+    else if (op.nw == 2) cot_diag<2, C>(X, W, D, op, gout, accumulate, phase);
+    else if (op.nw == 3) cot_diag<3, C>(X, W, D, op, gout, accumulate, phase);
+    else cot_diag<4, C>(X, W, D, op, gout, accumulate, phase);
   } else if (kt == 1) {
-    cot_dense<1>(X, W, D, op, gout, accumulate);
+    cot_dense<1, C>(X, W, D, op, gout, accumulate);
   } else {
-    cot_dense<2>(X, W, D, op, gout, accumulate);
+    cot_dense<2, C>(X, W, D, op, gout, accumulate);
   }
 }
 
@@ -598,13 +629,13 @@ __global__ void k_block_unbuild(const tqk_block_desc* blocks, const tqk_block_op
   const int64_t b = blockIdx.y;
   if (b >= bl.batch || bl.gu == nullptr) return;
   const int D = 1 << bl.k;
-  C2* W = reinterpret_cast<C2*>(smem_u);
-  C2* X = W + D * D;
+  F2* W = reinterpret_cast<F2*>(smem_u);
+  F2* X = W + D * D;
   const double2* us = static_cast<const double2*>(bl.u) + b * D * D;
   const double2* gs = static_cast<const double2*>(bl.gu) + b * D * D;
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-    W[e] = mk(us[e].x, us[e].y);
-    X[e] = mk(gs[e].x, gs[e].y);
+    W[e] = mkc<F2>(us[e].x, us[e].y);
+    X[e] = mkc<F2>(gs[e].x, gs[e].y);
   }
   __syncthreads();
   for (int i = bl.num_ops - 1; i >= 0; --i) {
@@ -669,6 +700,6 @@ extern "C" int tqk_block_unbuild(const tqk_block_desc* blocks, int nblocks, int 
   if (max_batch < 1 || max_batch > 65535) return fail(TQK_BAD_SHAPE, "tqk_block_unbuild: batch %d", max_batch);
   set_block_smem_attrs();
   dim3 grid(nblocks, max_batch, 1);
-  prog::k_block_unbuild<<<grid, 256, 2 * 64 * 64 * sizeof(double2), as_stream(stream)>>>(blocks, ops);
+  prog::k_block_unbuild<<<grid, 256, 2 * 64 * 64 * sizeof(float2), as_stream(stream)>>>(blocks, ops);
   return launch_status("tqk_block_unbuild");
 }
