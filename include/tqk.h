@@ -163,6 +163,13 @@ int tqk_adjoint_diagonal(void* psi, void* lam, int64_t bsz, int n, const int32_t
  * TQK_TIMEOUT there if one of its bounded waits gives up (it then stops early). */
 int64_t tqk_fused_image_bytes(int64_t u_batch);
 int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream);
+/* The image of U^H, built directly from U (what tqk_fused_prepare of U^H would give). */
+int tqk_fused_prepare_adjoint(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream);
+/* Block cotangent from an adjoint step: gu[b] += M_b U_b (complex128 [batch, 64, 64]),
+ * where M_b is the complex 64 x 64 matrix held by the real cross term mr[b]
+ * ([batch, 128, 128] float64 from tqk_fused_adjoint) and U_b the block unitary
+ * (complex128 [batch, 64, 64]); the product runs in float32, the sum in float64. */
+int tqk_fused_cross_grad(const double* mr, const void* u, int64_t batch, void* gu, void* stream);
 int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
                     int64_t u_batch, int* status, void* stream);
 

@@ -256,3 +256,26 @@ def test_autotuned_fusion_vs_oracle(tmp_path, monkeypatch):
     assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-4
     assert any(k.startswith("fusion|") for k in A._MEM)
     A.clear()
+
+
+def test_adjoint_image_and_cross_grad_kernels():
+    """tqk_fused_prepare_adjoint(U) is byte-identical to tqk_fused_prepare(U^H), and
+    tqk_fused_cross_grad adds M U (M from the real cross term) into a float64 cotangent
+    within float32 accuracy."""
+    from torchquantum_gb300 import _lib
+
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(5)
+    b = 3
+    z = rng.normal(size=(b, 64, 64)) + 1j * rng.normal(size=(b, 64, 64))
+    u = torch.tensor(np.linalg.qr(z)[0], dtype=torch.complex128, device=dev)
+    wires = [3, 9, 0, 14, 7, 11]
+    img_h = _lib.fused_prepare_adjoint(u, wires)
+    ref_h = _lib.fused_prepare(u.conj().transpose(-1, -2).contiguous(), wires)
+    assert torch.equal(img_h, ref_h)
+    mr = torch.tensor(rng.normal(size=(b, 128, 128)), dtype=torch.float64, device=dev)
+    gu = torch.tensor(rng.normal(size=(b, 64, 64)) + 1j * rng.normal(size=(b, 64, 64)), dtype=torch.complex128,
+                      device=dev)
+    want = gu + torch.matmul(_lib.cross_to_complex(mr), u)
+    _lib.fused_cross_grad(mr, u, torch.view_as_real(gu))
+    assert (gu - want).abs().max().item() < 1e-4 * want.abs().max().item()

@@ -57,6 +57,8 @@ _SIGS = {
     "tqk_adjoint_diagonal": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
     "tqk_fused_image_bytes": (_i64, [_i64]),
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp, _vp]),
+    "tqk_fused_prepare_adjoint": (_int, [_vp, _i64, _vp, _vp, _vp]),
+    "tqk_fused_cross_grad": (_int, [_vp, _vp, _i64, _vp, _vp]),
     "tqk_sample_scratch_bytes": (_i64, [_i64, _int]),
     "tqk_sample": (_int, [_vp, _i64, _int, _vp, _i64, _vp, _vp, _i64, _vp]),
     "tqk_staged_apply": (_int, [_vp, _i64, _int, _vp, _int, _int, _vp, _vp]),
@@ -320,6 +322,22 @@ def fused_prepare(u128: torch.Tensor, wires: Sequence[int]) -> torch.Tensor:
     img = torch.empty(lib.tqk_fused_image_bytes(b), dtype=torch.uint8, device=u128.device)
     _check(lib.tqk_fused_prepare(u128.data_ptr(), b, _i32(wires), img.data_ptr(), _stream(u128)))
     return img
+
+
+def fused_prepare_adjoint(u128: torch.Tensor, wires: Sequence[int]) -> torch.Tensor:
+    """The image of U^H for fused_adjoint, built from U (complex128 [B, 64, 64])."""
+    lib = load()
+    b = int(u128.shape[0])
+    img = torch.empty(lib.tqk_fused_image_bytes(b), dtype=torch.uint8, device=u128.device)
+    _check(lib.tqk_fused_prepare_adjoint(u128.data_ptr(), b, _i32(wires), img.data_ptr(), _stream(u128)))
+    return img
+
+
+def fused_cross_grad(mr: torch.Tensor, u128: torch.Tensor, gu: torch.Tensor) -> None:
+    """gu += M U per batch row (M from the adjoint step's cross term ``mr``); ``gu`` is a
+    complex128 [B, 64, 64] tensor or its float64 interleaved view."""
+    b = int(u128.shape[0])
+    _check(load().tqk_fused_cross_grad(mr.data_ptr(), u128.data_ptr(), b, gu.data_ptr(), _stream(u128)))
 
 
 def fused_apply(state, n, wires, image, u_batch):

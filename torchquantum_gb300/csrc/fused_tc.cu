@@ -588,18 +588,23 @@ __host__ PatternOrders pattern_orders(const int32_t* wires) {
 // the output and K orders), so one N = 128 product with a tile [Re x | Im x] gives the
 // real and imaginary parts of (U x)[o] side by side.  One thread per (batch, row,
 // 16-byte chunk).
+// ADJ: the image of U^H, read from U (entry (o, k) of U^H is conj U[k][o]).
+template <bool ADJ>
 __global__ void k_tc_prep(const double2* u, int64_t u_batch, uint8_t* img, const __grid_constant__ PatternOrders ord) {
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= u_batch * 128 * 16) return;
   const int64_t b = idx / (128 * 16);
   const int row = static_cast<int>((idx / 16) % 128);
   const int chunk = static_cast<int>(idx % 16);
-  const double2* ub = u + b * 64 * 64 + ord.nat_of_out[row >> 1] * 64;
+  const double2* ub = u + b * 64 * 64;
+  const int orow = ord.nat_of_out[row >> 1];
   float hv[8], lv[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int kk = chunk * 8 + e;
-    const double2 z = ub[ord.nat_of_k[kk & 63]];
+    const int kcol = ord.nat_of_k[kk & 63];
+    double2 z = ADJ ? ub[kcol * 64 + orow] : ub[orow * 64 + kcol];
+    if (ADJ) z.y = -z.y;
     const double v = (row & 1) == 0 ? (kk < 64 ? z.x : -z.y) : (kk < 64 ? z.y : z.x);
     const __nv_bfloat16 h = __double2bfloat16(v);
     hv[e] = __bfloat162float(h);
@@ -620,20 +625,92 @@ using namespace tqk;
 
 extern "C" int64_t tqk_fused_image_bytes(int64_t u_batch) { return u_batch * 2 * tc::kBImgBytes; }
 
-extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream) {
-  if (!u || !image || !wires) return fail(TQK_BAD_POINTER, "tqk_fused_prepare: null pointer");
-  if ((reinterpret_cast<uintptr_t>(image) & 15u) != 0)
-    return fail(TQK_BAD_POINTER, "tqk_fused_prepare: image must be 16-byte aligned");
-  if (u_batch < 1) return fail(TQK_BAD_SHAPE, "tqk_fused_prepare: u_batch must be >= 1");
+namespace {
+int prepare_entry(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream, bool adj,
+                  const char* what) {
+  if (!u || !image || !wires) return fail(TQK_BAD_POINTER, "%s: null pointer", what);
+  if ((reinterpret_cast<uintptr_t>(image) & 15u) != 0) return fail(TQK_BAD_POINTER, "%s: image must be 16-byte aligned", what);
+  if (u_batch < 1) return fail(TQK_BAD_SHAPE, "%s: u_batch must be >= 1", what);
   for (int i = 0; i < 6; ++i) {
-    if (wires[i] < 0) return fail(TQK_BAD_WIRES, "tqk_fused_prepare: negative wire %d", wires[i]);
+    if (wires[i] < 0) return fail(TQK_BAD_WIRES, "%s: negative wire %d", what, wires[i]);
     for (int k = 0; k < i; ++k)
-      if (wires[k] == wires[i]) return fail(TQK_BAD_WIRES, "tqk_fused_prepare: wire %d used twice", wires[i]);
+      if (wires[k] == wires[i]) return fail(TQK_BAD_WIRES, "%s: wire %d used twice", what, wires[i]);
   }
   const int64_t work = u_batch * 128 * 16;
-  tc::k_tc_prep<<<static_cast<unsigned>((work + 255) / 256), 256, 0, as_stream(stream)>>>(
-      static_cast<const double2*>(u), u_batch, static_cast<uint8_t*>(image), tc::pattern_orders(wires));
-  return launch_status("tqk_fused_prepare");
+  const unsigned grid = static_cast<unsigned>((work + 255) / 256);
+  if (adj)
+    tc::k_tc_prep<true><<<grid, 256, 0, as_stream(stream)>>>(static_cast<const double2*>(u), u_batch,
+                                                           static_cast<uint8_t*>(image), tc::pattern_orders(wires));
+  else
+    tc::k_tc_prep<false><<<grid, 256, 0, as_stream(stream)>>>(static_cast<const double2*>(u), u_batch,
+                                                            static_cast<uint8_t*>(image), tc::pattern_orders(wires));
+  return launch_status(what);
+}
+}  // namespace
+
+extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream) {
+  return prepare_entry(u, u_batch, wires, image, stream, false, "tqk_fused_prepare");
+}
+
+extern "C" int tqk_fused_prepare_adjoint(const void* u, int64_t u_batch, const int32_t* wires, void* image,
+                                         void* stream) {
+  return prepare_entry(u, u_batch, wires, image, stream, true, "tqk_fused_prepare_adjoint");
+}
+
+// gu[b] += M_b U_b for the block cotangent: M_b (64 x 64 complex) from the adjoint step's
+// real cross term mr[b] (rows / columns 64p + j, p = 0 real, 1 imaginary part:
+// M[j][j'] = mr[j][j'] + mr[64+j][64+j'] + i (mr[64+j][j'] - mr[j][64+j'])), U_b the
+// block unitary (complex128); the product in float32 (M carries fp32 accuracy),
+// accumulated into gu (complex128).  One CTA per batch row.
+namespace tqk {
+namespace tc {
+__global__ void __launch_bounds__(256) k_cross_grad(const double* mr, const double2* u, double2* gu) {
+  extern __shared__ float2 cg_smem[];  // M [64][64] then U [64][64]: 64 KB
+  float2(*M)[64] = reinterpret_cast<float2(*)[64]>(cg_smem);
+  float2(*U)[64] = reinterpret_cast<float2(*)[64]>(cg_smem + 64 * 64);
+  const int64_t b = blockIdx.x;
+  const double* m = mr + b * 128 * 128;
+  const double2* ub = u + b * 64 * 64;
+  for (int e = threadIdx.x; e < 64 * 64; e += 256) {
+    const int j = e >> 6, k = e & 63;
+    const double re = m[j * 128 + k] + m[(64 + j) * 128 + 64 + k];
+    const double im = m[(64 + j) * 128 + k] - m[j * 128 + 64 + k];
+    M[j][k] = make_float2(static_cast<float>(re), static_cast<float>(im));
+    const double2 z = ub[e];
+    U[j][k] = make_float2(static_cast<float>(z.x), static_cast<float>(z.y));
+  }
+  __syncthreads();
+  double2* g = gu + b * 64 * 64;
+  for (int e = threadIdx.x; e < 64 * 64; e += 256) {
+    const int j = e >> 6, k = e & 63;
+    float ax = 0.f, ay = 0.f;
+#pragma unroll 8
+    for (int t = 0; t < 64; ++t) {
+      const float2 a = M[j][t], c = U[t][k];
+      ax = fmaf(a.x, c.x, fmaf(-a.y, c.y, ax));
+      ay = fmaf(a.x, c.y, fmaf(a.y, c.x, ay));
+    }
+    g[e].x += static_cast<double>(ax);
+    g[e].y += static_cast<double>(ay);
+  }
+}
+}  // namespace tc
+}  // namespace tqk
+
+extern "C" int tqk_fused_cross_grad(const double* mr, const void* u, int64_t batch, void* gu, void* stream) {
+  if (!mr || !u || !gu) return fail(TQK_BAD_POINTER, "tqk_fused_cross_grad: null pointer");
+  if (batch < 1 || batch > 0x7fffffff) return fail(TQK_BAD_SHAPE, "tqk_fused_cross_grad: batch %lld", (long long)batch);
+  constexpr int smem = 2 * 64 * 64 * static_cast<int>(sizeof(float2));
+  static int attr_dev = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (attr_dev != dev) {
+    cudaFuncSetAttribute(tc::k_cross_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr_dev = dev;
+  }
+  tc::k_cross_grad<<<static_cast<unsigned>(batch), 256, smem, as_stream(stream)>>>(
+      mr, static_cast<const double2*>(u), static_cast<double2*>(gu));
+  return launch_status("tqk_fused_cross_grad");
 }
 
 namespace {

@@ -124,17 +124,16 @@ def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: O
     """Tensor-core adjoint step of a fused 6-wire block: psi, lam <- U^H (.), and the
     cotangent of U as M U with M = sum over columns of lam conj(psi)^T (U unitary),
     added into ``grad`` (float64 interleaved view of a complex128 [batch, 64, 64])."""
-    u = u128.detach()
-    img_h = _lib.fused_prepare(kernel_operand(u.conj().transpose(-1, -2)), wires)
+    u = kernel_operand(u128)
+    img_h = _lib.fused_prepare_adjoint(u, wires)
     mr = None
     if grad is not None:
         mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=psi.device)
     _lib.fused_adjoint(psi, lam, n, wires, img_h, batch, mr)
     if grad is not None:
-        # M carries fp32 accuracy (tensor-memory accumulation), so M U in complex64 loses
-        # nothing and avoids the slow float64 path
-        gu = torch.matmul(_lib.cross_to_complex(mr).to(torch.complex64), u.to(torch.complex64))
-        torch.view_as_complex(grad.view(-1, 2)).view(u.shape).add_(gu)
+        # M carries fp32 accuracy (tensor-memory accumulation), so M U in float32 loses
+        # nothing; one kernel adds it into the float64 cotangent
+        _lib.fused_cross_grad(mr, u, grad)
 
 
 class CircuitFunction(torch.autograd.Function):
