@@ -21,6 +21,7 @@
 
 #include <vector>
 
+#include "bulk.cuh"
 #include "common.cuh"
 
 namespace tqk {
@@ -197,7 +198,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
   __shared__ Tabs tabs;
   __shared__ long long s_i;
   __shared__ double red[THREADS / 32];
+  __shared__ uint64_t full;  // bulk-copy (TMA) tile loads complete here
+  __shared__ int abort_flag;
   if (t_done != nullptr && blockIdx.x == 0 && threadIdx.x == 0) t_done[ncirc] = global_ns();
+  if (threadIdx.x == 0) {
+    bulk::mbar_init(&full);
+    abort_flag = 0;
+  }
+  uint32_t use = 0;  // loads completed on `full` so far
   for (;;) {
     if (threadIdx.x == 0) s_i = atomicAdd(counter, 1);
     __syncthreads();
@@ -252,14 +260,28 @@ __global__ void __launch_bounds__(THREADS, MINB)
       ++j;
     }
     __syncthreads();
+    // Runs of 32 amplitudes (tile bits 0-4 are address bits 0-4) or the whole tile when it
+    // is smaller: contiguous in HBM, moved by the bulk-copy engine.
+    const int run = tsz < 32 ? tsz : 32;
+    const int nruns = tsz / run;
     if (P.flags & kFirst) {
       for (int l = threadIdx.x; l < tsz; l += THREADS)
         amp[l] = make_float2((base == 0u && l == 0) ? 1.f : 0.f, 0.f);
     } else {
-#pragma unroll 4
-      for (int l = threadIdx.x; l < tsz; l += THREADS) amp[l] = __ldcg(st + base + dep(tabs, l));
+      if (threadIdx.x == 0) bulk::mbar_expect(&full, static_cast<uint32_t>(tsz * sizeof(float2)));
+      __syncthreads();
+      asm volatile("fence.proxy.async.global;" ::: "memory");  // the dependency flag was read by the generic proxy
+      for (int r = threadIdx.x; r < nruns; r += THREADS)
+        bulk::bulk_load(amp + r * run, st + base + dep(tabs, static_cast<uint32_t>(r * run)),
+                        static_cast<uint32_t>(run * sizeof(float2)), &full);
+      if (threadIdx.x == 0 && !bulk::mbar_wait(&full, use & 1u)) {
+        atomicExch(status, TQK_TIMEOUT);
+        abort_flag = 1;
+      }
+      ++use;
     }
     __syncthreads();
+    if (abort_flag) break;  // uniform: a tile load never landed
     for (int oi = 0; oi < P.num_ops; ++oi) {
       apply_op<THREADS>(ops[P.first_op + oi], amp, n, tb, tmask, base, tabs, mats);
       __syncthreads();
@@ -276,8 +298,19 @@ __global__ void __launch_bounds__(THREADS, MINB)
       if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = zacc;
     }
     if (((P.flags & kLast) == 0 || write_states) && C.state_off >= 0) {
-#pragma unroll 4
-      for (int l = threadIdx.x; l < tsz; l += THREADS) __stcg(st + base + dep(tabs, l), amp[l]);
+      bulk::fence_async_smem();  // the ops' shared-memory writes, visible to the bulk stores
+      __syncthreads();
+      bool mine = false;
+      for (int r = threadIdx.x; r < nruns; r += THREADS) {
+        bulk::bulk_store(st + base + dep(tabs, static_cast<uint32_t>(r * run)), amp + r * run,
+                         static_cast<uint32_t>(run * sizeof(float2)));
+        mine = true;
+      }
+      if (mine) {
+        bulk::bulk_commit();
+        bulk::bulk_wait_all();  // stored in HBM / L2 before the tile counts as done
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+      }
     }
     __threadfence();
     __syncthreads();

@@ -18,6 +18,7 @@
 // memory across every tile the CTA handles; one atomic per value per CTA at the end).
 #include <stdint.h>
 
+#include "bulk.cuh"
 #include "common.cuh"
 
 namespace tqk {
@@ -25,54 +26,8 @@ namespace staged {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
-// ------------------------------------------------------------------ bulk-copy (TMA) tiles
-// A tile is contiguous in HBM (2^tile_bits amplitudes of one row), so one elected thread
-// moves it with the bulk-copy engine: cp.async.bulk global -> shared completing on an
-// mbarrier, and cp.async.bulk shared -> global in a bulk group.  Sizes are multiples of
-// 16 bytes and both addresses 16-byte aligned (tile_bits >= 1, rows of 2^n amplitudes).
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-// Bounded wait on phase `parity`; false if it did not complete within kWaitCycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const long long t0 = clock64();
-  for (;;) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
-}
-__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+using namespace bulk;
 
 // Thread 0: load `nreg` tile regions (bytes each) for use number `use` of the barrier; the
 // previous tile's bulk stores must have finished reading the buffer first.  Returns false
