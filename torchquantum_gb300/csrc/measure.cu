@@ -78,38 +78,41 @@ __device__ __forceinline__ float pair_term(float2 a, float2 ap, uint64_t i, uint
 }
 
 // x == 0: diagonal strings, contribution |psi_i|^2 * (-1)^{popcount(i & z)}
+// NS: strings the pass's accumulators hold (1, 2, 4 or 8 >= p.ns): fewer registers for
+// the common one-string pass, so more warps -- more loads in flight -- per SM.
+template <int NS>
 __global__ void __launch_bounds__(256) k_expval_diag(const ExpvalParams p) {
   const int64_t b = blockIdx.y;
   const float2* row = p.state + (b << p.n);
-  float acc[kMaxStringsPerPass];
+  float acc[NS];
 #pragma unroll
-  for (int s = 0; s < kMaxStringsPerPass; ++s) acc[s] = 0.f;
+  for (int s = 0; s < NS; ++s) acc[s] = 0.f;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < p.work; t += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t i = (uint64_t)t * 2;
     const float4 v = ld4(row + i);
     const float p0 = v.x * v.x + v.y * v.y, p1 = v.z * v.z + v.w * v.w;
 #pragma unroll
-    for (int s = 0; s < kMaxStringsPerPass; ++s)
+    for (int s = 0; s < NS; ++s)
       if (s < p.ns) acc[s] += sgn_parity(i & p.z[s]) * p0 + sgn_parity((i + 1) & p.z[s]) * p1;
   }
-  block_reduce_store<kMaxStringsPerPass>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
+  block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
 }
 
 // x != 0: pairs (i, i^x) with bit hbit of i clear.
-template <bool LOWX>  // LOWX: x == 1 (the pair is one float4)
+template <bool LOWX, int NS>  // LOWX: x == 1 (the pair is one float4)
 __global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
   const int64_t b = blockIdx.y;
   const float2* row = p.state + (b << p.n);
-  float acc[kMaxStringsPerPass];
+  float acc[NS];
 #pragma unroll
-  for (int s = 0; s < kMaxStringsPerPass; ++s) acc[s] = 0.f;
+  for (int s = 0; s < NS; ++s) acc[s] = 0.f;
   const uint64_t lomask = (1ull << p.hbit) - 1ull;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < p.work; t += (int64_t)gridDim.x * blockDim.x) {
     if (LOWX) {
       const uint64_t i = (uint64_t)t * 2;  // i has bit 0 clear, partner i+1
       const float4 v = ld4(row + i);
 #pragma unroll
-      for (int s = 0; s < kMaxStringsPerPass; ++s)
+      for (int s = 0; s < NS; ++s)
         if (s < p.ns) acc[s] += pair_term(lo2(v), hi2(v), i, i + 1, p.z[s], p.ny[s]);
     } else {
       const uint64_t g = (uint64_t)t * 2;  // two consecutive groups: i, i+1 (hbit >= 1)
@@ -121,16 +124,31 @@ __global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
       const float2 a0 = lo2(v), a1 = hi2(v);
       const float2 b0 = sw ? hi2(w) : lo2(w), b1 = sw ? lo2(w) : hi2(w);
 #pragma unroll
-      for (int s = 0; s < kMaxStringsPerPass; ++s)
+      for (int s = 0; s < NS; ++s)
         if (s < p.ns)
           acc[s] += pair_term(a0, b0, i, ip, p.z[s], p.ny[s]) + pair_term(a1, b1, i + 1, ip ^ 1ull, p.z[s], p.ny[s]);
     }
   }
-  block_reduce_store<kMaxStringsPerPass>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
+  block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
 }
 
 // The two kernels above store block partials contiguously as [row][block][slot];
 // this kernel reduces them in block order into out[row*m + col].
+// Launch the pass kernel with the smallest accumulator count that holds p.ns strings.
+template <int NS>
+void launch_expval_ns(const ExpvalParams& p, dim3 grid, cudaStream_t st) {
+  if (p.x == 0) k_expval_diag<NS><<<grid, 256, 0, st>>>(p);
+  else if (p.x == 1ull) k_expval_pair<true, NS><<<grid, 256, 0, st>>>(p);
+  else k_expval_pair<false, NS><<<grid, 256, 0, st>>>(p);
+}
+
+inline void launch_expval(const ExpvalParams& p, dim3 grid, cudaStream_t st) {
+  if (p.ns <= 1) launch_expval_ns<1>(p, grid, st);
+  else if (p.ns <= 2) launch_expval_ns<2>(p, grid, st);
+  else if (p.ns <= 4) launch_expval_ns<4>(p, grid, st);
+  else launch_expval_ns<8>(p, grid, st);
+}
+
 struct FinishCols {
   int c[kMaxStringsPerPass];
 };
@@ -181,6 +199,8 @@ __global__ void __launch_bounds__(256) k_pauli_apply_sum(const ApplySumParams p)
     o0 = lo2(v);
     o1 = hi2(v);
   }
+  // unrolled so that several partner loads are in flight per thread
+#pragma unroll 4
   for (int s = 0; s < p.ns; ++s) {
     const float c = __ldg(p.coef + b * p.m + p.col0 + s);
     const uint64_t x = p.x[s];
@@ -272,21 +292,14 @@ extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uin
       cols.c[s] = 0;
     }
     dim3 grid((unsigned)nblk, (unsigned)bsz, 1);
-    const int threads = 256;
+    // block partials land at partial[(b*nblk + blk)*kMax + s]
     if (p.x == 0) {
       p.work = (1ll << n) >> 1;
-      // block partials land at partial[(b*nblk + blk)*kMax + s]
-      k_expval_diag<<<grid, threads, 0, st>>>(p);
     } else {
       p.hbit = 63 - __builtin_clzll(p.x);
-      if (p.x == 1ull) {
-        p.work = (1ll << n) >> 1;
-        k_expval_pair<true><<<grid, threads, 0, st>>>(p);
-      } else {
-        p.work = (1ll << n) >> 2;
-        k_expval_pair<false><<<grid, threads, 0, st>>>(p);
-      }
+      p.work = p.x == 1ull ? (1ll << n) >> 1 : (1ll << n) >> 2;
     }
+    launch_expval(p, grid, st);
     if ((rc = launch_status(what))) return rc;
     const int64_t nout = bsz * p.ns;
     k_expval_finish<<<(unsigned)((nout + 127) / 128), 128, 0, st>>>(partial, nblk, p.ns, kMaxStringsPerPass,
@@ -432,17 +445,11 @@ extern "C" int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, c
     dim3 grid(static_cast<unsigned>(nblk), static_cast<unsigned>(bsz), 1);
     if (p.x == 0) {
       p.work = (1ll << n) >> 1;
-      k_expval_diag<<<grid, 256, 0, st>>>(p);
     } else {
       p.hbit = 63 - __builtin_clzll(p.x);
-      if (p.x == 1ull) {
-        p.work = (1ll << n) >> 1;
-        k_expval_pair<true><<<grid, 256, 0, st>>>(p);
-      } else {
-        p.work = (1ll << n) >> 2;
-        k_expval_pair<false><<<grid, 256, 0, st>>>(p);
-      }
+      p.work = p.x == 1ull ? (1ll << n) >> 1 : (1ll << n) >> 2;
     }
+    launch_expval(p, grid, st);
     if ((rc = launch_status(what))) return rc;
     const int64_t nout = bsz * p.ns;
     k_expval_finish<<<static_cast<unsigned>((nout + 127) / 128), 128, 0, st>>>(partial, nblk, p.ns,
