@@ -39,6 +39,7 @@ METRIC = "fwd+bwd circuits/s fused+adjoint vs plain at <=1e-5 vs FP64; HBM GB/s 
 # (n_wires=22, bsz=8, per-row U); the kernel streams every amplitude of psi and lam once,
 # so traffic scales with the amplitudes processed.
 ADJ_TRAFFIC_CAPTURE = {"n": 22, "bsz": 8, "dram_bytes": 539.099648e6 + 477.703168e6}
+ADJ_STORED_TRAFFIC_CAPTURE = {"n": 22, "bsz": 8, "dram_bytes": 539.196928e6 + 220.006656e6}
 UNIT = "circuits/s"
 
 
@@ -275,6 +276,9 @@ def run_ours(args):
         fusion_info = {"width": [getattr(sg, "fuse_width", None) for sg in segs],
                        "passes": sum(len(sg.exec_ops) for sg in segs),
                        "tensor_core_passes": sum(1 for sg in segs for op in sg.exec_ops if getattr(op, "tc", False)),
+                       # tensor-core blocks whose input state the forward kept for the backward
+                       "stored_inputs": sum(1 for sg in segs for op in sg.exec_ops
+                                            if getattr(op, "stored_input", None) is not None),
                        "chosen_by": "autotuner (measured pass costs)" if args.fuse == "auto" else f"fixed k={args.fuse}"}
     last.clear()
     ms = R.max_over_ranks(e0.elapsed_time(e1), dev)
@@ -333,7 +337,7 @@ def run_ours(args):
                        "h2d_bytes_per_step": int(pin_theta.numel() * 4),
                        "d2h_bytes_per_step": int(out_ev.numel() * 4 + out_g.numel() * 4)}
         # ---------------- roofline of the dominant kernel (adjoint dense 1-wire step)
-        line["roofline"], line["kernels"] = roofline(args, dev)
+        line["roofline"], line["kernels"] = roofline(args, dev, bool(fusion_info and fusion_info["stored_inputs"]))
         line["plain_gate_pass"] = line["kernels"]["dense1_fwd"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.quick:
         v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds)
@@ -352,9 +356,11 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def roofline(args, dev):
+def roofline(args, dev, stored=True):
     """Time the engine's hot kernels alone (CUDA events on the launching stream) on the
-    bench's state size; algorithmic bytes per launch from the touched amplitudes."""
+    bench's state size; algorithmic bytes per launch from the touched amplitudes.
+    ``stored``: the fused step's blocks kept their inputs, so its dominant kernel is the
+    stored-input adjoint step."""
     import torch
 
     from torchquantum_gb300 import _lib
@@ -436,10 +442,16 @@ def roofline(args, dev):
         mr = torch.zeros(bsz, 128, 128, dtype=torch.float64, device=dev)
         tiles = bsz * (1 << (n - 6)) // 128
         fl_apply = tiles * 24 * 128 * 128 * 16 * 2
+        out = torch.empty_like(psi)
         extra = {
             "fused6_tc_fwd": (lambda i: _lib.fused_apply(psi, n, wsets[i], imgs[i], bsz), 2 * S, fl_apply),
+            "fused6_tc_fwd_to": (lambda i: _lib.fused_apply_to(psi, out, n, wsets[i], imgs[i], bsz), 2 * S,
+                                 fl_apply),
             "fused6_tc_adj": (lambda i: _lib.fused_adjoint(psi, lam, n, wsets[i], imghs[i], bsz, mr), 4 * S,
                               3 * fl_apply),
+            # reads the block's stored input and lam, writes lam: 3 S
+            "fused6_tc_adj_stored": (lambda i: _lib.fused_adjoint_stored(out, lam, n, wsets[i], imghs[i], bsz, mr),
+                                     3 * S, 3 * fl_apply),
         }
         for name, (fn, nbytes, flops) in extra.items():
             t = timeit(fn)
@@ -448,12 +460,18 @@ def roofline(args, dev):
                          "tensor_TFLOP/s": flops / t / 1e12}
         _lib.check_status(dev)
     traffic = None
-    if args.method == "fused" and "fused6_tc_adj" in res:
+    cap = None
+    if args.method == "fused" and stored and "fused6_tc_adj_stored" in res:
+        dom = res["fused6_tc_adj_stored"]
+        kname = "tqk::tc::k_tc<true> (stored-input adjoint step of a fused 6-wire block, tcgen05 split-BF16)"
+        cap = ADJ_STORED_TRAFFIC_CAPTURE
+    elif args.method == "fused" and "fused6_tc_adj" in res:
         dom = res["fused6_tc_adj"]
         kname = "tqk::tc::k_tc<true> (adjoint step of a fused 6-wire block, tcgen05 split-BF16)"
         cap = ADJ_TRAFFIC_CAPTURE
+    if cap is not None and cap.get("dram_bytes"):
         traffic = cap["dram_bytes"] * (bsz << n) / (cap["bsz"] << cap["n"])
-    else:
+    if cap is None:
         dom = res["dense1_adj"]
         kname = "k_dense_adj<2> (adjoint step of a dense 1-wire gate)"
     roof = {"bound": "hbm", "achieved": dom["GB/s"], "peak": peak, "unit": "GB/s", "frac": dom["GB/s"] / peak,

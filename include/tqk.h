@@ -168,10 +168,18 @@ int tqk_fused_prepare_adjoint(const void* u, int64_t u_batch, const int32_t* wir
 /* Block cotangent from an adjoint step: gu[b] += M_b U_b (complex128 [batch, 64, 64]),
  * where M_b is the complex 64 x 64 matrix held by the real cross term mr[b]
  * ([batch, 128, 128] float64 from tqk_fused_adjoint) and U_b the block unitary
- * (complex128 [batch, 64, 64]); the product runs in float32, the sum in float64. */
+ * (complex128 [batch, 64, 64]); the product runs in float32, the sum in float64.
+ * u == NULL: gu[b] += M_b (the cross term of tqk_fused_adjoint_stored, taken against the
+ * block's input state, is the cotangent itself). */
 int tqk_fused_cross_grad(const double* mr, const void* u, int64_t batch, void* gu, void* stream);
 int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
                     int64_t u_batch, int* status, void* stream);
+/* Out-of-place tqk_fused_apply: state_out = U state_in, state_in unchanged.  The two
+ * buffers are the same (in place) or do not overlap.  A forward that writes every
+ * block's output to a new buffer keeps each block's input state for
+ * tqk_fused_adjoint_stored. */
+int tqk_fused_apply_to(const void* state_in, void* state_out, int64_t bsz, int n, const int32_t* wires,
+                       const void* image, int64_t u_batch, int* status, void* stream);
 
 /* Adjoint step of a fused block on the tensor cores: psi <- U^H psi, lam <- U^H lam
  * (image_h = tqk_fused_prepare of U^H on the same wires), and, if mr_out != NULL, the real cross term
@@ -182,6 +190,13 @@ int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const
 int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires,
                       const void* image_h, int64_t u_batch, double* mr_out, int* status,
                       void* stream);
+/* Adjoint step of a fused block whose input state is still stored: psi_in = the state
+ * the block was applied to (read only), lam <- U^H lam in place, and, if mr_out != NULL,
+ * the real cross term of lam (before the step) against psi_in in the layout of
+ * tqk_fused_adjoint, from which the cotangent of U is M itself (tqk_fused_cross_grad
+ * with u = NULL).  Reads two states and writes one, where tqk_fused_adjoint writes two. */
+int tqk_fused_adjoint_stored(const void* psi_in, void* lam, int64_t bsz, int n, const int32_t* wires,
+                             const void* image_h, int64_t u_batch, double* mr_out, int* status, void* stream);
 
 /* ---------------------------------------------------------------- gate programs
  * Parameterised gates whose operand the GPU builds from the parameters in place.

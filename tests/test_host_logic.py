@@ -70,10 +70,11 @@ def test_engine_defaults_roundtrip():
     import torchquantum_gb300 as tq
     from torchquantum_gb300 import device as D
 
-    prev = tq.set_engine_defaults(method="fused", fuse_wires=5, fused_backend="tc", stage_low=False)
+    prev = tq.set_engine_defaults(method="fused", fuse_wires=5, fused_backend="tc", stage_low=False, checkpoint=False)
     try:
-        assert D.ENGINE_DEFAULTS == {"method": "fused", "fuse_wires": 5, "fused_backend": "tc", "stage_low": False}
-        for bad in ({"method": "x"}, {"fuse_wires": 7}, {"fused_backend": "gpu"}):
+        assert D.ENGINE_DEFAULTS == {"method": "fused", "fuse_wires": 5, "fused_backend": "tc", "stage_low": False,
+                                     "checkpoint": False}
+        for bad in ({"method": "x"}, {"fuse_wires": 7}, {"fused_backend": "gpu"}, {"checkpoint": "yes"}):
             with pytest.raises(ValueError):
                 tq.set_engine_defaults(**bad)
     finally:

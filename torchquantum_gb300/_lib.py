@@ -68,6 +68,8 @@ _SIGS = {
     "tqk_batch_run": (_int, [_vp, _int, _vp, _vp, _vp, _i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tqk_fused_apply": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
     "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
+    "tqk_fused_apply_to": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
+    "tqk_fused_adjoint_stored": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
     "tqk_pauli_expval_noalloc_capacity": (_i64, []),
     "tqk_pauli_expval_noalloc": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp]),
     "tqk_gate_operand_size": (_int, [_int]),
@@ -333,16 +335,30 @@ def fused_prepare_adjoint(u128: torch.Tensor, wires: Sequence[int]) -> torch.Ten
     return img
 
 
-def fused_cross_grad(mr: torch.Tensor, u128: torch.Tensor, gu: torch.Tensor) -> None:
-    """gu += M U per batch row (M from the adjoint step's cross term ``mr``); ``gu`` is a
-    complex128 [B, 64, 64] tensor or its float64 interleaved view."""
-    b = int(u128.shape[0])
-    _check(load().tqk_fused_cross_grad(mr.data_ptr(), u128.data_ptr(), b, gu.data_ptr(), _stream(u128)))
+def fused_cross_grad(mr: torch.Tensor, u128: Optional[torch.Tensor], gu: torch.Tensor) -> None:
+    """gu += M U per batch row (M from the adjoint step's cross term ``mr``), or gu += M
+    when ``u128`` is None (the cross term of a stored-input step); ``gu`` is a complex128
+    [B, 64, 64] tensor or its float64 interleaved view."""
+    b = int(mr.shape[0])
+    _check(load().tqk_fused_cross_grad(mr.data_ptr(), _ptr(u128), b, gu.data_ptr(), _stream(mr)))
 
 
 def fused_apply(state, n, wires, image, u_batch):
     _check(load().tqk_fused_apply(state.data_ptr(), state.shape[0], n, _i32(wires), image.data_ptr(), u_batch,
                                   status_word(state.device).data_ptr(), _stream(state)))
+
+
+def fused_apply_to(src, dst, n, wires, image, u_batch):
+    """dst = U src for a fused block (src unchanged)."""
+    _check(load().tqk_fused_apply_to(src.data_ptr(), dst.data_ptr(), src.shape[0], n, _i32(wires), image.data_ptr(),
+                                     u_batch, status_word(src.device).data_ptr(), _stream(src)))
+
+
+def fused_adjoint_stored(psi_in, lam, n, wires, image_h, u_batch, mr_out):
+    """lam <- U^H lam and the cross term of lam against the block's stored input state."""
+    _check(load().tqk_fused_adjoint_stored(psi_in.data_ptr(), lam.data_ptr(), lam.shape[0], n, _i32(wires),
+                                           image_h.data_ptr(), u_batch, _ptr(mr_out),
+                                           status_word(lam.device).data_ptr(), _stream(lam)))
 
 
 def fused_adjoint(psi, lam, n, wires, image_h, u_batch, mr_out):

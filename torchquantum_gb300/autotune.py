@@ -153,11 +153,12 @@ SCRATCH_AMPS = 1 << 27   # cost probes run on at most 2^27 amplitudes (1 GiB) pe
 
 def pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool) -> dict:
     """Measured milliseconds per pass over a [bsz, 2^n] state: ``dense[k] = (fwd, adj)``
-    for the CUDA-core dense k-wire kernels (k = 1..min(6, n)) and ``tc = (fwd, adj)`` for
-    the tensor-core 6-wire block kernel (if ``tc_ok``).  Probes use min(bsz, rows that
+    for the CUDA-core dense k-wire kernels (k = 1..min(6, n)) and ``tc = (fwd, adj,
+    adj_stored)`` for the tensor-core 6-wire block kernel (if ``tc_ok``; adj_stored: the
+    reverse step that reads the block's stored input).  Probes use min(bsz, rows that
     fit 2^27 amplitudes) rows and are scaled to bsz (the kernels stream rows
     independently)."""
-    key = f"fusion|{gpu_key(dev)}|n{n}|b{bsz}|tc{int(tc_ok)}"
+    key = f"fusion2|{gpu_key(dev)}|n{n}|b{bsz}|tc{int(tc_ok)}"
     hit = lookup(key)
     if hit is not None:
         return hit
@@ -192,20 +193,23 @@ def _pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool, key: str) -> d
         u = torch.tensor(np.linalg.qr(z)[0], dtype=torch.complex128, device=dev)
         uh = u.conj().transpose(-1, -2).contiguous()
         mr = torch.zeros(rows, 128, 128, dtype=torch.float64, device=dev)
-        f = a = 0.0
+        f = a = s = 0.0
         for wires in layouts(6):
             img, imgh = _lib.fused_prepare(u, wires), _lib.fused_prepare(uh, wires)
             f += _time_ms(lambda: _lib.fused_apply(psi, n, wires, img, rows), dev)
             a += _time_ms(lambda: _lib.fused_adjoint(psi, lam, n, wires, imgh, rows, mr), dev)
-        out["tc"] = (f / 2 * scale, a / 2 * scale)
+            s += _time_ms(lambda: _lib.fused_adjoint_stored(psi, lam, n, wires, imgh, rows, mr), dev)
+        out["tc"] = (f / 2 * scale, a / 2 * scale, s / 2 * scale)
     _lib.check_status(dev)
     del psi, lam
     _store(key, out)
     return out
 
 
-def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool) -> Tuple[float, List[bool]]:
-    """(cost in ms, per-block use of the tensor-core kernel) of a fusion plan."""
+def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool,
+              stored: bool = False) -> Tuple[float, List[bool]]:
+    """(cost in ms, per-block use of the tensor-core kernel) of a fusion plan; ``stored``:
+    tensor-core blocks keep their inputs, so their reverse step is the stored-input one."""
     total = 0.0
     tc_flags = []
     for bwires, idxs in plan:
@@ -219,7 +223,9 @@ def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool) -> Tuple[float
         cd = dense[0] + (dense[1] if with_adjoint else 0.0) if dense else float("inf")
         ct = float("inf")
         if tc_ok and costs.get("tc"):
-            ct = costs["tc"][0] + (costs["tc"][1] if with_adjoint else 0.0)
+            tcc = costs["tc"]
+            adj = tcc[2] if stored and len(tcc) > 2 else tcc[1]
+            ct = tcc[0] + (adj if with_adjoint else 0.0)
         use_tc = ct < cd
         total += min(ct, cd)
         tc_flags.append(use_tc)
@@ -227,9 +233,10 @@ def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool) -> Tuple[float
 
 
 def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: torch.device, tc_ok: bool,
-                  with_adjoint: bool, widths: Sequence[int] = (4, 5, 6)):
+                  with_adjoint: bool, widths: Sequence[int] = (4, 5, 6), stored: bool = False):
     """(plan, per-block tensor-core flags, chosen width, cost table) for a segment: the
-    cheapest of the candidate plans under the measured per-pass costs."""
+    cheapest of the candidate plans under the measured per-pass costs (``stored``: the
+    tensor-core blocks are expected to keep their inputs for the backward)."""
     from . import fusion
 
     try:
@@ -239,13 +246,13 @@ def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: to
         # rule (tensor cores for multi-gate blocks when allowed) instead of measured costs
         torch.cuda.empty_cache()
         costs = {"dense": {str(k): (1.0 + 0.25 * k, 2.0 + 0.5 * k) for k in range(1, 7)},
-                 "tc": (1.0, 2.0) if tc_ok else None, "rows": 0}
+                 "tc": (1.0, 2.0, 1.5) if tc_ok else None, "rows": 0}
     best = None
     for k in widths:
         k = max(1, min(k, n, 6))
         for look, beam in ((0, 0), (8, 0), (8, 4)):
             plan = fusion.plan_cached(wire_lists, k, look, beam)
-            cost, flags = plan_cost(plan, costs, tc_ok, with_adjoint)
+            cost, flags = plan_cost(plan, costs, tc_ok, with_adjoint, stored)
             if best is None or cost < best[0]:
                 best = (cost, plan, flags, k)
     return best[1], best[2], best[3], costs

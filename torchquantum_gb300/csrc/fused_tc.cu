@@ -23,7 +23,10 @@
 // tile t+1 and stores of tile t overlap.  The adjoint step uses the same machinery on
 // mixed tiles (64 columns of psi and the same 64 columns of lam) against U^H, and adds
 // the cross term sum_columns lam~ psi~^T (MN-major reads of the same A image) in a
-// third accumulator.
+// third accumulator.  When the state the block was applied to is still in memory (the
+// forward wrote each block's output to a new buffer), the adjoint step reads it as the
+// psi half and stores only lam: three state transfers instead of four, and the cross
+// term is then the block cotangent itself.
 // Every mbarrier wait is bounded (clock-based); on a timeout the kernel records
 // TQK_TIMEOUT in *status, stops issuing work, waits (bounded) for MMAs in flight,
 // frees its tensor memory and returns.
@@ -240,7 +243,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // run over the 5 lowest-address remaining dimensions, so every load instruction is
 // coalesced whatever the target bits are.
 struct TcParams {
-  float2* psi;               // state (APPLY) / psi (ADJ)
+  float2* psi;               // state read (APPLY) / psi (ADJ)
+  float2* psi_out;           // APPLY: product destination (psi: in place); ADJ: U^H psi
+                             // destination (psi), or null when psi is the block's stored
+                             // input state, which is only read
   float2* lam;               // ADJ only
   int n;
   BitInsert ins;             // the 6 target bits
@@ -306,6 +312,31 @@ __device__ __forceinline__ int64_t tile_base(const TcParams& p, int64_t t, bool 
   return (b << p.n) + static_cast<int64_t>(insert6(static_cast<uint64_t>(c0), p.ins));
 }
 
+// Tiles ahead of the one being loaded whose lines the producers prefetch into L2, so that
+// DRAM stays busy while a tile is split and written to shared memory.
+#ifndef TQK_TC_PREFETCH
+#define TQK_TC_PREFETCH 1
+#endif
+constexpr int kPrefetchTiles = TQK_TC_PREFETCH;
+
+// Registers r whose amplitude starts a 128-byte line (16 amplitudes).  Address bits 0-3
+// are always tile dimensions (target bits or among the lowest non-target bits) and are
+// clear in a tile's base, so every line of a tile is whole and owned by exactly one
+// (thread, register).
+__device__ __forceinline__ uint32_t line_owner_mask(const TcParams& p, int64_t toff) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int r = 0; r < 32; ++r)
+    if (((static_cast<uint64_t>(toff) + p.reg_off[r]) & 15ull) == 0) m |= 1u << r;
+  return m;
+}
+
+__device__ __forceinline__ void prefetch_lines(const TcParams& p, const float2* src, uint32_t mask) {
+#pragma unroll
+  for (int r = 0; r < 32; ++r)
+    if ((mask >> r) & 1u) asm volatile("prefetch.global.L2 [%0];" ::"l"(src + p.reg_off[r]));
+}
+
 // Producer: load the thread's 32 amplitudes of tile t, split them into bf16 hi/lo and
 // store its four 16-byte chunks (K = 64p + 8g + e) into the A image.
 __device__ __forceinline__ void produce_tile(const TcParams& p, const float2* src, uint8_t* abuf, int row0, int g0) {
@@ -337,7 +368,9 @@ __device__ __forceinline__ void produce_tile(const TcParams& p, const float2* sr
 template <bool ADJ>
 __device__ __forceinline__ void drain_rows(const TcParams& p, int64_t tb, uint32_t d_tmem, int sub, int lane) {
   const int row = sub * 32 + lane;
-  float2* dst = ((ADJ && row >= 64) ? p.lam : p.psi) + tb + p.col_off[row];
+  float2* dbase = (ADJ && row >= 64) ? p.lam : p.psi_out;
+  if (ADJ && dbase == nullptr) return;  // psi rows of a stored-input step: warp-uniform (sub 0, 1)
+  float2* dst = dbase + tb + p.col_off[row];
   const uint32_t lanes = static_cast<uint32_t>(sub * 32) << 16;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -358,10 +391,11 @@ __device__ __forceinline__ void drain_cols(const TcParams& p, int64_t tb, uint32
   const int m = sub * 32 + lane;
   const uint32_t lanes = static_cast<uint32_t>(sub * 32) << 16;
   const int64_t o = tb + static_cast<int64_t>(p.off[m >> 1]);
-  float* dpsi = reinterpret_cast<float*>(p.psi + o) + (m & 1);
+  float* dpsi = p.psi_out ? reinterpret_cast<float*>(p.psi_out + o) + (m & 1) : nullptr;
   float* dlam = ADJ ? reinterpret_cast<float*>(p.lam + o) + (m & 1) : nullptr;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
+    if (ADJ && q < 4 && dpsi == nullptr) continue;  // psi columns of a stored-input step
     uint32_t v[16];
     tmem_ld16(d_tmem + lanes + q * 16, v);
     tmem_wait_ld();
@@ -452,8 +486,13 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
     const int row0 = p.lane_row[lane] + p.warp_row[warp];
     const int g0 = p.lane_g[lane] + p.warp_g[warp];
     const float2* base = (ADJ && p.warp_lam[warp]) ? p.lam : p.psi;
+    const uint32_t pf_mask = kPrefetchTiles > 0 ? line_owner_mask(p, toff) : 0u;
+    for (int64_t k = 1; k < kPrefetchTiles && k < ntiles; ++k)
+      prefetch_lines(p, base + tile_base(p, t_begin + k, ADJ) + toff, pf_mask);
     for (int64_t k = 0; k < ntiles; ++k) {
       const int buf = static_cast<int>(k % kABufs);
+      if (kPrefetchTiles > 0 && k + kPrefetchTiles < ntiles)
+        prefetch_lines(p, base + tile_base(p, t_begin + k + kPrefetchTiles, ADJ) + toff, pf_mask);
       if (k >= kABufs && !wait_or_abort(&sy->a_empty[buf], static_cast<uint32_t>((k / kABufs - 1) & 1), sy)) break;
       produce_tile(p, base + tile_base(p, t_begin + k, ADJ) + toff, abufs + buf * 2 * kImgBytes, row0, g0);
       fence_proxy_async();
@@ -694,12 +733,30 @@ __global__ void __launch_bounds__(256) k_cross_grad(const double* mr, const doub
     g[e].y += static_cast<double>(ay);
   }
 }
+
+// gu[b] += M_b: the cross term of a stored-input adjoint step is the cotangent itself
+// (float64 throughout).  One thread per complex entry.
+__global__ void __launch_bounds__(256) k_cross_add(const double* mr, int64_t batch, double2* gu) {
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= batch * 64 * 64) return;
+  const int64_t b = e >> 12;
+  const int j = static_cast<int>((e >> 6) & 63), k = static_cast<int>(e & 63);
+  const double* m = mr + b * 128 * 128;
+  gu[e].x += m[j * 128 + k] + m[(64 + j) * 128 + 64 + k];
+  gu[e].y += m[(64 + j) * 128 + k] - m[j * 128 + 64 + k];
+}
 }  // namespace tc
 }  // namespace tqk
 
 extern "C" int tqk_fused_cross_grad(const double* mr, const void* u, int64_t batch, void* gu, void* stream) {
-  if (!mr || !u || !gu) return fail(TQK_BAD_POINTER, "tqk_fused_cross_grad: null pointer");
+  if (!mr || !gu) return fail(TQK_BAD_POINTER, "tqk_fused_cross_grad: null pointer");
   if (batch < 1 || batch > 0x7fffffff) return fail(TQK_BAD_SHAPE, "tqk_fused_cross_grad: batch %lld", (long long)batch);
+  if (u == nullptr) {
+    const int64_t work = batch * 64 * 64;
+    tc::k_cross_add<<<static_cast<unsigned>((work + 255) / 256), 256, 0, as_stream(stream)>>>(
+        mr, batch, static_cast<double2*>(gu));
+    return launch_status("tqk_fused_cross_grad");
+  }
   constexpr int smem = 2 * 64 * 64 * static_cast<int>(sizeof(float2));
   static int attr_dev = -1;
   int dev = 0;
@@ -851,17 +908,28 @@ int tc_launch(const tqk::tc::TcParams& p, bool adj, void* stream, const char* wh
 
 }  // namespace
 
-extern "C" int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires,
-                                 const void* image_h, int64_t u_batch, double* mr_out, int* status, void* stream) {
-  const char* what = "tqk_fused_adjoint";
+namespace {
+
+// Stored state buffers must not overlap a buffer the same launch writes (other than
+// being that buffer).
+bool overlaps(const void* a, const void* b, int64_t bytes) {
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  return x != y && x < y + static_cast<uintptr_t>(bytes) && y < x + static_cast<uintptr_t>(bytes);
+}
+
+int adjoint_entry(const void* psi, float2* psi_out, void* lam, int64_t bsz, int n, const int32_t* wires,
+                  const void* image_h, int64_t u_batch, double* mr_out, int* status, void* stream, const char* what) {
   int rc = check_state(psi, bsz, n, what);
   if (rc) return rc;
   if ((rc = check_state(lam, bsz, n, what))) return rc;
   if ((rc = check_batch(u_batch, bsz, what))) return rc;
   if (!image_h || !status) return fail(TQK_BAD_POINTER, "%s: null image/status", what);
   if (n < 13) return fail(TQK_UNSUPPORTED, "%s: needs n_wires >= 13 (got %d)", what, n);
+  const int64_t bytes = bsz * (int64_t(8) << n);
+  if (psi == lam || overlaps(psi, lam, bytes)) return fail(TQK_BAD_POINTER, "%s: psi and lam overlap", what);
   tc::TcParams p;
-  p.psi = static_cast<float2*>(psi);
+  p.psi = const_cast<float2*>(static_cast<const float2*>(psi));
+  p.psi_out = psi_out;
   p.lam = static_cast<float2*>(lam);
   p.uimg = static_cast<const uint8_t*>(image_h);
   p.u_batch = u_batch;
@@ -871,17 +939,20 @@ extern "C" int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const
   return tc_launch(p, true, stream, what);
 }
 
-extern "C" int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
-                               int64_t u_batch, int* status, void* stream) {
-  const char* what = "tqk_fused_apply";
-  int rc = check_state(state, bsz, n, what);
+int apply_entry(const void* in, void* out, int64_t bsz, int n, const int32_t* wires, const void* image,
+                int64_t u_batch, int* status, void* stream, const char* what) {
+  int rc = check_state(in, bsz, n, what);
   if (rc) return rc;
+  if ((rc = check_state(out, bsz, n, what))) return rc;
   if ((rc = check_batch(u_batch, bsz, what))) return rc;
   if (!image || !status) return fail(TQK_BAD_POINTER, "%s: null image/status", what);
   if ((reinterpret_cast<uintptr_t>(image) & 15u) != 0) return fail(TQK_BAD_POINTER, "%s: image alignment", what);
   if (n < 13) return fail(TQK_UNSUPPORTED, "%s: needs n_wires >= 13 (got %d)", what, n);
+  if (overlaps(in, out, bsz * (int64_t(8) << n)))
+    return fail(TQK_BAD_POINTER, "%s: input and output states overlap without being the same buffer", what);
   tc::TcParams p;
-  p.psi = static_cast<float2*>(state);
+  p.psi = const_cast<float2*>(static_cast<const float2*>(in));
+  p.psi_out = static_cast<float2*>(out);
   p.lam = nullptr;
   p.uimg = static_cast<const uint8_t*>(image);
   p.u_batch = u_batch;
@@ -889,4 +960,29 @@ extern "C" int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* w
   p.status = status;
   if ((rc = tc_setup(p, bsz, n, wires, false, what))) return rc;
   return tc_launch(p, false, stream, what);
+}
+
+}  // namespace
+
+extern "C" int tqk_fused_adjoint(void* psi, void* lam, int64_t bsz, int n, const int32_t* wires,
+                                 const void* image_h, int64_t u_batch, double* mr_out, int* status, void* stream) {
+  return adjoint_entry(psi, static_cast<float2*>(psi), lam, bsz, n, wires, image_h, u_batch, mr_out, status, stream,
+                       "tqk_fused_adjoint");
+}
+
+extern "C" int tqk_fused_adjoint_stored(const void* psi_in, void* lam, int64_t bsz, int n, const int32_t* wires,
+                                        const void* image_h, int64_t u_batch, double* mr_out, int* status,
+                                        void* stream) {
+  return adjoint_entry(psi_in, nullptr, lam, bsz, n, wires, image_h, u_batch, mr_out, status, stream,
+                       "tqk_fused_adjoint_stored");
+}
+
+extern "C" int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const void* image,
+                               int64_t u_batch, int* status, void* stream) {
+  return apply_entry(state, state, bsz, n, wires, image, u_batch, status, stream, "tqk_fused_apply");
+}
+
+extern "C" int tqk_fused_apply_to(const void* state_in, void* state_out, int64_t bsz, int n, const int32_t* wires,
+                                  const void* image, int64_t u_batch, int* status, void* stream) {
+  return apply_entry(state_in, state_out, bsz, n, wires, image, u_batch, status, stream, "tqk_fused_apply_to");
 }

@@ -27,11 +27,16 @@ __all__ = ["QuantumDevice"]
 
 
 # Engine settings every new QuantumDevice starts with (``set_engine_defaults``).
-ENGINE_DEFAULTS = {"method": "plain", "fuse_wires": "auto", "fused_backend": "auto", "stage_low": True}
+ENGINE_DEFAULTS = {"method": "plain", "fuse_wires": "auto", "fused_backend": "auto", "stage_low": True,
+                   "checkpoint": "auto"}
+
+# "auto" keeps the inputs of a segment's tensor-core blocks when they fit in this share of
+# the device memory still available (free plus cached by torch)
+CHECKPOINT_MEMORY_SHARE = 0.5
 
 
 def set_engine_defaults(method: Optional[str] = None, fuse_wires=None, fused_backend: Optional[str] = None,
-                        stage_low: Optional[bool] = None) -> dict:
+                        stage_low: Optional[bool] = None, checkpoint=None) -> dict:
     """Set the engine settings of QuantumDevices created from now on -- e.g. the fused
     method for models that build their devices inside ``forward`` -- and return the
     previous defaults (pass them back as keyword arguments to restore them)."""
@@ -50,6 +55,10 @@ def set_engine_defaults(method: Optional[str] = None, fuse_wires=None, fused_bac
         ENGINE_DEFAULTS["fused_backend"] = fused_backend
     if stage_low is not None:
         ENGINE_DEFAULTS["stage_low"] = bool(stage_low)
+    if checkpoint is not None:
+        if checkpoint not in ("auto", True, False):
+            raise ValueError(f"checkpoint must be 'auto', True or False (got {checkpoint!r})")
+        ENGINE_DEFAULTS["checkpoint"] = checkpoint
     return prev
 
 
@@ -74,6 +83,9 @@ class QuantumDevice(nn.Module):
         self.fuse_wires = d["fuse_wires"]        # fused block width 1..6, or "auto" (autotune.choose_fusion)
         self.fused_backend = d["fused_backend"]  # "auto" | "tc" (tensor cores) | "cuda" (CUDA cores)
         self.stage_low = d["stage_low"]          # plain method: runs of low-qubit gates share one pass
+        # fused method: keep each tensor-core block's input state for the backward
+        # ("auto": when a backward may follow and the states fit in memory)
+        self.checkpoint = d["checkpoint"]
         self._tape: List[engine.TapeOp] = []
         self._pending: List[engine.TapeOp] = []   # fused method: recorded, not yet applied
         self._init: Optional[torch.Tensor] = None
@@ -139,9 +151,24 @@ class QuantumDevice(nn.Module):
                 self._buf = self._buf.clone()
                 self._exported = False
             seg = program.Segment(self, ops, self.method)
-            seg.apply(self._buf)
+            self._buf = seg.apply(self._buf, self._store_block_inputs(seg))
             self._tape.append(seg)
             self._out = None
+
+    def _store_block_inputs(self, seg) -> bool:
+        """Whether ``seg``'s tensor-core blocks keep their input states for the backward."""
+        mode = self.checkpoint
+        if mode is False or not seg.blocks or not torch.is_grad_enabled():
+            return False
+        if not any(b.tc for b in seg.blocks):
+            return False
+        if not (seg.diff_inputs or self._init is not None or any(sg.diff_inputs for sg in self._tape)):
+            return False  # no backward will reach this segment
+        if mode is True:
+            return True
+        free, _ = torch.cuda.mem_get_info(self.device)
+        cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
+        return seg.stored_bytes(self._buf) <= CHECKPOINT_MEMORY_SHARE * (free + cached)
 
     def _output(self) -> torch.Tensor:
         """[bsz, 2^n] state as an autograd-connected tensor (cached until the next gate)."""

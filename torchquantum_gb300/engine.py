@@ -9,7 +9,10 @@ to torch autograd as a function of every operand that requires grad.  Its backwa
 is the adjoint method: starting from the final state psi and the incoming cotangent
 lam it walks the tape in reverse, uncomputing psi <- U^H psi and lam <- U^H lam and
 accumulating each operand's cotangent ``sum lam_after conj(psi_before)^T`` in float64
--- two state buffers instead of one saved state per gate.  Torch autograd then
+-- two state buffers instead of one saved state per gate.  Fused tensor-core blocks
+may instead keep their input states (the forward writes each block's output to a new
+buffer, when memory allows): their reverse steps then read the stored input and only
+update lam.  Torch autograd then
 carries the operand cotangents through the differentiable matrix builders
 (``gates.py``) to the gate parameters.
 
@@ -120,20 +123,50 @@ def adjoint_op(psi: torch.Tensor, lam: torch.Tensor, n: int, op: TapeOp, grad: O
         raise ValueError(f"unknown op kind {k}")
 
 
-def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: Optional[torch.Tensor]) -> None:
+def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: Optional[torch.Tensor],
+                     psi_in: Optional[torch.Tensor] = None) -> None:
     """Tensor-core adjoint step of a fused 6-wire block: psi, lam <- U^H (.), and the
     cotangent of U as M U with M = sum over columns of lam conj(psi)^T (U unitary),
-    added into ``grad`` (float64 interleaved view of a complex128 [batch, 64, 64])."""
+    added into ``grad`` (float64 interleaved view of a complex128 [batch, 64, 64]).
+
+    With ``psi_in`` (the state the block was applied to, kept by the forward) psi is not
+    touched: lam <- U^H lam and the cotangent is sum lam conj(psi_in)^T directly."""
     u = kernel_operand(u128)
     img_h = _lib.fused_prepare_adjoint(u, wires)
     mr = None
     if grad is not None:
-        mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=psi.device)
+        mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=lam.device)
+    if psi_in is not None:
+        _lib.fused_adjoint_stored(psi_in, lam, n, wires, img_h, batch, mr)
+        if grad is not None:
+            _lib.fused_cross_grad(mr, None, grad)
+        return
     _lib.fused_adjoint(psi, lam, n, wires, img_h, batch, mr)
     if grad is not None:
         # M carries fp32 accuracy (tensor-memory accumulation), so M U in float32 loses
         # nothing; one kernel adds it into the float64 cotangent
         _lib.fused_cross_grad(mr, u, grad)
+
+
+class StateCursor:
+    """The state a reverse sweep has reached.  It starts as the saved final state and,
+    after a block whose input the forward kept, becomes that stored input: both are only
+    read, so the first step that uncomputes the state in place works on a copy."""
+
+    def __init__(self, state: torch.Tensor):
+        self.state = state
+        self.owned = False
+
+    def writable(self) -> torch.Tensor:
+        if not self.owned:
+            self.state = self.state.clone()
+            self.owned = True
+        return self.state
+
+    def jump(self, stored: torch.Tensor) -> None:
+        """The sweep is now before a block whose stored input is ``stored``."""
+        self.state = stored
+        self.owned = False
 
 
 class CircuitFunction(torch.autograd.Function):
@@ -158,7 +191,7 @@ class CircuitFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out: torch.Tensor):
         (final,) = ctx.saved_tensors
-        psi = final.detach().clone()
+        psi = StateCursor(final.detach())
         lam = kernel_operand(grad_out.to(torch.complex64)).clone()
         per_seg = []
         for sg, cnt in zip(reversed(ctx.segments), reversed(ctx.counts)):

@@ -187,7 +187,8 @@ class Segment:
 
                 with_adj = any(isinstance(r, NativeGate) and r.params.requires_grad for r in records) or \
                     any(not isinstance(r, NativeGate) and r.needs_grad for r in records)
-                plan, tc_flags, k, _ = autotune.choose_fusion(wl, n, self.bsz, dev, tc_ok, with_adj)
+                stored = with_adj and getattr(qdev, "checkpoint", "auto") is not False
+                plan, tc_flags, k, _ = autotune.choose_fusion(wl, n, self.bsz, dev, tc_ok, with_adj, stored=stored)
                 if backend == "tc":
                     tc_flags = [tc_ok for _ in plan]
             else:
@@ -291,33 +292,51 @@ class Segment:
         return self._dummy.data_ptr()
 
     # -------------------------------------------------------------- forward
-    def apply(self, buf: torch.Tensor) -> None:
+    def apply(self, buf: torch.Tensor, store_inputs: bool = False) -> torch.Tensor:
+        """Run the segment on ``buf``; returns the buffer holding the result.  With
+        ``store_inputs`` every tensor-core block writes its output to a new buffer and
+        keeps its input for the backward (``buf`` itself may become one of those stored
+        inputs, so the result is then a different tensor)."""
         _lib.nvtx_push(f"tqk.segment.forward[{len(self.exec_ops)} passes]")
-        self._apply(buf)
-        _lib.nvtx_pop()
+        try:
+            return self._apply(buf, store_inputs)
+        finally:
+            _lib.nvtx_pop()
 
-    def _apply(self, buf: torch.Tensor) -> None:
+    def _apply(self, buf: torch.Tensor, store_inputs: bool) -> torch.Tensor:
         for op in self.exec_ops:
             if isinstance(op, StagedRun):
                 _lib.staged_apply(buf, self.n, op.descs(), op.tile_bits)
             elif getattr(op, "members", None) is not None:
-                if op.tc:
+                if op.tc and store_inputs:
+                    out = torch.empty_like(buf)
+                    _lib.fused_apply_to(buf, out, self.n, op.wires, op.image, op.block_batch)
+                    op.stored_input = buf
+                    buf = out
+                elif op.tc:
                     _lib.fused_apply(buf, self.n, op.wires, op.image, op.block_batch)
                 else:
                     _lib.apply_matrix(buf, self.n, op.wires, op.operand, op.block_batch)
             else:
                 engine.apply_op(buf, self.n, op)
+        return buf
+
+    def stored_bytes(self, state: torch.Tensor) -> int:
+        """Device memory ``apply(..., store_inputs=True)`` keeps for the backward."""
+        return sum(1 for b in self.blocks if b.tc) * state.numel() * state.element_size()
 
     # -------------------------------------------------------------- backward
-    def backward(self, psi: torch.Tensor, lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
-        """Reverse sweep over this segment; returns grads for ``self.diff_inputs``."""
+    def backward(self, psi: "engine.StateCursor", lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
+        """Reverse sweep over this segment (``psi`` at its end on entry, at its start on
+        return; ``lam`` updated in place); returns grads for ``self.diff_inputs``."""
         _lib.nvtx_push(f"tqk.segment.backward[{len(self.exec_ops)} passes]")
         try:
             return self._backward(psi, lam, need_grads)
         finally:
             _lib.nvtx_pop()
 
-    def _backward(self, psi: torch.Tensor, lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
+    def _backward(self, psi: "engine.StateCursor", lam: torch.Tensor,
+                  need_grads: bool) -> List[Optional[torch.Tensor]]:
         dev = self.device
         n = self.n
         opg = torch.zeros_like(self.op128) if (need_grads and self.natives) else None
@@ -336,16 +355,20 @@ class Segment:
                         elif id(m) in gslots:
                             slot = torch.view_as_real(gslots[id(m)]).view(-1)
                     slots.append(slot)
-                _lib.staged_adjoint(psi, lam, n, op.descs(slots), op.tile_bits)
+                _lib.staged_adjoint(psi.writable(), lam, n, op.descs(slots), op.tile_bits)
                 continue
             if getattr(op, "members", None) is not None:
                 slot = None
                 if gu is not None and _block_needs_grad(op):
                     slot = _as_real(gu, op.u128, self.u128)
-                if op.tc:
-                    engine.adjoint_fused_tc(psi, lam, n, op.wires, op.u128, op.block_batch, slot)
+                stored = getattr(op, "stored_input", None) if op.tc else None
+                if stored is not None:
+                    engine.adjoint_fused_tc(None, lam, n, op.wires, op.u128, op.block_batch, slot, psi_in=stored)
+                    psi.jump(stored)
+                elif op.tc:
+                    engine.adjoint_fused_tc(psi.writable(), lam, n, op.wires, op.u128, op.block_batch, slot)
                 else:
-                    _lib.adjoint_matrix(psi, lam, n, op.wires, op.operand, op.block_batch, slot)
+                    _lib.adjoint_matrix(psi.writable(), lam, n, op.wires, op.operand, op.block_batch, slot)
                 continue
             slot = None
             if need_grads:
@@ -353,7 +376,7 @@ class Segment:
                     slot = _as_real(opg, op.op128, self.op128)
                 elif id(op) in gslots:
                     slot = torch.view_as_real(gslots[id(op)]).view(-1)
-            engine.adjoint_op(psi, lam, n, op, slot)
+            engine.adjoint_op(psi.writable(), lam, n, op, slot)
         if not need_grads:
             return [None] * len(self.diff_inputs)
         # block cotangents -> member operand cotangents
