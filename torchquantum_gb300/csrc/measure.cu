@@ -16,6 +16,7 @@ namespace tqk {
 
 constexpr int kMaxStringsPerPass = 8;
 constexpr int kMaxApplyStrings = 64;
+constexpr int kApplyChunk = 8;  // apply_sum partner loads issued together
 
 // Blocks per row for the reduction passes: enough to fill the GPU, bounded so the
 // partials stay small.  Depends only on (bsz, n) so scratch size is a pure function.
@@ -199,21 +200,28 @@ __global__ void __launch_bounds__(256) k_pauli_apply_sum(const ApplySumParams p)
     o0 = lo2(v);
     o1 = hi2(v);
   }
-  // unrolled so that several partner loads are in flight per thread
-#pragma unroll 4
-  for (int s = 0; s < p.ns; ++s) {
-    const float c = __ldg(p.coef + b * p.m + p.col0 + s);
-    const uint64_t x = p.x[s];
-    const float4 w = ld4(row + ((i ^ x) & ~1ull));
-    const bool sw = (x & 1ull) != 0;
-    const float2 src0 = sw ? hi2(w) : lo2(w), src1 = sw ? lo2(w) : hi2(w);
-    const float f0 = c * sgn_parity((i ^ x) & p.z[s]);
-    const float f1 = c * sgn_parity(((i + 1) ^ x) & p.z[s]);
-    const float2 v0 = ipow_mul(p.ny[s], src0), v1 = ipow_mul(p.ny[s], src1);
-    o0.x = fmaf(f0, v0.x, o0.x);
-    o0.y = fmaf(f0, v0.y, o0.y);
-    o1.x = fmaf(f1, v1.x, o1.x);
-    o1.y = fmaf(f1, v1.y, o1.y);
+  // partner loads of up to kApplyChunk strings issued together, then the arithmetic
+  for (int s0 = 0; s0 < p.ns; s0 += kApplyChunk) {
+    float4 w[kApplyChunk];
+#pragma unroll
+    for (int u = 0; u < kApplyChunk; ++u)
+      if (s0 + u < p.ns) w[u] = ld4(row + ((i ^ p.x[s0 + u]) & ~1ull));
+#pragma unroll
+    for (int u = 0; u < kApplyChunk; ++u) {
+      const int s = s0 + u;
+      if (s >= p.ns) break;
+      const float c = __ldg(p.coef + b * p.m + p.col0 + s);
+      const uint64_t x = p.x[s];
+      const bool sw = (x & 1ull) != 0;
+      const float2 src0 = sw ? hi2(w[u]) : lo2(w[u]), src1 = sw ? lo2(w[u]) : hi2(w[u]);
+      const float f0 = c * sgn_parity((i ^ x) & p.z[s]);
+      const float f1 = c * sgn_parity(((i + 1) ^ x) & p.z[s]);
+      const float2 v0 = ipow_mul(p.ny[s], src0), v1 = ipow_mul(p.ny[s], src1);
+      o0.x = fmaf(f0, v0.x, o0.x);
+      o0.y = fmaf(f0, v0.y, o0.y);
+      o1.x = fmaf(f1, v1.x, o1.x);
+      o1.y = fmaf(f1, v1.y, o1.y);
+    }
   }
   st4(orow + i, pack4(o0, o1));
 }
