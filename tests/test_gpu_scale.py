@@ -8,7 +8,9 @@
   method and against complex128 central differences at a reduced size, for the literal
   configuration and for the variant with a per-sample RY input layer; at full size
   (n = 20, bsz = 64, 10 layers, 50 strings) the step's peak device memory stays a small
-  multiple of one state, where per-gate autograd storage would need ~430 states.
+  multiple of one state with the in-place reverse sweep, and one more state per
+  tensor-core block with stored block inputs, where per-gate autograd storage would need
+  ~590 states.
 """
 import numpy as np
 import pytest
@@ -62,7 +64,7 @@ def _vqe(n, bsz, layers, m, seed, per_sample):
     return gates, theta, x, paulis, w
 
 
-def _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, method):
+def _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, method, checkpoint="auto", blocks=None):
     import torchquantum_gb300 as tq
     import torchquantum_gb300.functional as tqf
     from torchquantum_gb300 import workloads as W
@@ -71,6 +73,7 @@ def _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, method):
     q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
     q.method = method
     q.fuse_wires = 6
+    q.checkpoint = checkpoint
     if x is not None:
         xt = torch.tensor(x, device=dev)
         for wi in range(n):
@@ -80,6 +83,9 @@ def _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, method):
     ev = tq.expval_joint_analytical_batch(q, paulis)
     loss = (ev * torch.tensor(w, device=dev)).sum()
     loss.backward()
+    if blocks is not None:
+        blocks.append(sum(1 for sg in q._tape for op in sg.blocks
+                          if getattr(op, "stored_input", None) is not None))
     return loss.item(), th.grad.detach().cpu().numpy()[0]
 
 
@@ -112,16 +118,28 @@ def test_vqe_gradients_vs_plain_and_fd(per_sample):
 
 
 def test_vqe_full_size_memory():
+    """Peak memory of the differentiation workload: the in-place reverse sweep holds a few
+    states whatever the depth; with stored block inputs it holds one more state per
+    tensor-core block, still far below per-gate autograd storage; both give the same loss
+    and gradients."""
     n, bsz, layers = 20, 64, 10
     gates, theta, x, paulis, w = _vqe(n, bsz, layers, 50, seed=9, per_sample=True)
-    torch.cuda.synchronize()
-    torch.cuda.reset_peak_memory_stats()
-    base = torch.cuda.memory_allocated()
-    loss, g = _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, "fused")
-    torch.cuda.synchronize()
-    peak = torch.cuda.max_memory_allocated() - base
     state_bytes = bsz * (1 << n) * 8
-    print(f"differentiation workload n={n} bsz={bsz}: peak {peak / 2**30:.2f} GiB = {peak / state_bytes:.1f} states; "
-          f"per-gate autograd storage ~{len(gates)} states = {len(gates) * state_bytes / 2**30:.0f} GiB")
-    assert np.isfinite(loss) and np.isfinite(g).all() and g.shape == (theta.shape[1],)
-    assert peak < 8 * state_bytes
+    res = {}
+    for mode in (False, True):
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        blocks = []
+        loss, g = _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, "fused", checkpoint=mode, blocks=blocks)
+        torch.cuda.synchronize()
+        peak = torch.cuda.max_memory_allocated() - base
+        print(f"differentiation workload n={n} bsz={bsz} stored inputs={mode}: peak {peak / 2**30:.2f} GiB = "
+              f"{peak / state_bytes:.1f} states ({blocks[0]} stored); per-gate autograd storage ~{len(gates)} "
+              f"states = {len(gates) * state_bytes / 2**30:.0f} GiB")
+        assert np.isfinite(loss) and np.isfinite(g).all() and g.shape == (theta.shape[1],)
+        res[mode] = (loss, g, peak, blocks[0])
+    assert res[False][3] == 0 and res[False][2] < 8 * state_bytes
+    assert res[True][3] > 0 and res[True][2] < (res[True][3] + 8) * state_bytes
+    assert abs(res[True][0] - res[False][0]) < 1e-4 * max(1.0, abs(res[False][0]))
+    assert np.abs(res[True][1] - res[False][1]).max() < 1e-4 * max(1.0, np.abs(res[False][1]).max())
