@@ -237,18 +237,21 @@ def run_ours(args):
     pw = torch.tensor(np.random.default_rng(3).normal(size=(1, 8)), dtype=torch.float32, device=dev)
     theta_dev = torch.tensor(theta_host, device=dev)
 
-    def step(theta, method=args.method):
+    def step(theta, method=args.method, keep=False):
         q = tq.QuantumDevice(n_wires=n, bsz=bsz, device=dev)
         if method == "plain_gate_by_gate":  # the plain method without staged low-qubit runs
             q.stage_low = False
-        if method == "fused":
+        if method in ("fused", "fused_in_place"):
             q.method = "fused"
             q.fuse_wires = args.fuse if args.fuse == "auto" else int(args.fuse)
+            if method == "fused_in_place":  # reverse sweep uncomputes in place: O(1) extra states
+                q.checkpoint = False
         W.apply_circuit(q, gates, theta)
         pr = tq.probs(q)
         ev = tq.expval_joint_analytical_batch(q, paulis)
         (ev * pw).sum().backward()
-        last["q"] = q
+        if keep:
+            last["q"] = q
         return ev, pr
 
     last = {}
@@ -256,11 +259,24 @@ def run_ours(args):
     barrier = R.barrier
 
     th = theta_dev.clone().requires_grad_(True)
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
         th.grad = None
-        step(th)
+        step(th, keep=w == args.warmup - 1)  # the last warm-up step's plan describes the timed steps
+    fusion_info = None
+    if args.method == "fused":
+        segs = last["q"]._tape
+        fusion_info = {"width": [getattr(sg, "fuse_width", None) for sg in segs],
+                       "passes": sum(len(sg.exec_ops) for sg in segs),
+                       "tensor_core_passes": sum(1 for sg in segs for op in sg.exec_ops if getattr(op, "tc", False)),
+                       # tensor-core blocks whose input state the forward kept for the backward
+                       "stored_inputs": sum(1 for sg in segs for op in sg.exec_ops
+                                            if getattr(op, "stored_input", None) is not None),
+                       "chosen_by": "autotuner (measured pass costs)" if args.fuse == "auto" else f"fixed k={args.fuse}"}
+    last.clear()
     torch.cuda.synchronize()
     barrier()
+    torch.cuda.reset_peak_memory_stats(dev)
+    mem0 = torch.cuda.memory_allocated(dev)
     stream = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = _lib.LAUNCHES[0]
@@ -273,17 +289,7 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     launches = _lib.LAUNCHES[0] - launches0
-    fusion_info = None
-    if args.method == "fused":
-        segs = last["q"]._tape
-        fusion_info = {"width": [getattr(sg, "fuse_width", None) for sg in segs],
-                       "passes": sum(len(sg.exec_ops) for sg in segs),
-                       "tensor_core_passes": sum(1 for sg in segs for op in sg.exec_ops if getattr(op, "tc", False)),
-                       # tensor-core blocks whose input state the forward kept for the backward
-                       "stored_inputs": sum(1 for sg in segs for op in sg.exec_ops
-                                            if getattr(op, "stored_input", None) is not None),
-                       "chosen_by": "autotuner (measured pass costs)" if args.fuse == "auto" else f"fixed k={args.fuse}"}
-    last.clear()
+    peak_states = (torch.cuda.max_memory_allocated(dev) - mem0) / (bsz * (8 << n))
     ms = R.max_over_ranks(e0.elapsed_time(e1), dev)
     value = R.job_throughput(bsz * args.steps, world, ms / 1e3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -292,6 +298,7 @@ def run_ours(args):
             "clocks": clk.summary(), "gpu_launches": launches}
     if fusion_info:
         line["config"]["fusion"] = fusion_info
+        line["peak_states"] = peak_states  # device memory of the timed steps, in states
     # gate applications per second (each circuit applies `depth` gates forward and
     # reverses them in the adjoint sweep)
     line["gate_applications_per_s"] = value * args.depth
@@ -300,14 +307,18 @@ def run_ours(args):
 
     _lib.check_status(dev)
     if args.method == "fused" and not args.quick and not args.no_plain:
-        # ---------------- the plain method on the same workload: with staged low-qubit
-        # runs (its default) and strictly gate by gate
-        for variant, key in (("plain", "plain_method"), ("plain_gate_by_gate", "plain_gate_by_gate")):
+        # ---------------- the same fused step with the in-place reverse sweep (O(1) extra
+        # states), and the plain method: with staged low-qubit runs (its default) and
+        # strictly gate by gate
+        for variant, key in (("fused_in_place", "fused_adjoint_in_place"), ("plain", "plain_method"),
+                             ("plain_gate_by_gate", "plain_gate_by_gate")):
             for _ in range(2):
                 th.grad = None
                 step(th, variant)
             torch.cuda.synchronize()
             barrier()
+            torch.cuda.reset_peak_memory_stats(dev)
+            m0 = torch.cuda.memory_allocated(dev)
             e0.record(stream)
             for _ in range(args.steps):
                 th.grad = None
@@ -317,9 +328,12 @@ def run_ours(args):
             ms_plain = R.max_over_ranks(e0.elapsed_time(e1), dev)
             v_plain = R.job_throughput(bsz * args.steps, world, ms_plain / 1e3)
             line[key] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
-                         "gate_applications_per_s": v_plain * args.depth}
+                         "gate_applications_per_s": v_plain * args.depth,
+                         "peak_states": (torch.cuda.max_memory_allocated(dev) - m0) / (bsz * (8 << n))}
         line["fused_speedup_vs_plain"] = value / line["plain_gate_by_gate"]["value"]
         line["fused_speedup_vs_plain_staged"] = value / line["plain_method"]["value"]
+        line["fused_adjoint_in_place"]["speedup_vs_plain"] = \
+            line["fused_adjoint_in_place"]["value"] / line["plain_gate_by_gate"]["value"]
     if not args.quick:
         # ---------------- end to end through the public API with host buffers
         pin_theta = torch.from_numpy(theta_host).pin_memory()

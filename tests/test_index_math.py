@@ -181,3 +181,74 @@ def test_dense_k_groups_per_block_fit_shared_memory():
         gpb = 1 if D >= 256 else 256 // D
         assert gpb * D <= 16 * 256
         assert gpb * D * 8 <= 200 * 1024
+
+
+def _popc(v):
+    return bin(int(v)).count("1")
+
+
+def _pauli_apply(psi, x, z):
+    """(P psi)[i] = i^ny (-1)^popcount((i ^ x) & z) psi[i ^ x], ny = popcount(x & z) mod 4."""
+    ph = [1, 1j, -1, -1j][_popc(x & z) & 3]
+    return [ph * (-1) ** _popc((i ^ x) & z) * psi[i ^ x] for i in range(len(psi))]
+
+
+def test_expval_pass_sign_algebra():
+    """The per-pass formulas of k_expval_diag / k_expval_pair (one popcount per string for
+    two pairs, sign of the partner from ny, of the odd index from z & 1) against
+    <psi|P|psi> computed directly."""
+    import numpy as np
+
+    rng = np.random.default_rng(0)
+    n = 1 << 6
+    for trial in range(200):
+        psi = rng.normal(size=n) + 1j * rng.normal(size=n)
+        x = 0 if trial % 5 == 0 else 1 if trial % 7 == 0 else int(rng.integers(0, n))
+        z = int(rng.integers(0, n))
+        ny = _popc(x & z) & 3
+        f, z0 = (1 if ny < 2 else -1), (-1 if z & 1 else 1)
+        acc = 0.0
+        if x == 0:
+            for i in range(0, n, 2):
+                acc += (-1) ** _popc(i & z) * (abs(psi[i]) ** 2 + z0 * abs(psi[i + 1]) ** 2)
+        elif x == 1:
+            for i in range(0, n, 2):
+                u = np.conj(psi[i]) * psi[i + 1]
+                acc += 2 * f * (-1) ** _popc(i & z) * (u.imag if ny & 1 else u.real)
+        else:
+            hb = x.bit_length() - 1
+            for t in range(n // 4):
+                g = 2 * t
+                i = ((g >> hb) << (hb + 1)) | (g & ((1 << hb) - 1))
+                u0 = np.conj(psi[i]) * psi[i ^ x]
+                u1 = np.conj(psi[i + 1]) * psi[(i + 1) ^ x]
+                c = (u0.imag + z0 * u1.imag) if ny & 1 else (u0.real + z0 * u1.real)
+                acc += 2 * f * (-1) ** _popc(i & z) * c
+        want = np.vdot(psi, _pauli_apply(psi, x, z)).real
+        assert abs(acc - want) < 1e-10, (x, z)
+
+
+def test_apply_sum_sign_algebra():
+    """k_pauli_apply_sum's per-string step (sign from one popcount plus ny >> 1, quarter
+    turn for odd ny, odd index flipped by z & 1) against sum_s c_s P_s psi."""
+    import numpy as np
+
+    rng = np.random.default_rng(1)
+    n = 1 << 6
+    for _ in range(40):
+        psi = rng.normal(size=n) + 1j * rng.normal(size=n)
+        k = int(rng.integers(1, 9))
+        xs, zs, cs = rng.integers(0, n, k), rng.integers(0, n, k), rng.normal(size=k)
+        got = np.zeros(n, complex)
+        for t in range(n // 2):
+            i = 2 * t
+            for x, z, c in zip(xs, zs, cs):
+                x, z = int(x), int(z)
+                ny = _popc(x & z) & 3
+                c0 = c * (-1) ** (_popc((i ^ x) & z) + (ny >> 1))
+                c1 = -c0 if z & 1 else c0
+                rot = 1j if ny & 1 else 1
+                got[i] += c0 * rot * psi[i ^ x]
+                got[i + 1] += c1 * rot * psi[(i + 1) ^ x]
+        want = sum(c * np.array(_pauli_apply(psi, int(x), int(z))) for x, z, c in zip(xs, zs, cs))
+        assert np.abs(got - want).max() < 1e-10

@@ -63,71 +63,106 @@ struct ExpvalParams {
   double* partial;                // [bsz][gridDim.x][m]
 };
 
-__device__ __forceinline__ float sgn_parity(uint64_t v) { return (__popcll(v) & 1) ? -1.f : 1.f; }
 
-__device__ __forceinline__ float pair_term(float2 a, float2 ap, uint64_t i, uint64_t ip, uint64_t z, int ny) {
-  // u = conj(a) * ap
-  const float ur = a.x * ap.x + a.y * ap.y;
-  const float ui = a.x * ap.y - a.y * ap.x;
-  const float sa = sgn_parity(ip & z), sb = sgn_parity(i & z);
-  switch (ny) {
-    case 0: return (sa + sb) * ur;
-    case 1: return (sb - sa) * ui;
-    case 2: return -(sa + sb) * ur;
-    default: return (sa - sb) * ui;
-  }
+// Sign algebra of one pass.  All strings of a pass share the X-mask x; the pass visits
+// even indices i (bit 0 clear) and their partners i ^ x.  Per string (z its Z-mask, ny
+// its number of Y factors mod 4, so popcount(x & z) = ny mod 2):
+//   (-1)^popcount((i ^ x) & z)       = (-1)^popcount(i & z) * (-1)^ny,
+//   (-1)^popcount(((i + 1) ^ x) & z) = (-1)^popcount((i ^ x) & z) * (-1)^(z & 1).
+// The pair (a = psi[i], b = psi[i ^ x]) contributes conj(a) (P psi)_i + conj(b) (P psi)_{i^x}
+//   = 2 (-1)^popcount(i & z) F[ny] * (ny odd ? Im : Re)(conj(a) b),  F = (1, 1, -1, -1),
+// so a pass needs one popcount per string for two pairs instead of four.
+__device__ __forceinline__ float flip_if_odd(float v, uint32_t parity_bits) {  // v * (-1)^popcount
+  return __int_as_float(__float_as_int(v) ^ static_cast<int>(parity_bits << 31));
 }
+template <typename I>
+__device__ __forceinline__ uint32_t popc_t(I v) {
+  if constexpr (sizeof(I) == 8) return static_cast<uint32_t>(__popcll(v));
+  else return static_cast<uint32_t>(__popc(v));
+}
+
+// Per-string constants of a pass, kept in registers.
+template <int NS, typename I>
+struct PassStrings {
+  I z[NS];
+  float f[NS];       // 2 F[ny] (diagonal pass: 1)
+  uint32_t odd[NS];  // ny odd: take the imaginary part
+  float z0[NS];      // (-1)^(z & 1)
+  __device__ __forceinline__ void load(const ExpvalParams& p, float scale) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const int ny = s < p.ns ? p.ny[s] : 0;
+      z[s] = s < p.ns ? static_cast<I>(p.z[s]) : I(0);
+      f[s] = ny >= 2 ? -scale : scale;
+      odd[s] = static_cast<uint32_t>(ny & 1);
+      z0[s] = (z[s] & I(1)) ? -1.f : 1.f;
+    }
+  }
+};
 
 // x == 0: diagonal strings, contribution |psi_i|^2 * (-1)^{popcount(i & z)}
 // NS: strings the pass's accumulators hold (1, 2, 4 or 8 >= p.ns): fewer registers for
 // the common one-string pass, so more warps -- more loads in flight -- per SM.
-template <int NS>
+// I: index type (32-bit for rows of up to 2^31 amplitudes).
+template <int NS, typename I>
 __global__ void __launch_bounds__(256) k_expval_diag(const ExpvalParams p) {
   const int64_t b = blockIdx.y;
   const float2* row = p.state + (b << p.n);
+  PassStrings<NS, I> ps;
+  ps.load(p, 1.f);
   float acc[NS];
 #pragma unroll
   for (int s = 0; s < NS; ++s) acc[s] = 0.f;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < p.work; t += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t i = (uint64_t)t * 2;
+  const I work = static_cast<I>(p.work), stride = static_cast<I>(gridDim.x * blockDim.x);
+  for (I t = static_cast<I>(blockIdx.x * blockDim.x + threadIdx.x); t < work; t += stride) {
+    const I i = t * 2;
     const float4 v = ld4(row + i);
     const float p0 = v.x * v.x + v.y * v.y, p1 = v.z * v.z + v.w * v.w;
 #pragma unroll
     for (int s = 0; s < NS; ++s)
-      if (s < p.ns) acc[s] += sgn_parity(i & p.z[s]) * p0 + sgn_parity((i + 1) & p.z[s]) * p1;
+      if (s < p.ns) acc[s] += flip_if_odd(fmaf(ps.z0[s], p1, p0), popc_t<I>(i & ps.z[s]));
   }
   block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
 }
 
 // x != 0: pairs (i, i^x) with bit hbit of i clear.
-template <bool LOWX, int NS>  // LOWX: x == 1 (the pair is one float4)
+template <bool LOWX, int NS, typename I>  // LOWX: x == 1 (the pair is one float4)
 __global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
   const int64_t b = blockIdx.y;
   const float2* row = p.state + (b << p.n);
+  PassStrings<NS, I> ps;
+  ps.load(p, 2.f);
   float acc[NS];
 #pragma unroll
   for (int s = 0; s < NS; ++s) acc[s] = 0.f;
-  const uint64_t lomask = (1ull << p.hbit) - 1ull;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < p.work; t += (int64_t)gridDim.x * blockDim.x) {
+  const I x = static_cast<I>(p.x);
+  const int hb = p.hbit;
+  const I lomask = (I(1) << hb) - I(1);
+  const bool sw = (x & I(1)) != 0;
+  const I work = static_cast<I>(p.work), stride = static_cast<I>(gridDim.x * blockDim.x);
+  for (I t = static_cast<I>(blockIdx.x * blockDim.x + threadIdx.x); t < work; t += stride) {
     if (LOWX) {
-      const uint64_t i = (uint64_t)t * 2;  // i has bit 0 clear, partner i+1
+      const I i = t * 2;  // bit 0 clear, partner i + 1
       const float4 v = ld4(row + i);
+      const float ur = v.x * v.z + v.y * v.w, ui = v.x * v.w - v.y * v.z;  // conj(a) b
 #pragma unroll
       for (int s = 0; s < NS; ++s)
-        if (s < p.ns) acc[s] += pair_term(lo2(v), hi2(v), i, i + 1, p.z[s], p.ny[s]);
+        if (s < p.ns) acc[s] += flip_if_odd(ps.f[s] * (ps.odd[s] ? ui : ur), popc_t<I>(i & ps.z[s]));
     } else {
-      const uint64_t g = (uint64_t)t * 2;  // two consecutive groups: i, i+1 (hbit >= 1)
-      const uint64_t i = ((g >> p.hbit) << (p.hbit + 1)) | (g & lomask);
-      const uint64_t ip = i ^ p.x;
+      const I g = t * 2;  // two consecutive groups: i, i + 1 (hbit >= 1, so i is even)
+      const I i = ((g >> hb) << (hb + 1)) | (g & lomask);
       const float4 v = ld4(row + i);
-      const float4 w = ld4(row + (ip & ~1ull));
-      const bool sw = (p.x & 1ull) != 0;
+      const float4 w = ld4(row + ((i ^ x) & ~I(1)));
       const float2 a0 = lo2(v), a1 = hi2(v);
       const float2 b0 = sw ? hi2(w) : lo2(w), b1 = sw ? lo2(w) : hi2(w);
+      const float ur0 = a0.x * b0.x + a0.y * b0.y, ui0 = a0.x * b0.y - a0.y * b0.x;
+      const float ur1 = a1.x * b1.x + a1.y * b1.y, ui1 = a1.x * b1.y - a1.y * b1.x;
 #pragma unroll
       for (int s = 0; s < NS; ++s)
-        if (s < p.ns)
-          acc[s] += pair_term(a0, b0, i, ip, p.z[s], p.ny[s]) + pair_term(a1, b1, i + 1, ip ^ 1ull, p.z[s], p.ny[s]);
+        if (s < p.ns) {
+          const float c = ps.odd[s] ? fmaf(ps.z0[s], ui1, ui0) : fmaf(ps.z0[s], ur1, ur0);
+          acc[s] += flip_if_odd(ps.f[s] * c, popc_t<I>(i & ps.z[s]));
+        }
     }
   }
   block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
@@ -136,18 +171,24 @@ __global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
 // The two kernels above store block partials contiguously as [row][block][slot];
 // this kernel reduces them in block order into out[row*m + col].
 // Launch the pass kernel with the smallest accumulator count that holds p.ns strings.
-template <int NS>
+template <int NS, typename I>
 void launch_expval_ns(const ExpvalParams& p, dim3 grid, cudaStream_t st) {
-  if (p.x == 0) k_expval_diag<NS><<<grid, 256, 0, st>>>(p);
-  else if (p.x == 1ull) k_expval_pair<true, NS><<<grid, 256, 0, st>>>(p);
-  else k_expval_pair<false, NS><<<grid, 256, 0, st>>>(p);
+  if (p.x == 0) k_expval_diag<NS, I><<<grid, 256, 0, st>>>(p);
+  else if (p.x == 1ull) k_expval_pair<true, NS, I><<<grid, 256, 0, st>>>(p);
+  else k_expval_pair<false, NS, I><<<grid, 256, 0, st>>>(p);
+}
+
+template <typename I>
+void launch_expval_i(const ExpvalParams& p, dim3 grid, cudaStream_t st) {
+  if (p.ns <= 1) launch_expval_ns<1, I>(p, grid, st);
+  else if (p.ns <= 2) launch_expval_ns<2, I>(p, grid, st);
+  else if (p.ns <= 4) launch_expval_ns<4, I>(p, grid, st);
+  else launch_expval_ns<8, I>(p, grid, st);
 }
 
 inline void launch_expval(const ExpvalParams& p, dim3 grid, cudaStream_t st) {
-  if (p.ns <= 1) launch_expval_ns<1>(p, grid, st);
-  else if (p.ns <= 2) launch_expval_ns<2>(p, grid, st);
-  else if (p.ns <= 4) launch_expval_ns<4>(p, grid, st);
-  else launch_expval_ns<8>(p, grid, st);
+  if (p.n <= 31) launch_expval_i<uint32_t>(p, grid, st);
+  else launch_expval_i<uint64_t>(p, grid, st);
 }
 
 struct FinishCols {
@@ -177,23 +218,17 @@ struct ApplySumParams {
   int accumulate;
 };
 
-__device__ __forceinline__ float2 ipow_mul(int ny, float2 v) {  // i^ny * v
-  switch (ny) {
-    case 0: return v;
-    case 1: return make_float2(-v.y, v.x);
-    case 2: return make_float2(-v.x, -v.y);
-    default: return make_float2(v.y, -v.x);
-  }
-}
-
+// out[i] (+)= sum_s c_s (P_s psi)[i], (P_s psi)[i] = i^ny (-1)^popcount((i ^ x) & z) psi[i ^ x]
+// (the sign algebra above: one popcount per string for the two outputs of a thread).
+template <typename I>
 __global__ void __launch_bounds__(256) k_pauli_apply_sum(const ApplySumParams p) {
   const int64_t b = blockIdx.y;
-  const int64_t half = (1ll << p.n) >> 1;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const I half = static_cast<I>((1ll << p.n) >> 1);
+  const I t = static_cast<I>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= half) return;
   const float2* row = p.state + (b << p.n);
   float2* orow = p.out + (b << p.n);
-  const uint64_t i = (uint64_t)t * 2;
+  const I i = t * 2;
   float2 o0 = make_float2(0.f, 0.f), o1 = make_float2(0.f, 0.f);
   if (p.accumulate) {
     const float4 v = ld4(orow + i);
@@ -205,22 +240,30 @@ __global__ void __launch_bounds__(256) k_pauli_apply_sum(const ApplySumParams p)
     float4 w[kApplyChunk];
 #pragma unroll
     for (int u = 0; u < kApplyChunk; ++u)
-      if (s0 + u < p.ns) w[u] = ld4(row + ((i ^ p.x[s0 + u]) & ~1ull));
+      if (s0 + u < p.ns) w[u] = ld4(row + ((i ^ static_cast<I>(p.x[s0 + u])) & ~I(1)));
 #pragma unroll
     for (int u = 0; u < kApplyChunk; ++u) {
       const int s = s0 + u;
       if (s >= p.ns) break;
-      const float c = __ldg(p.coef + b * p.m + p.col0 + s);
-      const uint64_t x = p.x[s];
-      const bool sw = (x & 1ull) != 0;
+      const I x = static_cast<I>(p.x[s]), z = static_cast<I>(p.z[s]);
+      const int ny = p.ny[s];
+      const bool sw = (x & I(1)) != 0;
       const float2 src0 = sw ? hi2(w[u]) : lo2(w[u]), src1 = sw ? lo2(w[u]) : hi2(w[u]);
-      const float f0 = c * sgn_parity((i ^ x) & p.z[s]);
-      const float f1 = c * sgn_parity(((i + 1) ^ x) & p.z[s]);
-      const float2 v0 = ipow_mul(p.ny[s], src0), v1 = ipow_mul(p.ny[s], src1);
-      o0.x = fmaf(f0, v0.x, o0.x);
-      o0.y = fmaf(f0, v0.y, o0.y);
-      o1.x = fmaf(f1, v1.x, o1.x);
-      o1.y = fmaf(f1, v1.y, o1.y);
+      // i^ny: a quarter turn for odd ny, a sign for ny >= 2 (folded into the parity)
+      const float c0 = flip_if_odd(__ldg(p.coef + b * p.m + p.col0 + s),
+                                   popc_t<I>((i ^ x) & z) + static_cast<uint32_t>(ny >> 1));
+      const float c1 = (z & I(1)) ? -c0 : c0;
+      if (ny & 1) {
+        o0.x = fmaf(-c0, src0.y, o0.x);
+        o0.y = fmaf(c0, src0.x, o0.y);
+        o1.x = fmaf(-c1, src1.y, o1.x);
+        o1.y = fmaf(c1, src1.x, o1.y);
+      } else {
+        o0.x = fmaf(c0, src0.x, o0.x);
+        o0.y = fmaf(c0, src0.y, o0.y);
+        o1.x = fmaf(c1, src1.x, o1.x);
+        o1.y = fmaf(c1, src1.y, o1.y);
+      }
     }
   }
   st4(orow + i, pack4(o0, o1));
@@ -344,7 +387,8 @@ extern "C" int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const 
     p.accumulate = j0 > 0;
     const int threads = threads_for(half);
     dim3 grid((unsigned)((half + threads - 1) / threads), (unsigned)bsz, 1);
-    k_pauli_apply_sum<<<grid, threads, 0, st>>>(p);
+    if (n <= 31) k_pauli_apply_sum<uint32_t><<<grid, threads, 0, st>>>(p);
+    else k_pauli_apply_sum<uint64_t><<<grid, threads, 0, st>>>(p);
     if ((rc = launch_status(what))) return rc;
   }
   return TQK_OK;
