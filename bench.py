@@ -432,8 +432,10 @@ def roofline(args, dev, stored=True):
     tb = min(n, _lib.STAGED_MAX_TILE_BITS)
     kernels["staged8_fwd"] = (lambda i: _lib.staged_apply(psi, n, sdescs, tb), 2 * S)
     kernels["staged8_adj"] = (lambda i: _lib.staged_adjoint(psi, lam, n, sdescs_g, tb), 4 * S)
-    # the bench step's measurement kernels: 8 Pauli expvals (one pass per X-mask: 8 S read)
-    # and the backward seed sum_j c_j P_j psi (8 partner reads + 1 write: 9 S)
+    # the bench step's measurement kernels: 8 Pauli expvals (rows of up to 2^24 amplitudes:
+    # one row sweep, own + 8 partner loads per amplitude = 9 S loaded, mostly from L2;
+    # longer rows: one pass per X-mask, 8 S read) and the backward seed sum_j c_j P_j psi
+    # (8 partner reads + 1 write: 9 S)
     from torchquantum_gb300.measurement import pauli_masks
     from torchquantum_gb300 import workloads as W
 
@@ -441,8 +443,8 @@ def roofline(args, dev, stored=True):
     xs = [pauli_masks(o, n)[0] for o in strings]
     zs = [pauli_masks(o, n)[1] for o in strings]
     coef = torch.ones(bsz, 8, dtype=torch.float32, device=dev)
-    npass = len(set(xs))
-    kernels["expval8"] = (lambda i: _lib.pauli_expval(psi, n, xs, zs), npass * S)
+    rows = n <= _lib.ROWS_MAX_WIRES and len(set(xs)) > 1
+    kernels["expval8"] = (lambda i: _lib.pauli_expval(psi, n, xs, zs), (1 + len(xs)) * S if rows else len(set(xs)) * S)
     kernels["apply_sum8"] = (lambda i: _lib.pauli_apply_sum(psi, n, xs, zs, coef), 9 * S)
     for name, (fn, nbytes) in kernels.items():
         t = timeit(fn)

@@ -99,3 +99,36 @@ def test_reset_vs_oracle():
     tqf.reset(q, wires=[1, 4])
     ref = O.reset(s, [1, 4], n)
     assert np.abs(q.get_states_1d().cpu().numpy() - ref).max() < 1e-5
+
+
+@pytest.mark.parametrize("n,bsz,m", [(6, 5, 3), (10, 3, 20), (14, 2, 17), (22, 2, 9), (24, 1, 9)])
+def test_row_sweep_expvals(n, bsz, m):
+    """Strings with several X-masks at n <= 24 take the row sweep (k_expval_rows: every
+    string's partner read per amplitude pair, rows one after another): against the oracle
+    where it is cheap, and against the per-X-mask passes of the no-allocation entry point
+    at every size, including diagonal strings, X-mask 1 and chunks of 8 with a remainder."""
+    import ctypes
+
+    from torchquantum_gb300 import _lib
+    from torchquantum_gb300.measurement import pauli_masks
+
+    rng = np.random.default_rng(40 + n)
+    strings = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(m - 2)]
+    strings += ["Z" * n, "I" * (n - 1) + "Y"]
+    xs, zs = zip(*[pauli_masks(p, n) for p in strings])
+    assert len(set(xs)) > 1 and _lib.expval_passes(list(xs), n) == (m + 7) // 8
+    s = rng.normal(size=(bsz, 1 << n)) + 1j * rng.normal(size=(bsz, 1 << n))
+    s /= np.linalg.norm(s, axis=1, keepdims=True)
+    st = torch.tensor(s, dtype=torch.complex64, device="cuda")
+    got = _lib.pauli_expval(st, n, list(xs), list(zs))
+    lib = _lib.load()
+    ref = torch.full((bsz, m), float("nan"), dtype=torch.float64, device="cuda")
+    rc = lib.tqk_pauli_expval_noalloc(st.data_ptr(), bsz, n, _lib._u64(list(xs)), _lib._u64(list(zs)), m,
+                                      ref.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, lib.tqk_last_error().decode()
+    torch.cuda.synchronize()
+    assert (got - ref).abs().max().item() < 2e-6
+    if n <= 14:
+        s64 = st.cpu().numpy().astype(np.complex128)
+        want = np.stack([O.expval_pauli(s64, p, n) for p in strings], -1)
+        assert np.abs(got.cpu().numpy() - want).max() < 1e-6

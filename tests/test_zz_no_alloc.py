@@ -46,7 +46,9 @@ def test_noalloc_matches_scratch_entry_point_twice(n, bsz, m):
         got = _noalloc(lib, st, n, list(xs), list(zs))
         torch.cuda.synchronize()
         assert not torch.isnan(got).any()
-        assert (got - ref).abs().max().item() < 1e-12, call
+        # the scratch entry point sweeps whole rows for several X-masks (n <= 24), this
+        # one makes a pass per X-mask: the same sums in a different float32 order
+        assert (got - ref).abs().max().item() < 2e-6, call
 
 
 def test_noalloc_rejects_oversized_calls():

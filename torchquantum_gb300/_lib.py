@@ -199,8 +199,15 @@ def probs(state, n):
     return out
 
 
-def expval_passes(xmasks) -> int:
-    """Passes tqk_pauli_expval makes: strings grouped by xmask, at most 8 per pass."""
+ROWS_MAX_WIRES = 24  # tqk_pauli_expval sweeps rows of up to 2^24 amplitudes through L2
+
+
+def expval_passes(xmasks, n: int = 64) -> int:
+    """Passes tqk_pauli_expval makes: with several X-masks and rows of at most 2^24
+    amplitudes, one row sweep per 8 strings; otherwise strings grouped by X-mask, at most
+    8 per pass."""
+    if n <= ROWS_MAX_WIRES and len(set(xmasks)) > 1:
+        return (len(xmasks) + 7) // 8
     counts = {}
     for x in xmasks:
         counts[x] = counts.get(x, 0) + 1
@@ -216,7 +223,7 @@ def pauli_expval(state, n, xmasks, zmasks):
     nbytes = lib.tqk_pauli_expval_scratch_bytes(bsz, n, m)
     scratch = torch.empty(max(8, nbytes), dtype=torch.uint8, device=state.device)
     _check(lib.tqk_pauli_expval(state.data_ptr(), bsz, n, _u64(xmasks), _u64(zmasks), m, out.data_ptr(),
-                                scratch.data_ptr(), nbytes, _stream(state)), launches=2 * expval_passes(xmasks))
+                                scratch.data_ptr(), nbytes, _stream(state)), launches=2 * expval_passes(xmasks, n))
     return out
 
 

@@ -168,6 +168,101 @@ __global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
   block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
 }
 
+// Strings with different X-masks in one launch, the rows swept one after another by the
+// whole grid.  While a row of up to kRowsMaxAmps amplitudes is being swept it stays in L2,
+// so the partner reads psi[i ^ x_s] of every string are served from L2 and each row is
+// read from DRAM about once -- one pass per X-mask reads it once per mask.  Each thread
+// takes the two amplitudes i, i + 1 and adds Re(conj(psi_j) (P_s psi)_j) for both:
+//   (P psi)_j = i^ny (-1)^popcount((j ^ x) & z) psi_{j ^ x},
+// with the sign of j = i + 1 that of j = i times (-1)^(z & 1), and Re(i^ny u) = u_r, -u_i,
+// -u_r, u_i for ny = 0..3 (one popcount per string per thread).
+constexpr int kRowsBlocks = 152 * 4;             // CTAs of the row sweep (partials per row)
+constexpr int64_t kRowsMaxAmps = 1ll << 24;       // rows of up to 128 MB (about the L2)
+
+struct RowsParams {
+  const float2* state;
+  int n;
+  int ns;
+  int64_t bsz;
+  uint64_t x[kMaxStringsPerPass], z[kMaxStringsPerPass];
+  int ny[kMaxStringsPerPass];
+  double* partial;  // [bsz][gridDim.x][kMaxStringsPerPass]
+};
+
+template <int NS, typename I>
+__global__ void __launch_bounds__(256) k_expval_rows(const RowsParams p) {
+  I xs[NS], zs[NS];
+  float z0[NS];
+  uint32_t ny[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    xs[s] = s < p.ns ? static_cast<I>(p.x[s]) : I(0);
+    zs[s] = s < p.ns ? static_cast<I>(p.z[s]) : I(0);
+    z0[s] = (zs[s] & I(1)) ? -1.f : 1.f;
+    ny[s] = s < p.ns ? static_cast<uint32_t>(p.ny[s]) : 0u;
+  }
+  const I half = static_cast<I>((1ll << p.n) >> 1);
+  const I stride = static_cast<I>(gridDim.x * blockDim.x);
+  for (int64_t b = 0; b < p.bsz; ++b) {
+    const float2* row = p.state + (b << p.n);
+    float acc[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) acc[s] = 0.f;
+    for (I t = static_cast<I>(blockIdx.x * blockDim.x + threadIdx.x); t < half; t += stride) {
+      const I i = t * 2;
+      const float4 v = ld4(row + i);
+      float4 w[NS];
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+        if (s < p.ns) w[s] = ld4(row + ((i ^ xs[s]) & ~I(1)));
+      const float2 a0 = lo2(v), a1 = hi2(v);
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+        if (s < p.ns) {
+          const bool sw = (xs[s] & I(1)) != 0;
+          const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
+          const float ur = fmaf(z0[s], a1.x * b1.x + a1.y * b1.y, a0.x * b0.x + a0.y * b0.y);
+          const float ui = fmaf(z0[s], a1.x * b1.y - a1.y * b1.x, a0.x * b0.y - a0.y * b0.x);
+          const uint32_t neg = ((ny[s] + 1u) >> 1) & 1u;  // ny = 1, 2
+          acc[s] += flip_if_odd((ny[s] & 1u) ? ui : ur, popc_t<I>((i ^ xs[s]) & zs[s]) + neg);
+        }
+    }
+    block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
+    __syncthreads();  // the reduction's shared buffer is reused for the next row
+  }
+}
+
+// CTAs of the row sweep for rows of 2^n amplitudes (0: rows too long to stay in L2).
+static int64_t rows_blocks(int n) {
+  const int64_t amps = 1ll << n;
+  if (amps > kRowsMaxAmps) return 0;
+  const int64_t cap = (amps / 2 + 255) / 256;
+  return cap < kRowsBlocks ? cap : kRowsBlocks;
+}
+
+// Launch with every CTA resident at once (a CTA of a second wave would start the first
+// row after the others finished the last one); returns the grid size (partials per row).
+template <int NS, typename I>
+unsigned launch_rows_ns(const RowsParams& p, int64_t max_blocks, cudaStream_t st) {
+  int dev = 0, sms = 0, fit = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_expval_rows<NS, I>, 256, 0) != cudaSuccess || fit < 1)
+    fit = 1;
+  int64_t grid = static_cast<int64_t>(sms) * fit;
+  if (grid > max_blocks) grid = max_blocks;
+  k_expval_rows<NS, I><<<static_cast<unsigned>(grid), 256, 0, st>>>(p);
+  return static_cast<unsigned>(grid);
+}
+
+template <typename I>
+unsigned launch_rows(const RowsParams& p, int64_t max_blocks, cudaStream_t st) {
+  if (p.ns <= 1) return launch_rows_ns<1, I>(p, max_blocks, st);
+  if (p.ns <= 2) return launch_rows_ns<2, I>(p, max_blocks, st);
+  if (p.ns <= 4) return launch_rows_ns<4, I>(p, max_blocks, st);
+  return launch_rows_ns<8, I>(p, max_blocks, st);
+}
+
 // The two kernels above store block partials contiguously as [row][block][slot];
 // this kernel reduces them in block order into out[row*m + col].
 // Launch the pass kernel with the smallest accumulator count that holds p.ns strings.
@@ -295,7 +390,9 @@ extern "C" int tqk_probs(const void* state, int64_t bsz, int n, float* out, void
 extern "C" int64_t tqk_pauli_expval_scratch_bytes(int64_t bsz, int n, int m) {
   // partials [bsz][nblk][kMaxStringsPerPass] per pass (passes reuse the region; the
   // stream orders them)
-  const int64_t nblk = reduce_blocks_per_row(bsz, n);
+  int64_t nblk = reduce_blocks_per_row(bsz, n);
+  const int64_t rb = rows_blocks(n);  // the row sweep's partials, when it may be used
+  if (rb > nblk) nblk = rb;
   (void)m;
   return bsz * nblk * kMaxStringsPerPass * (int64_t)sizeof(double);
 }
@@ -316,6 +413,35 @@ extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uin
   cudaStream_t st = as_stream(stream);
   const int64_t nblk = reduce_blocks_per_row(bsz, n);
   double* partial = static_cast<double*>(scratch);
+  // several X-masks and rows that stay in L2: sweep the rows once per 8 strings
+  const int64_t rb = rows_blocks(n);
+  bool several = false;
+  for (int j = 1; j < m && !several; ++j) several = xmask[j] != xmask[0];
+  if (rb > 0 && several) {
+    for (int j0 = 0; j0 < m; j0 += kMaxStringsPerPass) {
+      RowsParams p;
+      p.state = static_cast<const float2*>(state);
+      p.n = n;
+      p.bsz = bsz;
+      p.partial = partial;
+      p.ns = (m - j0) < kMaxStringsPerPass ? (m - j0) : kMaxStringsPerPass;
+      FinishCols cols;
+      for (int s = 0; s < kMaxStringsPerPass; ++s) {
+        const bool on = s < p.ns;
+        p.x[s] = on ? xmask[j0 + s] : 0;
+        p.z[s] = on ? zmask[j0 + s] : 0;
+        p.ny[s] = on ? __builtin_popcountll(xmask[j0 + s] & zmask[j0 + s]) & 3 : 0;
+        cols.c[s] = on ? j0 + s : 0;
+      }
+      const unsigned grid = n <= 31 ? launch_rows<uint32_t>(p, rb, st) : launch_rows<uint64_t>(p, rb, st);
+      if ((rc = launch_status(what))) return rc;
+      const int64_t nout = bsz * p.ns;
+      k_expval_finish<<<(unsigned)((nout + 127) / 128), 128, 0, st>>>(partial, grid, p.ns, kMaxStringsPerPass,
+                                                                        cols, m, out, bsz);
+      if ((rc = launch_status(what))) return rc;
+    }
+    return TQK_OK;
+  }
   std::vector<int> done(m, 0);
   for (int j0 = 0; j0 < m; ++j0) {
     if (done[j0]) continue;
