@@ -195,3 +195,30 @@ def test_auto_mode_stores_only_when_needed(monkeypatch):
         assert not any(stored_blocks(True))
     monkeypatch.setattr(D, "CHECKPOINT_MEMORY_SHARE", 0.0)
     assert not any(stored_blocks(True))
+
+
+def test_out_of_memory_midway_falls_back_in_place(monkeypatch):
+    """When a stored input cannot be allocated the segment runs its remaining blocks in
+    place; the reverse sweep then mixes stored-input steps and in-place steps and still
+    gives the in-place sweep's state and gradients."""
+    from torchquantum_gb300 import program as P
+    from torchquantum_gb300 import workloads as W
+
+    n, bsz = 14, 2
+    gates, ncols = W.random_circuit(n, 160, seed=21)
+    theta = W.random_params(bsz, ncols, seed=22)
+    paulis = W.random_paulis(n, 4, seed=23)
+    _, s0, g0 = _circuit_run(n, bsz, gates, theta, paulis, False)
+    real = P._new_state
+    calls = {"n": 0}
+
+    def limited(like):
+        calls["n"] += 1
+        return real(like) if calls["n"] <= 3 else None
+
+    monkeypatch.setattr(P, "_new_state", limited)
+    q, s1, g1 = _circuit_run(n, bsz, gates, theta, paulis, True, retain=True)
+    flags = [getattr(op, "stored_input", None) is not None for sg in q._tape for op in sg.blocks if op.tc]
+    assert sum(flags) == 3 and len(flags) > 3
+    assert np.array_equal(s1, s0)
+    assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())

@@ -308,8 +308,12 @@ class Segment:
             if isinstance(op, StagedRun):
                 _lib.staged_apply(buf, self.n, op.descs(), op.tile_bits)
             elif getattr(op, "members", None) is not None:
+                out = None
                 if op.tc and store_inputs:
-                    out = torch.empty_like(buf)
+                    out = _new_state(buf)
+                    if out is None:  # out of memory: the remaining blocks run in place
+                        store_inputs = False
+                if out is not None:
                     _lib.fused_apply_to(buf, out, self.n, op.wires, op.image, op.block_batch)
                     op.stored_input = buf
                     buf = out
@@ -430,6 +434,16 @@ class Segment:
         for op in self.generic_sources:
             grads.append(gslots[id(op)].to(op.source.dtype).view(op.source.shape))
         return grads
+
+
+def _new_state(like: torch.Tensor) -> Optional[torch.Tensor]:
+    """A buffer for a block's output when its input is kept, or None when the device is out
+    of memory (the caller then continues in place; the reverse sweep uncomputes through
+    the blocks without a stored input)."""
+    try:
+        return torch.empty_like(like)
+    except torch.cuda.OutOfMemoryError:
+        return None
 
 
 # ---------------------------------------------------------------- staged low-qubit runs
