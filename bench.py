@@ -270,7 +270,7 @@ def run_ours(args):
                        "tensor_core_passes": sum(1 for sg in segs for op in sg.exec_ops if getattr(op, "tc", False)),
                        # tensor-core blocks whose input state the forward kept for the backward
                        "stored_inputs": sum(1 for sg in segs for op in sg.exec_ops
-                                            if getattr(op, "stored_input", None) is not None),
+                                            if getattr(op, "kept_input", False)),
                        "chosen_by": "autotuner (measured pass costs)" if args.fuse == "auto" else f"fixed k={args.fuse}"}
     last.clear()
     torch.cuda.synchronize()

@@ -85,7 +85,7 @@ def _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, method, checkpoint="au
     loss.backward()
     if blocks is not None:
         blocks.append(sum(1 for sg in q._tape for op in sg.blocks
-                          if getattr(op, "stored_input", None) is not None))
+                          if getattr(op, "kept_input", False)))
     return loss.item(), th.grad.detach().cpu().numpy()[0]
 
 

@@ -124,11 +124,17 @@ def test_circuit_with_stored_inputs_matches_recompute():
     q0, s0, g0 = _circuit_run(n, bsz, gates, theta, paulis, False)
     tc1 = [op for sg in q1._tape for op in sg.blocks if op.tc]
     tc0 = [op for sg in q0._tape for op in sg.blocks if op.tc]
-    assert tc1 and all(getattr(op, "stored_input", None) is not None for op in tc1)
-    assert all(getattr(op, "stored_input", None) is None for op in tc0)
+    assert tc1 and all(getattr(op, "kept_input", False) for op in tc1)
+    assert all(not getattr(op, "kept_input", False) for op in tc0)
     assert np.array_equal(s1, s0)
     assert np.abs(s1 - O.run(n, bsz, W.oracle_gates(gates, theta))).max() < 1e-5
     assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
+    # a backward that does not retain the graph releases the stored inputs, like torch's
+    # own saved tensors (the segments keep only weak references)
+    q2, _, g2 = _circuit_run(n, bsz, gates, theta, paulis, True)
+    blocks = [op for sg in q2._tape for op in sg.blocks if op.tc]
+    assert blocks and all(op.kept_input and op.stored_ref() is None for op in blocks)
+    assert np.array_equal(g2, g1)
 
 
 def test_mixed_segment_with_stored_inputs():
@@ -163,7 +169,7 @@ def test_mixed_segment_with_stored_inputs():
         res[method] = (q.get_states_1d().detach().cpu().numpy(), th.grad.cpu().numpy(), rz.grad.cpu().numpy())
         if method == "fused":
             ops = [op for sg in q._tape for op in sg.exec_ops]
-            assert any(getattr(op, "stored_input", None) is not None for op in ops)
+            assert any(getattr(op, "kept_input", False) for op in ops)
             assert any(getattr(op, "members", None) is None for op in ops)
     for a, b in zip(res["fused"], res["plain"]):
         assert np.abs(a - b).max() < 1e-4 * max(1.0, np.abs(b).max())
@@ -187,7 +193,7 @@ def test_auto_mode_stores_only_when_needed(monkeypatch):
         q.fuse_wires = 6
         W.apply_circuit(q, gates, th)
         q.get_states_1d()
-        return [getattr(op, "stored_input", None) is not None for sg in q._tape for op in sg.blocks if op.tc]
+        return [getattr(op, "kept_input", False) for sg in q._tape for op in sg.blocks if op.tc]
 
     assert all(stored_blocks(True))
     assert not any(stored_blocks(False))
@@ -218,7 +224,7 @@ def test_out_of_memory_midway_falls_back_in_place(monkeypatch):
 
     monkeypatch.setattr(P, "_new_state", limited)
     q, s1, g1 = _circuit_run(n, bsz, gates, theta, paulis, True, retain=True)
-    flags = [getattr(op, "stored_input", None) is not None for sg in q._tape for op in sg.blocks if op.tc]
+    flags = [getattr(op, "kept_input", False) for sg in q._tape for op in sg.blocks if op.tc]
     assert sum(flags) == 3 and len(flags) > 3
     assert np.array_equal(s1, s0)
     assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())

@@ -185,17 +185,23 @@ class CircuitFunction(torch.autograd.Function):
         ctx.segments = segments
         ctx.counts = [len(sg.diff_inputs) for sg in segments]
         ctx.has_init = init is not None
-        ctx.save_for_backward(final)
+        # the blocks' stored input states become saved tensors of this node (the segments
+        # keep weak references), so torch releases them when a backward that does not
+        # retain the graph has run, as it does for its own saved tensors
+        stored = [pair for sg in segments for pair in sg.take_stored_inputs()]
+        ctx.stored_ops = [op for op, _ in stored]
+        ctx.save_for_backward(final, *[t for _, t in stored])
         return final
 
     @staticmethod
     def backward(ctx, grad_out: torch.Tensor):
-        (final,) = ctx.saved_tensors
+        final, *stored = ctx.saved_tensors
+        inputs = {id(op): t for op, t in zip(ctx.stored_ops, stored)}
         psi = StateCursor(final.detach())
         lam = kernel_operand(grad_out.to(torch.complex64)).clone()
         per_seg = []
         for sg, cnt in zip(reversed(ctx.segments), reversed(ctx.counts)):
-            per_seg.append(sg.backward(psi, lam, cnt > 0))
+            per_seg.append(sg.backward(psi, lam, cnt > 0, inputs))
         grads = [g for gl in reversed(per_seg) for g in gl]
         g_init = lam if ctx.has_init else None
         return (None, None, None, g_init, *grads)

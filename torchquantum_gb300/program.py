@@ -23,6 +23,7 @@ torch-built operand and its autograd graph (``generic`` ops).
 from __future__ import annotations
 
 import ctypes
+import weakref
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -316,6 +317,7 @@ class Segment:
                 if out is not None:
                     _lib.fused_apply_to(buf, out, self.n, op.wires, op.image, op.block_batch)
                     op.stored_input = buf
+                    op.kept_input = True
                     buf = out
                 elif op.tc:
                     _lib.fused_apply(buf, self.n, op.wires, op.image, op.block_batch)
@@ -325,22 +327,41 @@ class Segment:
                 engine.apply_op(buf, self.n, op)
         return buf
 
+    def take_stored_inputs(self) -> list:
+        """(block, stored input) pairs for an autograd node to save; the segment keeps weak
+        references, so later nodes over the same segment still find the inputs while one
+        node holds them, and the memory goes when the last node releases them."""
+        out = []
+        for op in self.blocks:
+            t = getattr(op, "stored_input", None)
+            if t is None and getattr(op, "stored_ref", None) is not None:
+                t = op.stored_ref()
+            if t is None:
+                continue
+            op.stored_ref = weakref.ref(t)
+            op.stored_input = None
+            out.append((op, t))
+        return out
+
     def stored_bytes(self, state: torch.Tensor) -> int:
         """Device memory ``apply(..., store_inputs=True)`` keeps for the backward."""
         return sum(1 for b in self.blocks if b.tc) * state.numel() * state.element_size()
 
     # -------------------------------------------------------------- backward
-    def backward(self, psi: "engine.StateCursor", lam: torch.Tensor, need_grads: bool) -> List[Optional[torch.Tensor]]:
+    def backward(self, psi: "engine.StateCursor", lam: torch.Tensor, need_grads: bool,
+                 inputs: Optional[dict] = None) -> List[Optional[torch.Tensor]]:
         """Reverse sweep over this segment (``psi`` at its end on entry, at its start on
-        return; ``lam`` updated in place); returns grads for ``self.diff_inputs``."""
+        return; ``lam`` updated in place); ``inputs`` maps id(block) to the block's stored
+        input state, where the forward kept one and it is still held.  Returns grads for
+        ``self.diff_inputs``."""
         _lib.nvtx_push(f"tqk.segment.backward[{len(self.exec_ops)} passes]")
         try:
-            return self._backward(psi, lam, need_grads)
+            return self._backward(psi, lam, need_grads, inputs or {})
         finally:
             _lib.nvtx_pop()
 
-    def _backward(self, psi: "engine.StateCursor", lam: torch.Tensor,
-                  need_grads: bool) -> List[Optional[torch.Tensor]]:
+    def _backward(self, psi: "engine.StateCursor", lam: torch.Tensor, need_grads: bool,
+                  inputs: dict) -> List[Optional[torch.Tensor]]:
         dev = self.device
         n = self.n
         opg = torch.zeros_like(self.op128) if (need_grads and self.natives) else None
@@ -365,7 +386,7 @@ class Segment:
                 slot = None
                 if gu is not None and _block_needs_grad(op):
                     slot = _as_real(gu, op.u128, self.u128)
-                stored = getattr(op, "stored_input", None) if op.tc else None
+                stored = inputs.get(id(op)) if op.tc else None
                 if stored is not None:
                     engine.adjoint_fused_tc(None, lam, n, op.wires, op.u128, op.block_batch, slot, psi_in=stored)
                     psi.jump(stored)
