@@ -62,7 +62,21 @@ def set_engine_defaults(method: Optional[str] = None, fuse_wires=None, fused_bac
     return prev
 
 
+# Plain (non-module, non-parameter) attributes of QuantumDevice, written straight into
+# the instance dict: nn.Module.__setattr__ costs more than recording a gate on small
+# circuits, and `_out` is reset on every gate.
+_PLAIN_ATTRS = frozenset({"n_wires", "device_name", "bsz", "device", "record_op", "op_history", "method",
+                          "fuse_wires", "fused_backend", "stage_low", "checkpoint", "_tape", "_pending", "_init",
+                          "_exported", "_out", "_buf"})
+
+
 class QuantumDevice(nn.Module):
+    def __setattr__(self, name, value):
+        if name in _PLAIN_ATTRS:
+            self.__dict__[name] = value
+        else:
+            super().__setattr__(name, value)
+
     def __init__(self, n_wires: int, device_name: str = "default", bsz: int = 1,
                  device: Union[torch.device, str] = "cuda", record_op: bool = False):
         super().__init__()
