@@ -165,6 +165,29 @@ int64_t tqk_fused_image_bytes(int64_t u_batch);
 int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream);
 /* The image of U^H, built directly from U (what tqk_fused_prepare of U^H would give). */
 int tqk_fused_prepare_adjoint(const void* u, int64_t u_batch, const int32_t* wires, void* image, void* stream);
+/* One operand image for tqk_fused_prepare_many: the image of U (adjoint == 0) or of U^H
+ * (adjoint != 0), U complex128 [u_batch][64][64], laid out for `wires` as in
+ * tqk_fused_prepare; `image` holds tqk_fused_image_bytes(u_batch) bytes, 16-byte aligned. */
+typedef struct {
+  const void* u;
+  void* image;
+  int64_t u_batch;
+  int32_t wires[6];
+  int32_t adjoint;
+  int32_t pad;
+} tqk_image_job; /* 56 bytes */
+/* Builds njobs images in one launch.  `jobs` is a DEVICE array (read by the kernel);
+ * max_u_batch >= every job's u_batch. */
+int tqk_fused_prepare_many(const tqk_image_job* jobs, int njobs, int64_t max_u_batch, void* stream);
+/* One stored-input cotangent for tqk_fused_cross_add_many: gu += M from the cross term mr. */
+typedef struct {
+  const double* mr; /* [batch][128][128] float64, from tqk_fused_adjoint_stored */
+  void* gu;         /* complex128 [batch][64][64] */
+  int64_t batch;
+} tqk_cross_job;    /* 24 bytes */
+/* tqk_fused_cross_grad(mr, NULL, batch, gu) for njobs blocks in one launch; `jobs` is a
+ * DEVICE array, max_batch >= every job's batch. */
+int tqk_fused_cross_add_many(const tqk_cross_job* jobs, int njobs, int64_t max_batch, void* stream);
 /* Block cotangent from an adjoint step: gu[b] += M_b U_b (complex128 [batch, 64, 64]),
  * where M_b is the complex 64 x 64 matrix held by the real cross term mr[b]
  * ([batch, 128, 128] float64 from tqk_fused_adjoint) and U_b the block unitary

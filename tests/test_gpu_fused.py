@@ -279,3 +279,50 @@ def test_adjoint_image_and_cross_grad_kernels():
     want = gu + torch.matmul(_lib.cross_to_complex(mr), u)
     _lib.fused_cross_grad(mr, u, torch.view_as_real(gu))
     assert (gu - want).abs().max().item() < 1e-4 * want.abs().max().item()
+
+
+def test_batched_image_and_cross_add_kernels():
+    """tqk_fused_prepare_many builds the same bytes as one tqk_fused_prepare /
+    tqk_fused_prepare_adjoint call per block (blocks of different batch and wires in one
+    launch), and tqk_fused_cross_add_many adds each cross term into its own cotangent as
+    tqk_fused_cross_grad(mr, NULL) does."""
+    from torchquantum_gb300 import _lib
+    from torchquantum_gb300.program import _to_device_table
+
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(9)
+    specs = [(3, [3, 9, 0, 14, 7, 11]), (1, [0, 1, 2, 3, 4, 5]), (2, [13, 2, 8, 5, 10, 1])]
+    jobs, want, got = [], [], []
+    for b, wires in specs:
+        z = rng.normal(size=(b, 64, 64)) + 1j * rng.normal(size=(b, 64, 64))
+        u = torch.tensor(np.linalg.qr(z)[0], dtype=torch.complex128, device=dev)
+        for adj in (0, 1):
+            img = torch.zeros(_lib.load().tqk_fused_image_bytes(b), dtype=torch.uint8, device=dev)
+            j = _lib.ImageJob()
+            j.u, j.image, j.u_batch, j.adjoint = u.data_ptr(), img.data_ptr(), b, adj
+            for i, w in enumerate(wires):
+                j.wires[i] = w
+            jobs.append(j)
+            got.append((img, u))
+            want.append(_lib.fused_prepare_adjoint(u, wires) if adj else _lib.fused_prepare(u, wires))
+    table, host = _to_device_table(jobs, dev)
+    _lib.fused_prepare_many(table, len(jobs), 3)
+    torch.cuda.synchronize()
+    for (img, _), ref in zip(got, want):
+        assert torch.equal(img, ref)
+    cjobs, outs = [], []
+    for b, _ in specs:
+        mr = torch.tensor(rng.normal(size=(b, 128, 128)), dtype=torch.float64, device=dev)
+        gu = torch.tensor(rng.normal(size=(b, 64, 64)) + 1j * rng.normal(size=(b, 64, 64)), dtype=torch.complex128,
+                          device=dev)
+        ref = gu.clone()
+        _lib.fused_cross_grad(mr, None, torch.view_as_real(ref))
+        j = _lib.CrossJob()
+        j.mr, j.gu, j.batch = mr.data_ptr(), gu.data_ptr(), b
+        cjobs.append(j)
+        outs.append((gu, ref, mr))
+    ctable, chost = _to_device_table(cjobs, dev)
+    _lib.fused_cross_add_many(ctable, len(cjobs), 3)
+    torch.cuda.synchronize()
+    for gu, ref, _ in outs:
+        assert torch.equal(gu, ref)

@@ -59,6 +59,8 @@ _SIGS = {
     "tqk_fused_prepare": (_int, [_vp, _i64, _vp, _vp, _vp]),
     "tqk_fused_prepare_adjoint": (_int, [_vp, _i64, _vp, _vp, _vp]),
     "tqk_fused_cross_grad": (_int, [_vp, _vp, _i64, _vp, _vp]),
+    "tqk_fused_prepare_many": (_int, [_vp, _int, _i64, _vp]),
+    "tqk_fused_cross_add_many": (_int, [_vp, _int, _i64, _vp]),
     "tqk_sample_scratch_bytes": (_i64, [_i64, _int]),
     "tqk_sample": (_int, [_vp, _i64, _int, _vp, _i64, _vp, _vp, _i64, _vp]),
     "tqk_staged_apply": (_int, [_vp, _i64, _int, _vp, _int, _int, _vp, _vp]),
@@ -263,6 +265,30 @@ def sample(state, n, uniforms):
     _check(lib.tqk_sample(state.data_ptr(), bsz, n, uniforms.data_ptr(), shots, out.data_ptr(), scratch.data_ptr(),
                           nbytes, _stream(state)), launches=3)
     return out
+
+
+class ImageJob(ctypes.Structure):
+    """tqk_image_job: one operand image (of U, or of U^H when ``adjoint``) to build."""
+    _fields_ = [("u", ctypes.c_void_p), ("image", ctypes.c_void_p), ("u_batch", ctypes.c_int64),
+                ("wires", ctypes.c_int32 * 6), ("adjoint", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class CrossJob(ctypes.Structure):
+    """tqk_cross_job: gu += M from the cross term of a stored-input adjoint step."""
+    _fields_ = [("mr", ctypes.c_void_p), ("gu", ctypes.c_void_p), ("batch", ctypes.c_int64)]
+
+
+assert ctypes.sizeof(ImageJob) == 56 and ctypes.sizeof(CrossJob) == 24
+
+
+def fused_prepare_many(jobs_dev: torch.Tensor, njobs: int, max_u_batch: int) -> None:
+    """Build njobs operand images in one launch from a device table of ImageJob records."""
+    _check(load().tqk_fused_prepare_many(jobs_dev.data_ptr(), njobs, max_u_batch, _stream(jobs_dev)))
+
+
+def fused_cross_add_many(jobs_dev: torch.Tensor, njobs: int, max_batch: int) -> None:
+    """Add the cross terms of njobs stored-input steps into their cotangents in one launch."""
+    _check(load().tqk_fused_cross_add_many(jobs_dev.data_ptr(), njobs, max_batch, _stream(jobs_dev)))
 
 
 class StagedOp(ctypes.Structure):

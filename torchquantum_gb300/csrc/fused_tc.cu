@@ -596,9 +596,8 @@ struct PatternOrders {
 };
 
 // Output and K orders of a block from its wires: the wire with the largest number is the
-// lowest target bit.
-__host__ PatternOrders pattern_orders(const int32_t* wires) {
-  int asc[6];  // asc[b] = position jb in `wires` of the b-th lowest target bit
+// lowest target bit.  asc[b] = position jb in `wires` of the b-th lowest target bit.
+__host__ __device__ inline void target_order(const int32_t* wires, int (&asc)[6]) {
   for (int i = 0; i < 6; ++i) asc[i] = i;
   for (int x = 1; x < 6; ++x)
     for (int y = x; y > 0 && wires[asc[y - 1]] < wires[asc[y]]; --y) {
@@ -606,19 +605,56 @@ __host__ PatternOrders pattern_orders(const int32_t* wires) {
       asc[y] = asc[y - 1];
       asc[y - 1] = t;
     }
+}
+
+// Natural index of output-order index x (korder = false) or K-order index x (true).
+__host__ __device__ inline int nat_of(int x, const int (&asc)[6], bool korder) {
+  int r = 0;
+  for (int b = 0; b < 6; ++b)
+    if ((x >> b) & 1) r |= 1 << (5 - asc[korder ? 5 - b : b]);
+  return r;
+}
+
+__host__ PatternOrders pattern_orders(const int32_t* wires) {
+  int asc[6];
+  target_order(wires, asc);
   PatternOrders o;
   for (int x = 0; x < 64; ++x) {
-    int no = 0, nk = 0;
-    for (int b = 0; b < 6; ++b) {
-      if ((x >> b) & 1) {
-        no |= 1 << (5 - asc[b]);
-        nk |= 1 << (5 - asc[5 - b]);
-      }
-    }
-    o.nat_of_out[x] = static_cast<uint8_t>(no);
-    o.nat_of_k[x] = static_cast<uint8_t>(nk);
+    o.nat_of_out[x] = static_cast<uint8_t>(nat_of(x, asc, false));
+    o.nat_of_k[x] = static_cast<uint8_t>(nat_of(x, asc, true));
   }
   return o;
+}
+
+// U (complex128 [u_batch][64][64], row-major, natural order) -> hi/lo bf16 images of the
+// U operand expected by k_tc (SWIZZLE_128B K-major, 128 rows, K = 64p + jk): row 2o holds
+// [Re U[o][jk] | -Im U[o][jk]], row 2o+1 holds [Im U[o][jk] | Re U[o][jk]] (o, jk in
+// the output and K orders), so one N = 128 product with a tile [Re x | Im x] gives the
+// real and imaginary parts of (U x)[o] side by side.  One thread per (batch, row,
+// 16-byte chunk).
+// ADJ: the image of U^H, read from U (entry (o, k) of U^H is conj U[k][o]).
+// One 16-byte chunk (8 K entries) of row `row` of the image, hi and lo parts; orow is the
+// natural output index of the row, kcol(k) the natural index of K-order index k.
+template <bool ADJ, typename KCol>
+__device__ __forceinline__ void prep_chunk(const double2* ub, uint8_t* base, int row, int chunk, int orow,
+                                           KCol kcol) {
+  float hv[8], lv[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int kk = chunk * 8 + e;
+    const int kc = kcol(kk & 63);
+    double2 z = ADJ ? ub[kc * 64 + orow] : ub[orow * 64 + kc];
+    if (ADJ) z.y = -z.y;
+    const double v = (row & 1) == 0 ? (kk < 64 ? z.x : -z.y) : (kk < 64 ? z.y : z.x);
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    hv[e] = __bfloat162float(h);
+    lv[e] = static_cast<float>(v - static_cast<double>(hv[e]));
+  }
+  uint4 hi = make_uint4(pack_bf2(hv[0], hv[1]), pack_bf2(hv[2], hv[3]), pack_bf2(hv[4], hv[5]), pack_bf2(hv[6], hv[7]));
+  uint4 lo = make_uint4(pack_bf2(lv[0], lv[1]), pack_bf2(lv[2], lv[3]), pack_bf2(lv[4], lv[5]), pack_bf2(lv[6], lv[7]));
+  const uint32_t o = sw128_off(row, chunk, kBKBlockBytes);
+  *reinterpret_cast<uint4*>(base + o) = hi;
+  *reinterpret_cast<uint4*>(base + kBImgBytes + o) = lo;
 }
 
 // U (complex128 [u_batch][64][64], row-major, natural order) -> hi/lo bf16 images of the
@@ -635,32 +671,34 @@ __global__ void k_tc_prep(const double2* u, int64_t u_batch, uint8_t* img, const
   const int64_t b = idx / (128 * 16);
   const int row = static_cast<int>((idx / 16) % 128);
   const int chunk = static_cast<int>(idx % 16);
-  const double2* ub = u + b * 64 * 64;
-  const int orow = ord.nat_of_out[row >> 1];
-  float hv[8], lv[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int kk = chunk * 8 + e;
-    const int kcol = ord.nat_of_k[kk & 63];
-    double2 z = ADJ ? ub[kcol * 64 + orow] : ub[orow * 64 + kcol];
-    if (ADJ) z.y = -z.y;
-    const double v = (row & 1) == 0 ? (kk < 64 ? z.x : -z.y) : (kk < 64 ? z.y : z.x);
-    const __nv_bfloat16 h = __double2bfloat16(v);
-    hv[e] = __bfloat162float(h);
-    lv[e] = static_cast<float>(v - static_cast<double>(hv[e]));
-  }
-  uint4 hi = make_uint4(pack_bf2(hv[0], hv[1]), pack_bf2(hv[2], hv[3]), pack_bf2(hv[4], hv[5]), pack_bf2(hv[6], hv[7]));
-  uint4 lo = make_uint4(pack_bf2(lv[0], lv[1]), pack_bf2(lv[2], lv[3]), pack_bf2(lv[4], lv[5]), pack_bf2(lv[6], lv[7]));
-  uint8_t* base = img + b * 2 * kBImgBytes;
-  const uint32_t o = sw128_off(row, chunk, kBKBlockBytes);
-  *reinterpret_cast<uint4*>(base + o) = hi;
-  *reinterpret_cast<uint4*>(base + kBImgBytes + o) = lo;
+  prep_chunk<ADJ>(u + b * 64 * 64, img + b * 2 * kBImgBytes, row, chunk, ord.nat_of_out[row >> 1],
+                  [&](int k) { return static_cast<int>(ord.nat_of_k[k]); });
+}
+
+// Many images in one launch: blockIdx.y = job, the orders computed from the job's wires.
+__global__ void k_tc_prep_many(const tqk_image_job* jobs) {
+  const tqk_image_job j = jobs[blockIdx.y];
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= j.u_batch * 128 * 16) return;
+  int asc[6];
+  target_order(j.wires, asc);
+  const int64_t b = idx / (128 * 16);
+  const int row = static_cast<int>((idx / 16) % 128);
+  const int chunk = static_cast<int>(idx % 16);
+  const double2* ub = static_cast<const double2*>(j.u) + b * 64 * 64;
+  uint8_t* base = static_cast<uint8_t*>(j.image) + b * 2 * kBImgBytes;
+  const int orow = nat_of(row >> 1, asc, false);
+  auto kcol = [&](int k) { return nat_of(k, asc, true); };
+  if (j.adjoint) prep_chunk<true>(ub, base, row, chunk, orow, kcol);
+  else prep_chunk<false>(ub, base, row, chunk, orow, kcol);
 }
 
 }  // namespace tc
 }  // namespace tqk
 
 using namespace tqk;
+
+static_assert(sizeof(tqk_image_job) == 56 && sizeof(tqk_cross_job) == 24, "job records are part of the C ABI");
 
 extern "C" int64_t tqk_fused_image_bytes(int64_t u_batch) { return u_batch * 2 * tc::kBImgBytes; }
 
@@ -694,6 +732,17 @@ extern "C" int tqk_fused_prepare(const void* u, int64_t u_batch, const int32_t* 
 extern "C" int tqk_fused_prepare_adjoint(const void* u, int64_t u_batch, const int32_t* wires, void* image,
                                          void* stream) {
   return prepare_entry(u, u_batch, wires, image, stream, true, "tqk_fused_prepare_adjoint");
+}
+
+extern "C" int tqk_fused_prepare_many(const tqk_image_job* jobs, int njobs, int64_t max_u_batch, void* stream) {
+  if (njobs <= 0) return TQK_OK;
+  if (!jobs) return fail(TQK_BAD_POINTER, "tqk_fused_prepare_many: null job table");
+  if (njobs > 65535 || max_u_batch < 1 || max_u_batch > (1ll << 40))
+    return fail(TQK_BAD_SHAPE, "tqk_fused_prepare_many: %d jobs, max u_batch %lld", njobs, (long long)max_u_batch);
+  const int64_t work = max_u_batch * 128 * 16;
+  dim3 grid(static_cast<unsigned>((work + 255) / 256), static_cast<unsigned>(njobs), 1);
+  tc::k_tc_prep_many<<<grid, 256, 0, as_stream(stream)>>>(jobs);
+  return launch_status("tqk_fused_prepare_many");
 }
 
 // gu[b] += M_b U_b for the block cotangent: M_b (64 x 64 complex) from the adjoint step's
@@ -736,14 +785,24 @@ __global__ void __launch_bounds__(256) k_cross_grad(const double* mr, const doub
 
 // gu[b] += M_b: the cross term of a stored-input adjoint step is the cotangent itself
 // (float64 throughout).  One thread per complex entry.
-__global__ void __launch_bounds__(256) k_cross_add(const double* mr, int64_t batch, double2* gu) {
-  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= batch * 64 * 64) return;
+__device__ __forceinline__ void cross_add_entry(const double* mr, double2* gu, int64_t e) {
   const int64_t b = e >> 12;
   const int j = static_cast<int>((e >> 6) & 63), k = static_cast<int>(e & 63);
   const double* m = mr + b * 128 * 128;
   gu[e].x += m[j * 128 + k] + m[(64 + j) * 128 + 64 + k];
   gu[e].y += m[(64 + j) * 128 + k] - m[j * 128 + 64 + k];
+}
+
+__global__ void __launch_bounds__(256) k_cross_add(const double* mr, int64_t batch, double2* gu) {
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < batch * 64 * 64) cross_add_entry(mr, gu, e);
+}
+
+// Many blocks in one launch: blockIdx.y = job.
+__global__ void __launch_bounds__(256) k_cross_add_many(const tqk_cross_job* jobs) {
+  const tqk_cross_job j = jobs[blockIdx.y];
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < j.batch * 64 * 64) cross_add_entry(j.mr, static_cast<double2*>(j.gu), e);
 }
 }  // namespace tc
 }  // namespace tqk
@@ -768,6 +827,17 @@ extern "C" int tqk_fused_cross_grad(const double* mr, const void* u, int64_t bat
   tc::k_cross_grad<<<static_cast<unsigned>(batch), 256, smem, as_stream(stream)>>>(
       mr, static_cast<const double2*>(u), static_cast<double2*>(gu));
   return launch_status("tqk_fused_cross_grad");
+}
+
+extern "C" int tqk_fused_cross_add_many(const tqk_cross_job* jobs, int njobs, int64_t max_batch, void* stream) {
+  if (njobs <= 0) return TQK_OK;
+  if (!jobs) return fail(TQK_BAD_POINTER, "tqk_fused_cross_add_many: null job table");
+  if (njobs > 65535 || max_batch < 1 || max_batch > (1ll << 40))
+    return fail(TQK_BAD_SHAPE, "tqk_fused_cross_add_many: %d jobs, max batch %lld", njobs, (long long)max_batch);
+  const int64_t work = max_batch * 64 * 64;
+  dim3 grid(static_cast<unsigned>((work + 255) / 256), static_cast<unsigned>(njobs), 1);
+  tc::k_cross_add_many<<<grid, 256, 0, as_stream(stream)>>>(jobs);
+  return launch_status("tqk_fused_cross_add_many");
 }
 
 namespace {

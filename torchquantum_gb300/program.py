@@ -261,12 +261,34 @@ class Segment:
         maxb = max(b.block_batch for b in self.blocks)
         _lib.block_build(bt, len(bdescs), maxb, ot, dev)
         for blk in self.blocks:
-            if blk.tc:
-                blk.image = _lib.fused_prepare(blk.u128, blk.wires)
-            else:
+            if not blk.tc:
                 blk.operand = blk.u128.to(torch.complex64)
+        self._prepare_images(adjoint=False)
         # keep operands of non-native members alive in complex128
         self._member128 = [getattr(m, "_op128_keep", None) for b in self.blocks for m in b.members]
+
+    def _prepare_images(self, adjoint: bool) -> None:
+        """Tensor-core operand images of every block of the segment (of U, or of U^H for
+        the reverse sweep) in one buffer and one launch: ``blk.image`` / ``blk.image_h``."""
+        tcb = [b for b in self.blocks if b.tc]
+        if not tcb:
+            return
+        lib = _lib.load()
+        sizes = [lib.tqk_fused_image_bytes(b.block_batch) for b in tcb]
+        buf = torch.empty(sum(sizes), dtype=torch.uint8, device=self.device)
+        jobs, off = [], 0
+        for b, sz in zip(tcb, sizes):
+            img = buf[off:off + sz]  # every image is a multiple of 64 KB: offsets stay aligned
+            off += sz
+            setattr(b, "image_h" if adjoint else "image", img)
+            j = _lib.ImageJob()
+            j.u, j.image, j.u_batch, j.adjoint = b.u128.data_ptr(), img.data_ptr(), b.block_batch, int(adjoint)
+            for i, w in enumerate(b.wires):
+                j.wires[i] = w
+            jobs.append(j)
+        table, host = _to_device_table(jobs, self.device)
+        self._keep += [table, host]
+        _lib.fused_prepare_many(table, len(jobs), max(b.block_batch for b in tcb))
 
     def _block_op(self, m, where):
         bo = BlockOp()
@@ -369,6 +391,19 @@ class Segment:
         for op in self.generic_sources:
             gslots[id(op)] = torch.zeros(op.operand.shape, dtype=torch.complex128, device=dev)
         gu = torch.zeros_like(self.u128) if (need_grads and self.blocks) else None
+        # tensor-core blocks: U^H images in one launch, one zeroed buffer for the cross
+        # terms of the blocks that need a cotangent, stored-input cotangents added in one
+        # launch after the sweep
+        self._prepare_images(adjoint=True)
+        mr_of = {}
+        tc_grad = [b for b in self.blocks if b.tc and gu is not None and _block_needs_grad(b)]
+        if tc_grad:
+            mr_all = torch.zeros(sum(b.block_batch for b in tc_grad), 128, 128, dtype=torch.float64, device=dev)
+            row = 0
+            for b in tc_grad:
+                mr_of[id(b)] = mr_all[row:row + b.block_batch]
+                row += b.block_batch
+        cross_jobs = []
         for op in reversed(self.exec_ops):
             if isinstance(op, StagedRun):
                 slots = []
@@ -387,11 +422,18 @@ class Segment:
                 if gu is not None and _block_needs_grad(op):
                     slot = _as_real(gu, op.u128, self.u128)
                 stored = inputs.get(id(op)) if op.tc else None
+                mr = mr_of.get(id(op)) if slot is not None else None
                 if stored is not None:
-                    engine.adjoint_fused_tc(None, lam, n, op.wires, op.u128, op.block_batch, slot, psi_in=stored)
+                    _lib.fused_adjoint_stored(stored, lam, n, op.wires, op.image_h, op.block_batch, mr)
+                    if mr is not None:  # the cross term against the stored input is the cotangent
+                        j = _lib.CrossJob()
+                        j.mr, j.gu, j.batch = mr.data_ptr(), slot.data_ptr(), op.block_batch
+                        cross_jobs.append(j)
                     psi.jump(stored)
                 elif op.tc:
-                    engine.adjoint_fused_tc(psi.writable(), lam, n, op.wires, op.u128, op.block_batch, slot)
+                    _lib.fused_adjoint(psi.writable(), lam, n, op.wires, op.image_h, op.block_batch, mr)
+                    if mr is not None:  # M U (float32 product, float64 sum)
+                        _lib.fused_cross_grad(mr, engine.kernel_operand(op.u128), slot)
                 else:
                     _lib.adjoint_matrix(psi.writable(), lam, n, op.wires, op.operand, op.block_batch, slot)
                 continue
@@ -402,6 +444,10 @@ class Segment:
                 elif id(op) in gslots:
                     slot = torch.view_as_real(gslots[id(op)]).view(-1)
             engine.adjoint_op(psi.writable(), lam, n, op, slot)
+        if cross_jobs:
+            table, host = _to_device_table(cross_jobs, dev)
+            self._keep_cross = [table, host, mr_of]
+            _lib.fused_cross_add_many(table, len(cross_jobs), max(j.batch for j in cross_jobs))
         if not need_grads:
             return [None] * len(self.diff_inputs)
         # block cotangents -> member operand cotangents
