@@ -123,31 +123,6 @@ def adjoint_op(psi: torch.Tensor, lam: torch.Tensor, n: int, op: TapeOp, grad: O
         raise ValueError(f"unknown op kind {k}")
 
 
-def adjoint_fused_tc(psi, lam, n, wires, u128: torch.Tensor, batch: int, grad: Optional[torch.Tensor],
-                     psi_in: Optional[torch.Tensor] = None) -> None:
-    """Tensor-core adjoint step of a fused 6-wire block: psi, lam <- U^H (.), and the
-    cotangent of U as M U with M = sum over columns of lam conj(psi)^T (U unitary),
-    added into ``grad`` (float64 interleaved view of a complex128 [batch, 64, 64]).
-
-    With ``psi_in`` (the state the block was applied to, kept by the forward) psi is not
-    touched: lam <- U^H lam and the cotangent is sum lam conj(psi_in)^T directly."""
-    u = kernel_operand(u128)
-    img_h = _lib.fused_prepare_adjoint(u, wires)
-    mr = None
-    if grad is not None:
-        mr = torch.zeros(batch, 128, 128, dtype=torch.float64, device=lam.device)
-    if psi_in is not None:
-        _lib.fused_adjoint_stored(psi_in, lam, n, wires, img_h, batch, mr)
-        if grad is not None:
-            _lib.fused_cross_grad(mr, None, grad)
-        return
-    _lib.fused_adjoint(psi, lam, n, wires, img_h, batch, mr)
-    if grad is not None:
-        # M carries fp32 accuracy (tensor-memory accumulation), so M U in float32 loses
-        # nothing; one kernel adds it into the float64 cotangent
-        _lib.fused_cross_grad(mr, u, grad)
-
-
 class StateCursor:
     """The state a reverse sweep has reached.  It starts as the saved final state and,
     after a block whose input the forward kept, becomes that stored input: both are only
