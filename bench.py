@@ -280,14 +280,23 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = _lib.LAUNCHES[0]
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            th.grad = None
-            step(th)
-        e1.record(stream)
-        torch.cuda.synchronize()
+    # the dominant kernel's launches inside the timed steps, bracketed by CUDA events on
+    # the stream they run on (the roofline's live duration)
+    live = {name: LaunchTimer(getattr(_lib, name)) for name in ("fused_adjoint_stored", "fused_adjoint")}
+    for name, t in live.items():
+        setattr(_lib, name, t)
+    try:
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                th.grad = None
+                step(th)
+            e1.record(stream)
+            torch.cuda.synchronize()
+    finally:
+        for name, t in live.items():
+            setattr(_lib, name, t.fn)
     launches = _lib.LAUNCHES[0] - launches0
     peak_states = (torch.cuda.max_memory_allocated(dev) - mem0) / (bsz * (8 << n))
     ms = R.max_over_ranks(e0.elapsed_time(e1), dev)
@@ -354,7 +363,8 @@ def run_ours(args):
                        "h2d_bytes_per_step": int(pin_theta.numel() * 4),
                        "d2h_bytes_per_step": int(out_ev.numel() * 4 + out_g.numel() * 4)}
         # ---------------- roofline of the dominant kernel (adjoint dense 1-wire step)
-        line["roofline"], line["kernels"] = roofline(args, dev, bool(fusion_info and fusion_info["stored_inputs"]))
+        line["roofline"], line["kernels"] = roofline(args, dev, bool(fusion_info and fusion_info["stored_inputs"]),
+                                                     live)
         line["plain_gate_pass"] = line["kernels"]["dense1_fwd"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.quick:
         v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds)
@@ -373,11 +383,34 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def roofline(args, dev, stored=True):
+class LaunchTimer:
+    """Wraps an engine entry point: each call made while installed is bracketed by CUDA
+    events on the current stream (the one the kernel is launched on)."""
+
+    def __init__(self, fn):
+        self.fn = fn
+        self.events = []
+
+    def __call__(self, *a, **k):
+        import torch
+
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        out = self.fn(*a, **k)
+        e.record()
+        self.events.append((s, e))
+        return out
+
+    def mean_s(self):
+        return sum(s.elapsed_time(e) for s, e in self.events) / len(self.events) / 1e3 if self.events else None
+
+
+def roofline(args, dev, stored=True, live=None):
     """Time the engine's hot kernels alone (CUDA events on the launching stream) on the
     bench's state size; algorithmic bytes per launch from the touched amplitudes.
     ``stored``: the fused step's blocks kept their inputs, so its dominant kernel is the
-    stored-input adjoint step."""
+    stored-input adjoint step.  ``live``: LaunchTimers of the adjoint entry points over the
+    timed steps; the roofline's achieved rate uses their average launch duration."""
     import torch
 
     from torchquantum_gb300 import _lib
@@ -493,7 +526,15 @@ def roofline(args, dev, stored=True):
     if cap is None:
         dom = res["dense1_adj"]
         kname = "k_dense_adj<2> (adjoint step of a dense 1-wire gate)"
-    roof = {"bound": "hbm", "achieved": dom["GB/s"], "peak": peak, "unit": "GB/s", "frac": dom["GB/s"] / peak,
+    achieved, source = dom["GB/s"], "kernel timed alone (CUDA events, random wire sets)"
+    entry = "fused_adjoint_stored" if cap is ADJ_STORED_TRAFFIC_CAPTURE else "fused_adjoint"
+    if live and cap is not None and live[entry].events:
+        t = live[entry].mean_s()
+        achieved = dom["bytes"] / t / 1e9
+        source = (f"average of its {len(live[entry].events)} launches inside the timed steps (CUDA events on the "
+                  f"launching stream); alone: {dom['GB/s']:.0f} GB/s")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "achieved_source": source,
             "traffic": traffic, "algorithmic_bytes": dom["bytes"], "kernel": kname,
             "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=22, bsz=8, scaled by amplitudes"
