@@ -146,7 +146,9 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": _config(args, "plain"), "impl": "reference",
+        "config": _config(args), "impl": "reference",
+        "method": "upstream algorithm restated on the host (numpy complex64, autograd-style forward "
+                  "keeping per-gate states, then the reverse sweep)",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"1 circuit, first {g} of {args.depth} gates fwd+bwd per step, extrapolated"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -154,14 +156,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _config(args, method):
+def _config(args):
+    """The workload (identical for both arms; the engine method is reported beside it)."""
     state_mb = args.bsz * (8 << args.n) / 2**20
     flush = (f"none needed: state {state_mb:.0f} MiB > L2 129 MB" if state_mb > 129 else
              f"not flushed: state {state_mb:.0f} MiB fits in L2 (129 MB)")
     return {"workload": f"random circuit n={args.n} bsz={args.bsz} depth={args.depth} "
                         "(U3 60%, CNOT/CZ/CRX 40%) + probs + 8 Pauli expvals, fwd + adjoint bwd",
-            "n_wires": args.n, "global_batch": args.bsz, "depth": args.depth, "method": method,
-            "l2_flush": flush}
+            "n_wires": args.n, "global_batch": args.bsz, "depth": args.depth, "l2_flush": flush}
 
 
 # ------------------------------------------------------------------ GPU leg
@@ -303,7 +305,7 @@ def run_ours(args):
     value = R.job_throughput(bsz * args.steps, world, ms / 1e3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": _config(args, args.method),
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": _config(args), "method": args.method,
             "clocks": clk.summary(), "gpu_launches": launches}
     if fusion_info:
         line["config"]["fusion"] = fusion_info

@@ -228,3 +228,46 @@ def test_out_of_memory_midway_falls_back_in_place(monkeypatch):
     assert sum(flags) == 3 and len(flags) > 3
     assert np.array_equal(s1, s0)
     assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
+
+
+def _two_reads(n, bsz, gates, theta, paulis, init, checkpoint):
+    """Gradients (angles, initial state) of <P> read twice: after the first half of the
+    circuit and after all of it (two autograd nodes over shared segments)."""
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import workloads as W
+
+    th = torch.tensor(theta, device="cuda", requires_grad=True)
+    s0 = torch.tensor(init, dtype=torch.complex64, device="cuda", requires_grad=True)
+    q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+    q.method = "fused"
+    q.fuse_wires = 6
+    q.checkpoint = checkpoint
+    q.set_states(s0)
+    half = len(gates) // 2
+    W.apply_circuit(q, gates[:half], th)
+    e1 = tq.expval_joint_analytical_batch(q, paulis)
+    W.apply_circuit(q, gates[half:], th)
+    e2 = tq.expval_joint_analytical_batch(q, paulis)
+    (e1.sum() + 2.0 * e2.sum()).backward()
+    kept = sum(1 for sg in q._tape for op in sg.blocks if getattr(op, "kept_input", False))
+    return th.grad.cpu().numpy(), s0.grad.cpu().numpy(), kept
+
+
+def test_two_reads_and_initial_state_gradient():
+    """Two reads of one device (the second node's segments include the first's) and a
+    differentiable initial state: stored block inputs give the in-place sweep's gradients
+    for the angles and for the initial state."""
+    from torchquantum_gb300 import workloads as W
+
+    n, bsz = 14, 2
+    gates, ncols = W.random_circuit(n, 200, seed=31)
+    theta = W.random_params(bsz, ncols, seed=32)
+    paulis = W.random_paulis(n, 3, seed=33)
+    rng = np.random.default_rng(34)
+    init = rng.normal(size=(bsz, 1 << n)) + 1j * rng.normal(size=(bsz, 1 << n))
+    init /= np.linalg.norm(init, axis=1, keepdims=True)
+    g1, s1, k1 = _two_reads(n, bsz, gates, theta, paulis, init, True)
+    g0, s0, k0 = _two_reads(n, bsz, gates, theta, paulis, init, False)
+    assert k1 > 0 and k0 == 0
+    assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
+    assert np.abs(s1 - s0).max() < 1e-5 * max(1.0, np.abs(s0).max())
