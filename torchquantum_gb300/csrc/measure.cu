@@ -290,15 +290,34 @@ struct FinishCols {
   int c[kMaxStringsPerPass];
 };
 
-__global__ void k_expval_finish(const double* partial, int64_t nblk, int ns, int slot_stride, const FinishCols cols,
-                                int m, double* out, int64_t bsz) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= bsz * ns) return;
-  const int64_t b = idx / ns;
-  const int s = (int)(idx % ns);
-  double acc = 0.0;
-  for (int64_t k = 0; k < nblk; ++k) acc += partial[(b * nblk + k) * slot_stride + s];
-  out[b * m + cols.c[s]] = acc;
+// One CTA of kFinishThreads per row: thread t sums the partials k = t, t + kFinishThreads,
+// ... of every slot, then a fixed tree in shared memory adds the threads' sums (the same
+// order on every call, so the results are deterministic).
+constexpr int kFinishThreads = 128;
+
+__global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* partial, int64_t nblk, int ns,
+                                                                  int slot_stride, const FinishCols cols, int m,
+                                                                  double* out, int64_t bsz) {
+  __shared__ double red[kMaxStringsPerPass][kFinishThreads];
+  const int64_t b = blockIdx.x;
+  double acc[kMaxStringsPerPass];
+#pragma unroll
+  for (int s = 0; s < kMaxStringsPerPass; ++s) acc[s] = 0.0;
+  for (int64_t k = threadIdx.x; k < nblk; k += kFinishThreads) {
+    const double* pk = partial + (b * nblk + k) * slot_stride;
+#pragma unroll
+    for (int s = 0; s < kMaxStringsPerPass; ++s)
+      if (s < ns) acc[s] += pk[s];
+  }
+#pragma unroll
+  for (int s = 0; s < kMaxStringsPerPass; ++s) red[s][threadIdx.x] = acc[s];
+  __syncthreads();
+  for (int half = kFinishThreads / 2; half > 0; half >>= 1) {
+    if (threadIdx.x < half)
+      for (int s = 0; s < ns; ++s) red[s][threadIdx.x] += red[s][threadIdx.x + half];
+    __syncthreads();
+  }
+  if (threadIdx.x < ns) out[b * m + cols.c[threadIdx.x]] = red[threadIdx.x][0];
 }
 
 struct ApplySumParams {
@@ -435,8 +454,7 @@ extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uin
       }
       const unsigned grid = n <= 31 ? launch_rows<uint32_t>(p, rb, st) : launch_rows<uint64_t>(p, rb, st);
       if ((rc = launch_status(what))) return rc;
-      const int64_t nout = bsz * p.ns;
-      k_expval_finish<<<(unsigned)((nout + 127) / 128), 128, 0, st>>>(partial, grid, p.ns, kMaxStringsPerPass,
+      k_expval_finish<<<(unsigned)bsz, kFinishThreads, 0, st>>>(partial, grid, p.ns, kMaxStringsPerPass,
                                                                         cols, m, out, bsz);
       if ((rc = launch_status(what))) return rc;
     }
@@ -478,8 +496,7 @@ extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uin
     }
     launch_expval(p, grid, st);
     if ((rc = launch_status(what))) return rc;
-    const int64_t nout = bsz * p.ns;
-    k_expval_finish<<<(unsigned)((nout + 127) / 128), 128, 0, st>>>(partial, nblk, p.ns, kMaxStringsPerPass,
+    k_expval_finish<<<(unsigned)bsz, kFinishThreads, 0, st>>>(partial, nblk, p.ns, kMaxStringsPerPass,
                                                                       cols, m, out, bsz);
     if ((rc = launch_status(what))) return rc;
   }
@@ -629,8 +646,7 @@ extern "C" int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, c
     }
     launch_expval(p, grid, st);
     if ((rc = launch_status(what))) return rc;
-    const int64_t nout = bsz * p.ns;
-    k_expval_finish<<<static_cast<unsigned>((nout + 127) / 128), 128, 0, st>>>(partial, nblk, p.ns,
+    k_expval_finish<<<static_cast<unsigned>(bsz), kFinishThreads, 0, st>>>(partial, nblk, p.ns,
                                                                                kMaxStringsPerPass, cols, m, out, bsz);
     if ((rc = launch_status(what))) return rc;
   }
