@@ -124,7 +124,10 @@ def test_circuit_with_stored_inputs_matches_recompute():
     q0, s0, g0 = _circuit_run(n, bsz, gates, theta, paulis, False)
     tc1 = [op for sg in q1._tape for op in sg.blocks if op.tc]
     tc0 = [op for sg in q0._tape for op in sg.blocks if op.tc]
-    assert tc1 and all(getattr(op, "kept_input", False) for op in tc1)
+    # from |0...0> the circuit's first block keeps nothing (its reverse step is a gather)
+    first = q1._tape[0].exec_ops[0]
+    assert getattr(first, "zero_input", False) == bool(getattr(first, "tc", False))
+    assert tc1 and all(getattr(op, "kept_input", False) or getattr(op, "zero_input", False) for op in tc1)
     assert all(not getattr(op, "kept_input", False) for op in tc0)
     assert np.array_equal(s1, s0)
     assert np.abs(s1 - O.run(n, bsz, W.oracle_gates(gates, theta))).max() < 1e-5
@@ -132,7 +135,7 @@ def test_circuit_with_stored_inputs_matches_recompute():
     # a backward that does not retain the graph releases the stored inputs, like torch's
     # own saved tensors (the segments keep only weak references)
     q2, _, g2 = _circuit_run(n, bsz, gates, theta, paulis, True)
-    blocks = [op for sg in q2._tape for op in sg.blocks if op.tc]
+    blocks = [op for sg in q2._tape for op in sg.blocks if op.tc and not getattr(op, "zero_input", False)]
     assert blocks and all(op.kept_input and op.stored_ref() is None for op in blocks)
     assert np.array_equal(g2, g1)
 
@@ -193,7 +196,8 @@ def test_auto_mode_stores_only_when_needed(monkeypatch):
         q.fuse_wires = 6
         W.apply_circuit(q, gates, th)
         q.get_states_1d()
-        return [getattr(op, "kept_input", False) for sg in q._tape for op in sg.blocks if op.tc]
+        return [getattr(op, "kept_input", False) for sg in q._tape for op in sg.blocks
+                if op.tc and not getattr(op, "zero_input", False)]
 
     assert all(stored_blocks(True))
     assert not any(stored_blocks(False))
@@ -271,3 +275,35 @@ def test_two_reads_and_initial_state_gradient():
     assert k1 > 0 and k0 == 0
     assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
     assert np.abs(s1 - s0).max() < 1e-5 * max(1.0, np.abs(s0).max())
+
+
+@pytest.mark.parametrize("per_row", [False, True])
+def test_first_block_from_zero_state(per_row):
+    """The circuit's first tensor-core block acting on |0...0> takes the gather reverse
+    step (cotangent lam conj(e_0)^T, no lam update): gradients equal the plain method's,
+    for one U shared by every row and for per-row U."""
+    import torchquantum_gb300 as tq
+    import torchquantum_gb300.functional as tqf
+    from torchquantum_gb300 import workloads as W
+
+    n, bsz = 14, 3
+    gates, ncols = W.random_circuit(n, 120, seed=41 + per_row)
+    theta = W.random_params(1 if not per_row else bsz, ncols, seed=42)
+    paulis = W.random_paulis(n, 3, seed=43)
+    res = {}
+    for method in ("fused", "plain"):
+        th = torch.tensor(theta, device="cuda", requires_grad=True)
+        q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+        q.method = method
+        q.fuse_wires = 6
+        for w in range(6):  # a first block of several gates on wires 0-5
+            tqf.ry(q, wires=w, params=th[:, w:w + 1])
+        W.apply_circuit(q, gates, th)
+        ev = tq.expval_joint_analytical_batch(q, paulis)
+        (ev * torch.tensor([1.0, -0.5, 2.0], device="cuda")).sum().backward()
+        res[method] = (ev.detach().cpu().numpy(), th.grad.cpu().numpy())
+        if method == "fused":
+            first = q._tape[0].exec_ops[0]
+            assert getattr(first, "tc", False) and first.zero_input and first.block_batch == (bsz if per_row else 1)
+    assert np.abs(res["fused"][0] - res["plain"][0]).max() < 1e-5
+    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-4 * max(1.0, np.abs(res["plain"][1]).max())

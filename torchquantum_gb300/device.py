@@ -67,7 +67,7 @@ def set_engine_defaults(method: Optional[str] = None, fuse_wires=None, fused_bac
 # circuits, and `_out` is reset on every gate.
 _PLAIN_ATTRS = frozenset({"n_wires", "device_name", "bsz", "device", "record_op", "op_history", "method",
                           "fuse_wires", "fused_backend", "stage_low", "checkpoint", "_tape", "_pending", "_init",
-                          "_exported", "_out", "_buf"})
+                          "_exported", "_out", "_buf", "_zero_start"})
 
 
 class QuantumDevice(nn.Module):
@@ -106,6 +106,7 @@ class QuantumDevice(nn.Module):
         self._exported = False
         self._out: Optional[torch.Tensor] = None
         self._buf = self._zero_state(self.bsz)
+        self._zero_start = True  # the tape starts from |0...0> (no initial state given)
 
     # ------------------------------------------------------------------ buffers
     def _zero_state(self, bsz: int) -> torch.Tensor:
@@ -119,6 +120,7 @@ class QuantumDevice(nn.Module):
         self._pending = []
         self._out = None
         self._exported = False
+        self._zero_start = states is None
         if states is None:
             self._init = None
             self._buf = self._zero_state(bsz if bsz is not None else self.bsz)
@@ -165,7 +167,8 @@ class QuantumDevice(nn.Module):
                 self._buf = self._buf.clone()
                 self._exported = False
             seg = program.Segment(self, ops, self.method)
-            self._buf = seg.apply(self._buf, self._store_block_inputs(seg))
+            self._buf = seg.apply(self._buf, self._store_block_inputs(seg),
+                                  zero_input=self._zero_start and not self._tape)
             self._tape.append(seg)
             self._out = None
 

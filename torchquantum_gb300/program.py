@@ -315,24 +315,30 @@ class Segment:
         return self._dummy.data_ptr()
 
     # -------------------------------------------------------------- forward
-    def apply(self, buf: torch.Tensor, store_inputs: bool = False) -> torch.Tensor:
+    def apply(self, buf: torch.Tensor, store_inputs: bool = False, zero_input: bool = False) -> torch.Tensor:
         """Run the segment on ``buf``; returns the buffer holding the result.  With
         ``store_inputs`` every tensor-core block writes its output to a new buffer and
         keeps its input for the backward (``buf`` itself may become one of those stored
-        inputs, so the result is then a different tensor)."""
+        inputs, so the result is then a different tensor).  ``zero_input``: ``buf`` is
+        |0...0> in every row and no initial state or earlier segment precedes it (the
+        device's first segment from its default state)."""
         _lib.nvtx_push(f"tqk.segment.forward[{len(self.exec_ops)} passes]")
         try:
-            return self._apply(buf, store_inputs)
+            return self._apply(buf, store_inputs, zero_input)
         finally:
             _lib.nvtx_pop()
 
-    def _apply(self, buf: torch.Tensor, store_inputs: bool) -> torch.Tensor:
-        for op in self.exec_ops:
+    def _apply(self, buf: torch.Tensor, store_inputs: bool, zero_input: bool) -> torch.Tensor:
+        for i, op in enumerate(self.exec_ops):
             if isinstance(op, StagedRun):
                 _lib.staged_apply(buf, self.n, op.descs(), op.tile_bits)
             elif getattr(op, "members", None) is not None:
                 out = None
-                if op.tc and store_inputs:
+                if op.tc and zero_input and i == 0:
+                    # a first block on |0...0>: its reverse step needs neither its input nor
+                    # the cotangent before it (nothing precedes it), so nothing is kept
+                    op.zero_input = True
+                elif op.tc and store_inputs:
                     out = _new_state(buf)
                     if out is None:  # out of memory: the remaining blocks run in place
                         store_inputs = False
@@ -423,6 +429,13 @@ class Segment:
                     slot = _as_real(gu, op.u128, self.u128)
                 stored = inputs.get(id(op)) if op.tc else None
                 mr = mr_of.get(id(op)) if slot is not None else None
+                if op.tc and getattr(op, "zero_input", False):
+                    # the last reverse step of the circuit, from |0...0>: the cotangent of U
+                    # is lam conj(e_0)^T -- lam at the block's 64 patterns with every other
+                    # bit clear, in column 0; lam and psi are not needed any further
+                    if slot is not None:
+                        _add_zero_input_cotangent(lam, op, slot, n)
+                    continue
                 if stored is not None:
                     _lib.fused_adjoint_stored(stored, lam, n, op.wires, op.image_h, op.block_batch, mr)
                     if mr is not None:  # the cross term against the stored input is the cotangent
@@ -501,6 +514,23 @@ class Segment:
         for op in self.generic_sources:
             grads.append(gslots[id(op)].to(op.source.dtype).view(op.source.shape))
         return grads
+
+
+def _add_zero_input_cotangent(lam: torch.Tensor, blk, slot: torch.Tensor, n: int) -> None:
+    """gu[b][j][0] += lam[b, offset of pattern j] for a block applied to |0...0> (wires[0] is
+    the pattern's most significant bit; the sum over rows when one U serves every row)."""
+    offs = [sum(1 << (n - 1 - w) for i, w in enumerate(blk.wires) if (j >> (5 - i)) & 1) for j in range(64)]
+    # a pinned staging copy: a copy from pageable memory would block the stream (and with
+    # it the host's run-ahead into the next step)
+    host = torch.tensor(offs, dtype=torch.long).pin_memory()
+    idx = host.to(lam.device, non_blocking=True)
+    blk._zero_idx_host = host  # alive until the copy has run
+    vals = lam.index_select(1, idx).to(torch.complex128)  # [bsz, 64]
+    g = torch.view_as_complex(slot.view(-1, 2)).view(blk.block_batch, 64, 64)
+    if blk.block_batch == 1:
+        g[0, :, 0] += vals.sum(0)
+    else:
+        g[:, :, 0] += vals
 
 
 def _new_state(like: torch.Tensor) -> Optional[torch.Tensor]:
