@@ -120,3 +120,15 @@ def test_choose_fusion_without_room_for_probes(monkeypatch):
     assert all(flags[i] for i, (_, idx) in enumerate(plan) if len(idx) > 1)
     plan, flags, k, costs = A.choose_fusion(wl, 20, 4, None, False, False)
     assert not any(flags)
+
+
+def test_plan_cost_uses_stored_input_adjoint_when_inputs_are_kept():
+    """With stored block inputs the tensor-core reverse step is the stored-input one (the
+    third cost entry); without it, or when the cost table predates it, the in-place one."""
+    plan = [([0, 1, 2, 3, 4, 5], [0, 1, 2]), ([0, 1, 2, 3, 4, 5], [3, 4])]
+    costs = {"dense": {str(k): (10.0, 20.0) for k in range(1, 7)}, "tc": (1.0, 2.0, 1.5), "rows": 1}
+    assert A.plan_cost(plan, costs, True, True, stored=False)[0] == 2 * (1.0 + 2.0)
+    assert A.plan_cost(plan, costs, True, True, stored=True)[0] == 2 * (1.0 + 1.5)
+    assert A.plan_cost(plan, costs, True, False, stored=True)[0] == 2 * 1.0
+    old = dict(costs, tc=(1.0, 2.0))
+    assert A.plan_cost(plan, old, True, True, stored=True)[0] == 2 * (1.0 + 2.0)

@@ -80,3 +80,55 @@ def test_engine_defaults_roundtrip():
     finally:
         tq.set_engine_defaults(**prev)
     assert D.ENGINE_DEFAULTS == prev
+
+
+def test_state_cursor_copies_only_before_writing():
+    """engine.StateCursor: the saved final state and stored block inputs are only read; the
+    first in-place uncompute works on a copy, a jump makes the cursor read-only again."""
+    from torchquantum_gb300 import engine
+
+    final = torch.arange(8, dtype=torch.float32)
+    cur = engine.StateCursor(final)
+    assert cur.state is final and not cur.owned
+    w = cur.writable()
+    assert w is not final and torch.equal(w, final) and cur.owned
+    w.zero_()
+    assert final[3] == 3.0 and cur.writable() is w
+    stored = torch.ones(8)
+    cur.jump(stored)
+    assert cur.state is stored and not cur.owned
+    assert cur.writable() is not stored
+
+
+def test_stored_inputs_move_to_the_autograd_node():
+    """Segment.take_stored_inputs hands each kept input to the caller once and keeps a weak
+    reference: a second node finds the input while the first holds it, and the input is
+    gone once every holder has dropped it."""
+    import gc
+    import types
+
+    from torchquantum_gb300 import program
+
+    a, b = types.SimpleNamespace(stored_input=torch.zeros(4)), types.SimpleNamespace(stored_input=None)
+    seg = types.SimpleNamespace(blocks=[a, b])
+    first = program.Segment.take_stored_inputs(seg)
+    assert [op for op, _ in first] == [a] and a.stored_input is None
+    held = first[0][1]
+    second = program.Segment.take_stored_inputs(seg)
+    assert len(second) == 1 and second[0][1] is held
+    del first, second, held
+    gc.collect()
+    assert a.stored_ref() is None and program.Segment.take_stored_inputs(seg) == []
+
+
+def test_expval_pass_count_follows_the_row_sweep_rule():
+    """_lib.expval_passes mirrors tqk_pauli_expval: several X-masks on rows of at most 2^24
+    amplitudes -> one row sweep per 8 strings; otherwise one pass per X-mask (8 strings
+    each)."""
+    from torchquantum_gb300 import _lib
+
+    xs = [1, 2, 3, 4, 5, 6, 7, 8, 9, 10]
+    assert _lib.expval_passes(xs, 20) == 2 and _lib.expval_passes(xs, 24) == 2
+    assert _lib.expval_passes(xs, 25) == 10
+    assert _lib.expval_passes([0] * 9, 20) == 2  # one X-mask: grouped passes
+    assert _lib.expval_passes([0, 0, 3], 26) == 2
