@@ -132,3 +132,38 @@ def test_expval_pass_count_follows_the_row_sweep_rule():
     assert _lib.expval_passes(xs, 25) == 10
     assert _lib.expval_passes([0] * 9, 20) == 2  # one X-mask: grouped passes
     assert _lib.expval_passes([0, 0, 3], 26) == 2
+
+
+def test_stored_input_policy(monkeypatch):
+    """QuantumDevice._store_block_inputs: keep block inputs only with tensor-core blocks, grad
+    mode on, something differentiable reaching the segment, and (for "auto") room in half
+    of the memory still available; True / False force the choice."""
+    import types
+
+    from torchquantum_gb300 import device as D
+
+    free = {"b": 100 << 30}
+    monkeypatch.setattr(torch.cuda, "mem_get_info", lambda dev=None: (free["b"], 280 << 30))
+    monkeypatch.setattr(torch.cuda, "memory_reserved", lambda dev=None: 10 << 30)
+    monkeypatch.setattr(torch.cuda, "memory_allocated", lambda dev=None: 4 << 30)
+    tc = types.SimpleNamespace(tc=True)
+    seg = types.SimpleNamespace(blocks=[tc, tc], diff_inputs=["theta"], stored_bytes=lambda buf: 40 << 30)
+    dev = types.SimpleNamespace(checkpoint="auto", _init=None, _tape=[], _buf=None, device="cuda:0")
+    decide = lambda s=seg: D.QuantumDevice._store_block_inputs(dev, s)
+    assert decide()                                  # 40 GiB <= (100 + 6) / 2
+    free["b"] = 60 << 30
+    assert not decide()                              # 40 GiB > (60 + 6) / 2
+    dev.checkpoint = True
+    assert decide()
+    dev.checkpoint = False
+    free["b"] = 200 << 30
+    assert not decide()
+    dev.checkpoint = "auto"
+    with torch.no_grad():
+        assert not decide()
+    assert not decide(types.SimpleNamespace(blocks=[types.SimpleNamespace(tc=False)], diff_inputs=["t"],
+                                            stored_bytes=lambda buf: 0))
+    quiet = types.SimpleNamespace(blocks=[tc], diff_inputs=[], stored_bytes=lambda buf: 1)
+    assert not decide(quiet)                         # nothing differentiable reaches it
+    dev._tape = [types.SimpleNamespace(diff_inputs=["earlier"])]
+    assert decide(quiet)                             # an earlier segment's inputs need its lam
