@@ -287,7 +287,9 @@ class Segment:
                 j.wires[i] = w
             jobs.append(j)
         table, host = _to_device_table(jobs, self.device)
-        self._keep += [table, host]
+        # the pinned staging copy must outlive its asynchronous upload (one slot per
+        # direction, so repeated reverse sweeps do not accumulate them)
+        setattr(self, "_keep_images_h" if adjoint else "_keep_images", (table, host))
         _lib.fused_prepare_many(table, len(jobs), max(b.block_batch for b in tcb))
 
     def _block_op(self, m, where):
@@ -459,7 +461,7 @@ class Segment:
             engine.adjoint_op(psi.writable(), lam, n, op, slot)
         if cross_jobs:
             table, host = _to_device_table(cross_jobs, dev)
-            self._keep_cross = [table, host, mr_of]
+            self._keep_cross = (table, host)  # the cross terms themselves are stream-ordered
             _lib.fused_cross_add_many(table, len(cross_jobs), max(j.batch for j in cross_jobs))
         if not need_grads:
             return [None] * len(self.diff_inputs)
