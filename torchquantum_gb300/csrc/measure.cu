@@ -3,11 +3,15 @@
 // <psi|P|psi> for P = (x) sigma_w is evaluated from two bit masks over the in-row
 // index: xmask (X or Y on the wire) and zmask (Z or Y), with
 //   (P psi)_i = i^{#Y} (-1)^{popcount((i ^ x) & z)} psi_{i ^ x}.
-// Strings that share an xmask are evaluated in one pass over the state (each
-// amplitude pair (i, i^x) is read once for all of them).  Each thread accumulates in
-// float32, blocks reduce in float64 and write one partial per (row, block, string) to
-// scratch; a second kernel adds the partials in a fixed order, so results are
-// bitwise reproducible run to run.
+// Strings with several xmasks on rows of up to 2^24 amplitudes are evaluated 8 at a
+// time in one sweep of the rows through L2 (k_expval_rows: each amplitude's partners
+// for all 8 strings, the rows in order so that DRAM reads the state once); otherwise
+// strings that share an xmask are evaluated in one pass over the state (each amplitude
+// pair (i, i^x) is read once for all of them).  Each thread accumulates in float32,
+// blocks reduce in float64 and write one partial per (row, block, string) to scratch;
+// a second kernel adds the partials in a fixed order, so results are bitwise
+// reproducible run to run.  The backward seed sum_s c_s P_s psi (k_pauli_apply_sum)
+// reads each output's partners for up to 64 strings in one pass.
 #include <vector>
 
 #include "common.cuh"
