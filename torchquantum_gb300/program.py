@@ -11,11 +11,14 @@ the state is read:
   per block chosen by ``autotune.choose_fusion`` from measured pass costs when
   ``fuse_wires == "auto"``), builds every block unitary in float64 with one
   ``tqk_block_build`` launch, and applies each block with the tensor-core kernel or
-  the CUDA-core dense kernel;
-* the backward walks the segment in reverse with the adjoint kernels, turns block
-  cotangents into gate-operand cotangents with ``tqk_block_unbuild``, and gate-operand
-  cotangents into parameter gradients with ``tqk_param_grads`` (analytic
-  derivatives), accumulated in float64 into one buffer per parameter base tensor.
+  the CUDA-core dense kernel -- out of place, keeping the block's input state, when a
+  backward can follow and memory allows (``QuantumDevice.checkpoint``);
+* the backward walks the segment in reverse with the adjoint kernels (a tensor-core
+  block with a stored input reads it instead of uncomputing the state; the images and
+  cotangents of all tensor-core blocks take one launch each), turns block cotangents
+  into gate-operand cotangents with ``tqk_block_unbuild``, and gate-operand cotangents
+  into parameter gradients with ``tqk_param_grads`` (analytic derivatives), accumulated
+  in float64 into one buffer per parameter base tensor.
 
 Gates with no native type (qubitunitary, multirz, qft, user matrices, ...) keep the
 torch-built operand and its autograd graph (``generic`` ops).
