@@ -7,7 +7,9 @@ significant bit), ``get_states_1d``, ``set_states``, ``clone_states``,
 every functional gate bound as a method.  Differences by design:
 
 * the state lives in one contiguous ``[bsz, 2^n]`` buffer updated in place by the
-  CUDA kernels (upstream rebuilds a permuted view per gate);
+  CUDA kernels (upstream rebuilds a permuted view per gate); with ``checkpoint``
+  (``"auto"``: when a backward can follow and memory allows) fused tensor-core blocks
+  write to new buffers and keep their inputs for the backward;
 * reading ``states`` returns a tensor connected to autograd through
   ``engine.CircuitFunction`` (adjoint-method backward) instead of a per-gate graph;
 * CUDA devices only: there is no CPU path.
