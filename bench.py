@@ -368,6 +368,8 @@ def run_ours(args):
         line["roofline"], line["kernels"] = roofline(args, dev, bool(fusion_info and fusion_info["stored_inputs"]),
                                                      live)
         line["plain_gate_pass"] = line["kernels"]["dense1_fwd"]
+        line["plain_gate_pass_summary"] = plain_pass_summary(line["kernels"], bsz * (8 << n),
+                                                             line["roofline"]["peak"])
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.quick:
         v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
@@ -383,6 +385,21 @@ def _peaks():
         return float(p["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+# gate mix of the random circuit: 60 % U3 (dense 1-wire), 40 % CNOT / CZ / CRX evenly
+PLAIN_GATE_MIX = {"dense1_fwd": 0.6, "cnot_fwd": 0.4 / 3, "cz_fwd": 0.4 / 3, "crx_fwd": 0.4 / 3}
+
+
+def plain_pass_summary(kernels: dict, state_bytes: int, peak: float) -> dict:
+    """The plain method's HBM rate over the circuit's gate mix: algorithmic bytes of an
+    average gate over its average kernel time (each kernel timed alone on the bench state),
+    and the same time against a uniform 2 S per gate (the convention CPU numbers use)."""
+    b = sum(w * kernels[k]["bytes"] for k, w in PLAIN_GATE_MIX.items())
+    t = sum(w * kernels[k]["us"] for k, w in PLAIN_GATE_MIX.items()) / 1e6
+    return {"GB/s": b / t / 1e9, "frac": b / t / 1e9 / peak, "us_per_gate": t * 1e6,
+            "uniform_2S_GB/s": 2 * state_bytes / t / 1e9,
+            "mix": "60% U3, 13.3% each CNOT / CZ / CRX; bytes 2 S / S / S/2 / S per pass"}
 
 
 class LaunchTimer:
