@@ -112,12 +112,13 @@ int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uint64_t* xmas
  * allocates nothing.  For callers that cannot allocate: a host binding this C ABI over
  * FFI that holds only raw pointers to its own buffers and has no device allocator, or
  * a service held to a fixed device-memory budget.  No counterpart in the upstream
- * project.  Limits: partials (tqk_pauli_expval_scratch_bytes) must fit
- * tqk_pauli_expval_noalloc_capacity() bytes and m <= 4096, else
+ * project.  Limits: its partials, bsz * min(ceil(1216 / bsz), ceil(2^n / 1024)) * 64
+ * bytes (one pass per distinct X-mask), must fit tqk_pauli_expval_noalloc_capacity()
+ * bytes (1 MiB: up to bsz = 16384 at n <= 10, bsz = 1216 at any n) and m <= 4096, else
  * TQK_SCRATCH_TOO_SMALL / TQK_BAD_SHAPE.  Calls that overlap on the GPU race on the
  * shared array.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress, device current); make that first call before any stream
- * capture. */
+ * (cudaGetSymbolAddress, device current) and caches it per CUDA context; make that
+ * first call before any stream capture (and again after a device reset). */
 int64_t tqk_pauli_expval_noalloc_capacity(void);
 int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, const uint64_t* xmask,
                              const uint64_t* zmask, int m, double* out, void* stream);

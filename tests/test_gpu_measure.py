@@ -122,13 +122,14 @@ def test_row_sweep_expvals(n, bsz, m):
     st = torch.tensor(s, dtype=torch.complex64, device="cuda")
     got = _lib.pauli_expval(st, n, list(xs), list(zs))
     lib = _lib.load()
-    ref = torch.full((bsz, m), float("nan"), dtype=torch.float64, device="cuda")
+    per_mask = torch.full((bsz, m), float("nan"), dtype=torch.float64, device="cuda")
     rc = lib.tqk_pauli_expval_noalloc(st.data_ptr(), bsz, n, _lib._u64(list(xs)), _lib._u64(list(zs)), m,
-                                      ref.data_ptr(), torch.cuda.current_stream().cuda_stream)
+                                      per_mask.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == 0, lib.tqk_last_error().decode()
     torch.cuda.synchronize()
-    assert (got - ref).abs().max().item() < 2e-6
+    assert (got - per_mask).abs().max().item() < 2e-6
     if n <= 14:
         s64 = st.cpu().numpy().astype(np.complex128)
         want = np.stack([O.expval_pauli(s64, p, n) for p in strings], -1)
         assert np.abs(got.cpu().numpy() - want).max() < 1e-6
+        assert np.abs(per_mask.cpu().numpy() - want).max() < 1e-6

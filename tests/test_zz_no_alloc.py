@@ -34,7 +34,7 @@ def _noalloc(lib, st, n, xs, zs):
     return out
 
 
-@pytest.mark.parametrize("n,bsz,m", [(12, 3, 20), (20, 16, 9)])
+@pytest.mark.parametrize("n,bsz,m", [(12, 3, 20), (20, 16, 9), (20, 32, 9), (20, 128, 5)])
 def test_noalloc_matches_scratch_entry_point_twice(n, bsz, m):
     lib = _lib.load()
     rng = np.random.default_rng(n + bsz)
@@ -63,5 +63,29 @@ def test_noalloc_rejects_oversized_calls():
     assert rc == 2 and b"exceed the limit" in lib.tqk_last_error()
     big = torch.zeros(20000, 1 << 10, dtype=torch.complex64, device="cuda")  # 20000 rows of partials > 1 MiB
     rc = lib.tqk_pauli_expval_noalloc(big.data_ptr(), 20000, 10, _lib._u64([0]), _lib._u64([1]), 1,
+                                      out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 7 and b"static array holds" in lib.tqk_last_error()
+
+
+def test_noalloc_capacity_boundary():
+    """The largest call whose partials fill the 1 MiB array exactly is accepted and
+    matches the scratch entry point; one more row is rejected before any launch.
+    At n = 10 each row has one block of partials (8 doubles = 64 B), so 16384 rows fill
+    1 MiB."""
+    lib = _lib.load()
+    rng = np.random.default_rng(3)
+    n = 10
+    strings = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(3)] + ["Z" * n]
+    xs, zs = zip(*[pauli_masks(p, n) for p in strings])
+    st = _state(rng, 16384, n)
+    ref = _lib.pauli_expval(st, n, list(xs), list(zs))
+    got = _noalloc(lib, st, n, list(xs), list(zs))
+    torch.cuda.synchronize()
+    assert not torch.isnan(got).any()
+    assert (got - ref).abs().max().item() < 2e-6
+    del st
+    big = torch.zeros(16385, 1 << n, dtype=torch.complex64, device="cuda")
+    out = torch.zeros(16385, 1, dtype=torch.float64, device="cuda")
+    rc = lib.tqk_pauli_expval_noalloc(big.data_ptr(), 16385, n, _lib._u64([0]), _lib._u64([1]), 1,
                                       out.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == 7 and b"static array holds" in lib.tqk_last_error()

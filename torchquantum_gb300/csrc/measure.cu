@@ -12,6 +12,8 @@
 // a second kernel adds the partials in a fixed order, so results are bitwise
 // reproducible run to run.  The backward seed sum_s c_s P_s psi (k_pauli_apply_sum)
 // reads each output's partners for up to 64 strings in one pass.
+#include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -548,10 +550,12 @@ extern "C" int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const 
 // allocator to draw from, or a service that runs inside a fixed device-memory budget
 // where the library must not call cudaMalloc.  Its block partials live in the
 // file-scope array below instead of caller scratch, so the call allocates nothing,
-// neither device memory nor host heap.
+// neither device memory nor host heap.  It always makes one pass per distinct X-mask.
 //
 // Limits: the partials must fit kNoAllocScratchBytes (1 MiB): bsz * blocks_per_row * 8
-// doubles, where blocks_per_row = min(ceil(1216 / bsz), ceil(2^n / 1024)); and at most
+// doubles, where blocks_per_row = min(ceil(1216 / bsz), ceil(2^n / 1024)) -- so any
+// bsz <= 16384 fits at n <= 10, and at every n up to bsz = 1216 (bsz * 1216 rounded up
+// to a multiple of bsz stays below 16384 rows of partials); and at most
 // kNoAllocMaxStrings strings per call.  Larger calls are rejected with
 // TQK_SCRATCH_TOO_SMALL / TQK_BAD_SHAPE before any launch.
 //
@@ -560,9 +564,12 @@ extern "C" int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const 
 // earlier in the same call.  Calls whose kernels overlap on the GPU (different
 // streams, or different host threads without ordering) race on the array.
 //
-// Set-up: the first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (the device must be current) and caches it; make that first
-// call before any stream capture.
+// Set-up: the first call on each device (with that device current) looks up the
+// array's device address with cudaGetSymbolAddress and caches it, keyed by the CUDA
+// context that was current; make that first call before any stream capture.  A call
+// made in a different context of the device (after cudaDeviceReset, or under another
+// context made current by the driver API) looks the address up again.  The cache is
+// safe to fill from several host threads at once.
 namespace tqk {
 
 constexpr int64_t kNoAllocScratchBytes = 1 << 20;
@@ -571,21 +578,68 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocScratchBytes / sizeof(double)];
 
-static void* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+// Partials the pass loop below writes: one region of [bsz][blocks_per_row][8] doubles,
+// reused by every pass (the stream orders them).
+static int64_t noalloc_partial_bytes(int64_t bsz, int n) {
+  return bsz * reduce_blocks_per_row(bsz, n) * kMaxStringsPerPass * static_cast<int64_t>(sizeof(double));
+}
+
+// Identity of the context current on this thread (0 when none is current or the driver
+// entry points are unavailable, in which case the address is looked up on every call).
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+
+static unsigned long long current_context_id() {
+  static std::once_flag once;
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  if (get_current == nullptr || get_id == nullptr) return 0;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || ctx == nullptr) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+struct NoAllocSlot {
+  std::atomic<unsigned long long> ctx{0};  // context the address was looked up in
+  std::atomic<void*> ptr{nullptr};
+};
+static NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mutex;
 
 static int noalloc_scratch(void** out, const char* what) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(TQK_CUDA_ERROR, "%s: cudaGetDevice failed", what);
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(TQK_UNSUPPORTED, "%s: device %d beyond %d", what, dev,
                                                         kNoAllocMaxDevices);
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-    if (e != cudaSuccess || p == nullptr)
-      return fail(TQK_CUDA_ERROR, "%s: cudaGetSymbolAddress failed: %s", what, cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
+  NoAllocSlot& slot = g_noalloc_slot[dev];
+  const unsigned long long ctx = current_context_id();
+  if (ctx != 0 && slot.ctx.load(std::memory_order_acquire) == ctx) {
+    *out = slot.ptr.load(std::memory_order_acquire);
+    return TQK_OK;
   }
-  *out = g_noalloc_ptr[dev];
+  std::lock_guard<std::mutex> guard(g_noalloc_mutex);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+  if (e != cudaSuccess || p == nullptr)
+    return fail(TQK_CUDA_ERROR, "%s: cudaGetSymbolAddress failed: %s", what, cudaGetErrorString(e));
+  // the lookup makes the device's primary context current if none was: key by the
+  // context seen afterwards; the address is published before the key
+  slot.ptr.store(p, std::memory_order_release);
+  slot.ctx.store(current_context_id(), std::memory_order_release);
+  *out = p;
   return TQK_OK;
 }
 
@@ -602,7 +656,7 @@ extern "C" int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, c
   if (m > kNoAllocMaxStrings)
     return fail(TQK_BAD_SHAPE, "%s: %d strings exceed the limit of %d per call", what, m, kNoAllocMaxStrings);
   if (!xmask || !zmask || !out) return fail(TQK_BAD_POINTER, "%s: null mask/output pointer", what);
-  const int64_t need = tqk_pauli_expval_scratch_bytes(bsz, n, m);
+  const int64_t need = noalloc_partial_bytes(bsz, n);
   if (need > kNoAllocScratchBytes)
     return fail(TQK_SCRATCH_TOO_SMALL, "%s: needs %lld bytes of partials, the static array holds %lld (reduce bsz)",
                 what, (long long)need, (long long)kNoAllocScratchBytes);
