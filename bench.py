@@ -12,10 +12,10 @@ the public API with the angles copied from pinned host memory and the expvals an
 gradients copied back every step.  The state (2 GiB) is larger than L2 (129 MB), so no
 flush is needed between steps.
 
-``--impl reference`` times the CPU oracle's restatement of the upstream algorithm
-(torch-autograd-style forward keeping every gate's input state, then the reverse
-sweep) on the host cores, on a bounded sample of the same circuit, extrapolated to
-circuits/s.
+``--impl reference`` times upstream torchquantum itself (the offline install in
+``baseline/_ref``: its gate functions, ``apply_unitary_bmm`` and torch autograd on the
+host cores, every host thread) on a bounded sample of the same circuit, extrapolated to
+circuits/s; without that install it times the oracle's numpy restatement instead.
 """
 from __future__ import annotations
 
@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--bsz", type=int, default=16)
     ap.add_argument("--depth", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations' summaries (c1, c3, c4, c5) in the headline line")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the baseline sample")
     ap.add_argument("--fuse", default="auto", help="fused block width 1..6 or auto (autotuner)")
     ap.add_argument("--kernels", action="store_true",
@@ -73,7 +75,31 @@ def dist_env():
     return rank_env()
 
 
-# ------------------------------------------------------------------ CPU (oracle) leg
+# ------------------------------------------------------------------ CPU legs
+def cpu_model() -> str:
+    """CPU model of this host (x86 "model name", or the Arm implementer/part ids)."""
+    info = {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if ":" in line:
+                    k, v = line.split(":", 1)
+                    info.setdefault(k.strip(), v.strip())
+    except OSError:
+        pass
+    if "model name" in info:
+        return info["model name"]
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    parts = [f"{k} {info[k]}" for k in ("CPU implementer", "CPU part") if k in info]
+    return ", ".join(parts) or "unknown"
+
+
 def cpu_sample(args, seconds: float):
     """Time the oracle's autograd-style fwd + reverse sweep on one circuit of the
     workload (bsz 1) over the first G gates, G sized to ~``seconds``; returns
@@ -107,50 +133,351 @@ def cpu_sample(args, seconds: float):
     return 1.0 / per_circuit, desc, threads, g, t
 
 
+class UpstreamStep:
+    """The headline step run by upstream torchquantum itself on the host cores.
+
+    Gates go through upstream's own public path: ``tqf.u3 / cnot / cz / crx`` on an
+    upstream ``QuantumDevice`` (``torchquantum/functional/gate_wrapper.py:324-446`` ->
+    ``apply_unitary_bmm``, ``:96-140``), and torch autograd differentiates them with
+    respect to the per-sample angles, as an upstream training step does.  The 8 Pauli
+    expvals cannot use upstream's ``expval_joint_analytical`` at n = 24 (it builds a dense
+    2^n x 2^n matrix, ``measurement/measurements.py:232-279``), so they use the same
+    sum over amplitude pairs as the engine, written with torch ops on the host and
+    differentiated by autograd; the probabilities are ``|psi|^2`` of the final state.
+    A step of the sample is ``gates_per_step`` consecutive gates of the circuit (the
+    window advances every step) forward + backward on a fresh device; the measurement
+    (forward + backward) is timed once.  Circuits/s = bsz / (measurement time + depth x
+    mean time per gate)."""
+
+    def __init__(self, args):
+        import torch
+
+        from oracle import upstream as U
+        from oracle import statevec as O
+        from torchquantum_gb300 import workloads as W
+
+        self.torch = torch
+        self.tq = U.import_upstream()
+        import torchquantum.functional as tqf  # upstream's gate functions
+
+        self.fns = {"u3": tqf.u3, "cnot": tqf.cnot, "cz": tqf.cz, "crx": tqf.crx}
+        self.n, self.bsz, self.depth = args.n, args.bsz, args.depth
+        self.gates, ncols = W.random_circuit(args.n, args.depth, seed=0)
+        self.theta = torch.tensor(W.random_params(args.bsz, ncols, seed=1))
+        self.paulis = W.random_paulis(args.n, 8, seed=2)
+        self.pw = torch.tensor(np.random.default_rng(3).normal(size=(1, 8)), dtype=torch.float32)
+        self.masks = [O.pauli_masks(p, args.n) for p in self.paulis]
+        self.pos = 0
+
+    def gates_fwd_bwd(self, g: int) -> float:
+        """Wall seconds of g consecutive gates (forward + autograd backward)."""
+        torch = self.torch
+        th = self.theta.clone().requires_grad_(True)
+        t0 = time.perf_counter()
+        q = self.tq.QuantumDevice(n_wires=self.n, bsz=self.bsz)
+        # in the full circuit nearly every gate follows a parameterised one, so its
+        # backward propagates the state cotangent: make the window's input differentiable
+        q.states.requires_grad_(True)
+        for k in range(g):
+            gd = self.gates[(self.pos + k) % self.depth]
+            p = th[:, gd["off"]:gd["off"] + gd["np"]] if gd["np"] else None
+            self.fns[gd["name"]](q, wires=gd["wires"], params=p)
+        s = q.get_states_1d()
+        s[:, :1].abs().pow(2).sum().backward()
+        dt = time.perf_counter() - t0
+        self.pos = (self.pos + g) % self.depth
+        del q, s, th
+        return dt
+
+    def _tables(self, strings):
+        torch = self.torch
+        idx = torch.arange(1 << self.n, dtype=torch.int64)
+        out = []
+        for j in strings:
+            x, z, ny = self.masks[j]
+            src = idx ^ x
+            v, par = src & z, torch.zeros_like(idx)
+            for b in range(self.n):
+                par ^= (v >> b) & 1
+            ph = (1j ** ny) * (1.0 - 2.0 * par.to(torch.float32))
+            out.append((j, src, ph.to(torch.complex64)))
+        return out
+
+    def measurement_fwd_bwd(self, strings) -> float:
+        """Wall seconds of probs + the given strings' expvals, forward + backward, on a
+        normalised random state (the observables' index tables are built beforehand)."""
+        torch = self.torch
+        tabs = self._tables(strings)
+        g = torch.Generator().manual_seed(4)
+        s = torch.randn(self.bsz, 1 << self.n, dtype=torch.complex64, generator=g)
+        s = (s / s.abs().pow(2).sum(1, keepdim=True).sqrt()).requires_grad_(True)
+        t0 = time.perf_counter()
+        pr = s.abs() ** 2
+        ev = torch.stack([(s.conj() * ph * s[:, src]).sum(1).real for _, src, ph in tabs], 1)
+        loss = (ev * self.pw[:, [j for j, _, _ in tabs]]).sum() + 0.0 * pr[:, 0].sum()
+        loss.backward()
+        dt = time.perf_counter() - t0
+        del s, pr, ev, loss, tabs
+        return dt
+
+
+def upstream_cpu_baseline(args, seconds: float):
+    """cpu_baseline of our arm: upstream on the host cores, a bounded sample (about
+    ``seconds`` of gates plus one string's measurement, scaled to 8)."""
+    import torch
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    up = UpstreamStep(args)
+    c0, w0 = time.process_time(), time.perf_counter()
+    t1 = up.gates_fwd_bwd(1)
+    g = int(max(1, min(8, seconds / max(t1, 1e-6))))
+    tg = up.gates_fwd_bwd(g)
+    tm = up.measurement_fwd_bwd([0]) * 8
+    cores = round((time.process_time() - c0) / max(time.perf_counter() - w0, 1e-9), 2)
+    value = args.bsz / (tm + args.depth * tg / g)
+    desc = (f"upstream torchquantum 0.1.8 (torch CPU, complex64, autograd) on {os.cpu_count()} threads of "
+            f"{cpu_model()}: {g} gates of the circuit fwd+bwd at n={args.n} bsz={args.bsz} in {tg:.1f} s, "
+            f"1 of the 8 Pauli expvals fwd+bwd in {tm / 8:.1f} s (x8); circuits/s = bsz / (8 expvals + "
+            f"{args.depth} x time per gate)")
+    return value, desc, cores
+
+
+def _peak_rss_reset() -> None:
+    """Reset this process's peak resident set (VmHWM) so the next reading covers only
+    what follows (Linux: writing 5 to /proc/self/clear_refs)."""
+    try:
+        with open("/proc/self/clear_refs", "w") as f:
+            f.write("5")
+    except OSError:
+        pass
+
+
+def _peak_rss_bytes() -> int:
+    try:
+        with open("/proc/self/status") as f:
+            for line in f:
+                if line.startswith("VmHWM:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def upstream_c1_baseline(steps: int = 30) -> dict:
+    """Upstream's own CPU path for the n=4 model (GeneralEncoder + 2 x (Op1QAllLayer(U3) +
+    Op2QAllLayer(CNOT, circular)), 4 x expval_joint_analytical, bsz 32), fwd + autograd bwd."""
+    import torch
+
+    from oracle import upstream as U
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    tq = U.import_upstream()
+    from torchquantum.measurement import expval_joint_analytical
+
+    funcs = ["rx", "ry", "rz", "rx"]
+    enc = tq.GeneralEncoder([{"input_idx": [4 * g + w], "func": funcs[g], "wires": [w]} for g in range(4)
+                             for w in range(4)])
+    layers = []
+    for _ in range(2):
+        layers += [tq.layer.Op1QAllLayer(op=tq.U3, n_wires=4, has_params=True, trainable=True),
+                   tq.layer.Op2QAllLayer(op=tq.CNOT, n_wires=4, circular=True)]
+    model = torch.nn.ModuleList([enc] + layers)
+    x = torch.rand(32, 16, generator=torch.Generator().manual_seed(0)) * np.pi
+    obs = ["".join("Z" if i == j else "I" for i in range(4)) for j in range(4)]
+
+    def step():
+        model.zero_grad(set_to_none=True)
+        q = tq.QuantumDevice(n_wires=4, bsz=32)
+        enc(q, x)
+        for lay in layers:
+            lay(q)
+        torch.stack([expval_joint_analytical(q, o) for o in obs], -1).sum().backward()
+
+    for _ in range(3):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": 32 / dt, "unit": UNIT, "ms_per_step": dt * 1e3, "cores": os.cpu_count(),
+            "kind": "reference", "cpu_model": cpu_model(),
+            "sample": f"upstream torchquantum 0.1.8, the same model fwd+bwd, {steps} steps after 3 warm-up"}
+
+
+def upstream_c4_baseline(specs, angles, seconds: float = 20.0) -> dict:
+    """Upstream's CPU path for the 256 uneven circuits: a Python loop, one upstream
+    QuantumDevice per circuit (RY, RZ per wire, CZ ladder per layer through tqf), <Z_0> by
+    tq.expval (measurements.py:282-312).  Circuits are timed in a seeded random order
+    until ``seconds`` have passed; the total is extrapolated by gate work (layers x gates
+    per layer x 2^n)."""
+    import torch
+
+    from oracle import upstream as U
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    tq = U.import_upstream()
+    import torchquantum.functional as tqf
+
+    def cost(i):
+        n, L = specs[i]
+        return L * (3 * n - 1) * (1 << n)
+
+    order = np.random.default_rng(5).permutation(len(specs))
+    done, spent, lat = [], 0.0, []
+    with torch.no_grad():
+        for i in order:
+            (n, L), (ry, rz) = specs[i], angles[i]
+            t0 = time.perf_counter()
+            q = tq.QuantumDevice(n_wires=n, bsz=1)
+            for l in range(L):
+                for w in range(n):
+                    tqf.ry(q, wires=w, params=float(ry[l, w]))
+                    tqf.rz(q, wires=w, params=float(rz[l, w]))
+                for w in range(n - 1):
+                    tqf.cz(q, wires=[w, w + 1])
+            tq.expval(q, 0, tq.PauliZ())
+            dt = time.perf_counter() - t0
+            done.append(int(i))
+            lat.append(dt)
+            spent += dt
+            if spent > seconds:
+                break
+    rate = sum(cost(i) for i in done) / spent
+    total = sum(cost(i) for i in range(len(specs))) / rate
+    return {"value": len(specs) / total, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+            "cpu_model": cpu_model(),
+            "sample": f"upstream torchquantum 0.1.8, {len(done)} of {len(specs)} circuits one at a time in "
+                      f"{spent:.1f} s (forward, no grad), total extrapolated by gate work L x (3n - 1) x 2^n",
+            "sample_latency_ms": {"p50": float(np.percentile(lat, 50)) * 1e3,
+                                  "p99": float(np.percentile(lat, 99)) * 1e3}}
+
+
+def upstream_c5_baseline(batches=(1, 4)) -> dict:
+    """Upstream autograd for the differentiation workload (n=20, 10 layers of RY, RZ per
+    wire + CZ ladder after the per-sample RY input layer, 400 shared angles, 50 weighted
+    Pauli strings) at reduced bsz: upstream's tqf gates with torch autograd on the host;
+    the 50 expvals as the torch sum over amplitude pairs (upstream's dense-kron
+    expval_joint_analytical needs a 2^20 x 2^20 matrix).  Peak RSS per bsz."""
+    import torch
+
+    from oracle import upstream as U
+    from oracle import statevec as O
+    from torchquantum_gb300 import workloads as W
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    tq = U.import_upstream()
+    import torchquantum.functional as tqf
+
+    n, layers, m = 20, 10, 50
+    gates, ncols = W.hea_circuit(n, layers)
+    rng = np.random.default_rng(7)
+    theta0 = rng.uniform(-np.pi, np.pi, size=(1, ncols)).astype(np.float32)
+    x = rng.uniform(0, np.pi, size=(64, n)).astype(np.float32)
+    paulis = W.random_paulis(n, m, seed=8)
+    w = torch.tensor(rng.normal(size=m).astype(np.float32))
+    idx = torch.arange(1 << n, dtype=torch.int64)
+    tabs = []
+    for pstr in paulis:
+        xm, zm, ny = O.pauli_masks(pstr, n)
+        src = idx ^ xm
+        v, par = src & zm, torch.zeros_like(idx)
+        for b in range(n):
+            par ^= (v >> b) & 1
+        tabs.append((src, ((1j ** ny) * (1.0 - 2.0 * par.to(torch.float32))).to(torch.complex64)))
+    fns = {"ry": tqf.ry, "rz": tqf.rz, "cz": tqf.cz}
+    out = {}
+    for bsz in batches:
+        th = torch.tensor(theta0, requires_grad=True)
+        xt = torch.tensor(x[:bsz])
+        _peak_rss_reset()
+        t0 = time.perf_counter()
+        q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+        for wi in range(n):
+            tqf.ry(q, wires=wi, params=xt[:, wi:wi + 1])
+        for g in gates:
+            p = th[:, g["off"]:g["off"] + g["np"]] if g["np"] else None
+            fns[g["name"]](q, wires=g["wires"], params=p)
+        s = q.get_states_1d()
+        ev = torch.stack([(s.conj() * ph * s[:, src]).sum(1).real for src, ph in tabs], 1)
+        (ev * w).sum().backward()
+        dt = time.perf_counter() - t0
+        out[f"bsz{bsz}"] = {"circuits_per_s": bsz / dt, "s_per_step": dt, "peak_rss_bytes": _peak_rss_bytes()}
+        del q, s, ev, th
+    best = max(v["circuits_per_s"] for v in out.values())
+    return {"value": best, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference", "cpu_model": cpu_model(),
+            "sample": "upstream torchquantum 0.1.8 autograd, one fwd+bwd step per bsz in "
+                      f"{list(batches)} (bsz=64 would need ~317 GB of saved states); value = the better bsz",
+            "per_bsz": out}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    w = args.warmup
-    from oracle import statevec as O
-    from torchquantum_gb300 import workloads as W
+    import torch
 
-    gates, ncols = W.random_circuit(args.n, args.depth, seed=0)
-    theta = W.random_params(1, ncols, seed=1)
-    og = W.oracle_gates(gates, theta)
+    torch.set_num_threads(os.cpu_count() or 1)
+    from oracle import upstream as U
 
-    def one(g):
-        s, saved, mats = O.forward_saving(args.n, 1, og[:g], np.complex64)
-        O.backward_sweep(args.n, og[:g], saved, mats, s.copy())
+    c_start, t_run0 = time.process_time(), time.perf_counter()
+    if U.available():
+        up = UpstreamStep(args)
+        t_meas = up.measurement_fwd_bwd(range(8))
+        t1 = up.gates_fwd_bwd(1)
+        # gates per step sized so warm-up + timed steps take about three minutes
+        budget = 180.0 / max(1, args.steps + args.warmup)
+        g = int(max(1, min(8, budget / max(t1, 1e-6))))
+        for _ in range(args.warmup):
+            up.gates_fwd_bwd(g)
+        times = [up.gates_fwd_bwd(g) for _ in range(args.steps)]
+        per_step = sum(times) / len(times)
+        value = args.bsz / (t_meas + args.depth * per_step / g)
+        method = ("upstream torchquantum 0.1.8 itself (baseline/_ref, imported with stand-ins for its absent "
+                  "optional deps): tqf gates -> gate_wrapper -> apply_unitary_bmm with torch autograd, torch CPU, "
+                  "complex64; Pauli expvals as a torch sum over amplitude pairs (upstream's dense-kron "
+                  "expval_joint_analytical needs a 2^24 x 2^24 matrix)")
+        sample = (f"each step: {g} consecutive gates of the circuit (window advancing) fwd+bwd at n={args.n} "
+                  f"bsz={args.bsz}; probs + 8 expvals fwd+bwd timed once ({t_meas:.1f} s); circuits/s = bsz / "
+                  f"(expvals + {args.depth} x mean time per gate)")
+        kind = "reference"
+    else:
+        # upstream not installed: the oracle's restatement of its algorithm
+        from oracle import statevec as O
+        from torchquantum_gb300 import workloads as W
 
-    c_start = time.process_time()
+        gates, ncols = W.random_circuit(args.n, args.depth, seed=0)
+        og = W.oracle_gates(gates, W.random_params(1, ncols, seed=1))
 
-    t0 = t_run0 = time.perf_counter()
-    one(1)
-    t1 = time.perf_counter() - t0
-    # each step is a bounded sample sized so steps+warmup fit in ~3 minutes
-    budget = 180.0 / max(1, args.steps + w)
-    g = int(max(1, min(args.depth, budget / max(t1, 1e-6))))
-    for _ in range(w):
-        one(g)
-    times = []
-    for _ in range(args.steps):
+        def one(g):
+            s, saved, mats = O.forward_saving(args.n, 1, og[:g], np.complex64)
+            O.backward_sweep(args.n, og[:g], saved, mats, s.copy())
+
         t0 = time.perf_counter()
-        one(g)
-        times.append(time.perf_counter() - t0)
-    per_step = sum(times) / len(times)
-    value = 1.0 / (per_step / g * args.depth)
-    # cores actually used: process CPU time over the whole run / its wall time
+        one(1)
+        t1 = time.perf_counter() - t0
+        budget = 180.0 / max(1, args.steps + args.warmup)
+        g = int(max(1, min(args.depth, budget / max(t1, 1e-6))))
+        for _ in range(args.warmup):
+            one(g)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            one(g)
+            times.append(time.perf_counter() - t0)
+        per_step = sum(times) / len(times)
+        value = 1.0 / (per_step / g * args.depth)
+        method = ("upstream algorithm restated on the host (numpy complex64, autograd-style forward keeping "
+                  "per-gate states, then the reverse sweep); upstream itself not installed in baseline/_ref")
+        sample = f"1 circuit, first {g} of {args.depth} gates fwd+bwd per step, extrapolated"
+        kind = "port"
     threads = round((time.process_time() - c_start) / max(time.perf_counter() - t_run0, 1e-9), 2)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": _config(args), "impl": "reference",
-        "method": "upstream algorithm restated on the host (numpy complex64, autograd-style forward "
-                  "keeping per-gate states, then the reverse sweep)",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"1 circuit, first {g} of {args.depth} gates fwd+bwd per step, extrapolated"},
+        "config": _config(args), "impl": "reference", "method": method,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+                         "cpu_model": cpu_model(), "host_threads": os.cpu_count()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -371,11 +698,95 @@ def run_ours(args):
         line["plain_gate_pass_summary"] = plain_pass_summary(line["kernels"], bsz * (8 << n),
                                                              line["roofline"]["peak"])
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.quick:
-        v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+        from oracle import upstream as U
+
+        if U.available():
+            v, desc, threads = upstream_cpu_baseline(args, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "reference", "sample": desc,
+                                    "cpu_model": cpu_model()}
+        v, desc, threads, g, tcpu = cpu_sample(args, args.cpu_seconds / 2)
+        port = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc, "cpu_model": cpu_model()}
+        line.setdefault("cpu_baseline", port)
+        if line["cpu_baseline"] is not port:
+            line["cpu_baseline_port"] = port
+    if rank == 0 and world == 1 and not args.quick and not args.no_configs:
+        line["configs"] = other_configs(args)
     R.finish()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def upstream_forward_sample(n: int, bsz: int, depth: int, gates_timed: int = 3) -> dict:
+    """Upstream's gate-by-gate forward of the random circuit (no grad) on the host:
+    ``gates_timed`` gates timed after one warm-up gate, extrapolated to ``depth``."""
+    import torch
+
+    from oracle import upstream as U
+    from torchquantum_gb300 import workloads as W
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    tq = U.import_upstream()
+    import torchquantum.functional as tqf
+
+    fns = {"u3": tqf.u3, "cnot": tqf.cnot, "cz": tqf.cz, "crx": tqf.crx}
+    gates, ncols = W.random_circuit(n, depth, seed=0)
+    th = torch.tensor(W.random_params(bsz, ncols, seed=1))
+    with torch.no_grad():
+        q = tq.QuantumDevice(n_wires=n, bsz=bsz)
+        times = []
+        for g in gates[:gates_timed + 1]:
+            t0 = time.perf_counter()
+            fns[g["name"]](q, wires=g["wires"], params=th[:, g["off"]:g["off"] + g["np"]] if g["np"] else None)
+            times.append(time.perf_counter() - t0)
+        del q
+    per_gate = sum(times[1:]) / gates_timed
+    return {"value": bsz / (per_gate * depth), "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+            "cpu_model": cpu_model(),
+            "sample": f"upstream torchquantum 0.1.8 forward gate by gate at n={n} bsz={bsz}: {gates_timed} gates "
+                      f"timed ({per_gate:.2f} s per gate), extrapolated to {depth} gates"}
+
+
+def other_configs(args) -> dict:
+    """The other configurations measured in the same run (short: a few steps each), each
+    with upstream's own CPU path timed on the host as its baseline (when upstream is
+    installed)."""
+    import copy
+
+    import torch
+
+    from oracle import upstream as U
+
+    a = copy.copy(args)
+    a.steps, a.warmup = min(args.steps, 10), 3
+    have_up = U.available()
+    out = {}
+
+    def keep(d, keys):
+        return {k: d[k] for k in keys if k in d}
+
+    c1 = run_c1(a, emit=False)
+    out["c1"] = keep(c1, ("value", "unit", "ms_per_step", "config", "p50_ms", "p99_ms"))
+    if have_up:
+        out["c1"]["cpu_baseline"] = upstream_c1_baseline()
+    torch.cuda.empty_cache()
+    c3 = run_c3(a, emit=False)
+    out["c3"] = keep(c3, ("value", "unit", "ms_per_step", "config", "cases"))
+    if have_up:
+        out["c3"]["cpu_baseline"] = upstream_forward_sample(26, 8, args.depth)
+    torch.cuda.empty_cache()
+    c4 = run_c4(a, emit=False)
+    out["c4"] = keep(c4, ("value", "unit", "ms_per_step", "config", "e2e", "latency_ms", "batch_kernel",
+                          "default_launch_shape", "engine_one_circuit_at_a_time"))
+    if have_up:
+        specs, angles = c4_workload(np.random.default_rng(0))
+        out["c4"]["cpu_baseline"] = upstream_c4_baseline(specs, angles)
+    torch.cuda.empty_cache()
+    c5 = run_c5(a, emit=False)
+    out["c5"] = keep(c5, ("value", "unit", "ms_per_step", "config", "variants"))
+    if have_up:
+        out["c5"]["cpu_baseline"] = upstream_c5_baseline()
+    torch.cuda.empty_cache()
+    return out
 
 
 def _peaks():
@@ -484,10 +895,10 @@ def roofline(args, dev, stored=True, live=None):
     tb = min(n, _lib.STAGED_MAX_TILE_BITS)
     kernels["staged8_fwd"] = (lambda i: _lib.staged_apply(psi, n, sdescs, tb), 2 * S)
     kernels["staged8_adj"] = (lambda i: _lib.staged_adjoint(psi, lam, n, sdescs_g, tb), 4 * S)
-    # the bench step's measurement kernels: 8 Pauli expvals (rows of up to 2^24 amplitudes:
-    # one row sweep, own + 8 partner loads per amplitude = 9 S loaded, mostly from L2;
-    # longer rows: one pass per X-mask, 8 S read) and the backward seed sum_j c_j P_j psi
-    # (8 partner reads + 1 write: 9 S)
+    # the bench step's measurement kernels, at the algorithmic bytes of the unit: 8 Pauli
+    # expvals fused in one pass read the state once (S); the backward seed
+    # sum_j c_j P_j psi reads it and writes the result (2 S).  Strings with different
+    # X-masks run as coset passes (partners read from shared memory): one pass per group
     from torchquantum_gb300.measurement import pauli_masks
     from torchquantum_gb300 import workloads as W
 
@@ -495,13 +906,16 @@ def roofline(args, dev, stored=True, live=None):
     xs = [pauli_masks(o, n)[0] for o in strings]
     zs = [pauli_masks(o, n)[1] for o in strings]
     coef = torch.ones(bsz, 8, dtype=torch.float32, device=dev)
-    rows = n <= _lib.ROWS_MAX_WIRES and len(set(xs)) > 1
-    kernels["expval8"] = (lambda i: _lib.pauli_expval(psi, n, xs, zs), (1 + len(xs)) * S if rows else len(set(xs)) * S)
-    kernels["apply_sum8"] = (lambda i: _lib.pauli_apply_sum(psi, n, xs, zs, coef), 9 * S)
+    kernels["expval8"] = (lambda i: _lib.pauli_expval(psi, n, xs, zs), S)
+    kernels["apply_sum8"] = (lambda i: _lib.pauli_apply_sum(psi, n, xs, zs, coef), 2 * S)
     for name, (fn, nbytes) in kernels.items():
         t = timeit(fn)
         gbs = nbytes / t / 1e9
         res[name] = {"us": t * 1e6, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak}
+    for name in ("expval8", "apply_sum8"):
+        res[name]["passes"] = _lib.expval_passes(xs, n) if name == "expval8" else len(_lib.coset_groups(xs, n))
+        # shared-memory reads of the coset passes: own pair + one partner pair per string
+        res[name]["smem_loads_GB/s"] = (9 if name == "expval8" else 8) * S / (res[name]["us"] / 1e6) / 1e9
     if n >= 13:
         # fused 6-wire block on the tensor cores: forward (2S) and adjoint step (4S) per launch
         rng = np.random.default_rng(0)
@@ -581,15 +995,19 @@ def _timed(fn, steps, warmup, dev):
     return ev[0].elapsed_time(ev[-1]), per
 
 
-def _line(args, workload_cfg, value, ms, extra):
+def _line(args, workload_cfg, value, ms, extra, emit=True):
+    """The workload's result: printed as its own JSON line (``--workload cN``), or
+    returned as a summary for the headline line's ``configs``."""
     d = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
          "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
          "dtype": "c64", "data": "synthetic", "config": workload_cfg}
     d.update(extra)
-    print(json.dumps(d), flush=True)
+    if emit:
+        print(json.dumps(d), flush=True)
+    return d
 
 
-def run_c1(args):
+def run_c1(args, emit=True):
     """Small model: GeneralEncoder(rx, ry, rz, rx on 4 wires) + 2 x (U3 on every wire,
     CNOT ring) + Z on every wire, n=4, bsz=32, forward + backward per step."""
     import torch
@@ -624,13 +1042,13 @@ def run_c1(args):
         model(x).sum().backward()
 
     ms, per = _timed(step, args.steps, args.warmup, dev)
-    _line(args, {"workload": "n=4 bsz=32: encoder (16 rotations) + 2 x (U3 on each wire, CNOT ring), Z per wire, "
-                             "fwd + bwd", "n_wires": 4, "global_batch": 32},
-          32 * args.steps / (ms / 1e3), ms, {"p50_ms": float(np.percentile(per, 50)),
-                                             "p99_ms": float(np.percentile(per, 99))})
+    return _line(args, {"workload": "n=4 bsz=32: encoder (16 rotations) + 2 x (U3 on each wire, CNOT ring), Z per "
+                                    "wire, fwd + bwd", "n_wires": 4, "global_batch": 32},
+                 32 * args.steps / (ms / 1e3), ms, {"p50_ms": float(np.percentile(per, 50)),
+                                                    "p99_ms": float(np.percentile(per, 99))}, emit)
 
 
-def run_c3(args):
+def run_c3(args, emit=True):
     """Fused forward at scale: the headline random circuit at (n=26, bsz=8) with fused
     widths k = 4, 5, 6 and (n=28, bsz=1) with k = 6; circuits/s of the forward pass."""
     import torch
@@ -640,7 +1058,8 @@ def run_c3(args):
 
     dev = torch.device("cuda")
     res = {}
-    for n, bsz, k in [(26, 8, 4), (26, 8, 5), (26, 8, 6), (28, 1, 6)]:
+    widths = (4, 5, 6) if emit else (6,)
+    for n, bsz, k in [(26, 8, k) for k in widths] + [(28, 1, 6)]:
         gates, ncols = W.random_circuit(n, args.depth, seed=0)
         th = torch.tensor(W.random_params(bsz, ncols, seed=1), device=dev)
         holder = {}
@@ -664,12 +1083,13 @@ def run_c3(args):
                                       "hbm_GBps_2S_per_pass": 2 * S * blocks / (per_step / 1e3) / 1e9}
         del holder
     main = res["n26_bsz8_k6"]
-    _line(args, {"workload": f"random circuit depth {args.depth}, fused forward, n=26 bsz=8 (k=4,5,6) and n=28 bsz=1 "
-                             "(k=6)", "n_wires": 26, "global_batch": 8},
-          main["circuits_per_s"], main["ms_per_step"] * args.steps, {"cases": res})
+    return _line(args, {"workload": f"random circuit depth {args.depth}, fused forward, n=26 bsz=8 (k="
+                                    f"{','.join(str(k) for k in widths)}) and n=28 bsz=1 (k=6)", "n_wires": 26,
+                        "global_batch": 8},
+                 main["circuits_per_s"], main["ms_per_step"] * args.steps, {"cases": res}, emit)
 
 
-def run_c5(args):
+def run_c5(args, emit=True):
     """Differentiation workload: n=20, bsz=64, 10 layers of (RY, RZ on every wire with
     shared parameters, CZ ladder) = 400 parameters, loss = sum_j w_j <P_j> over 50 random
     Pauli strings; fwd + adjoint bwd per step.  Literal variant (|0> input: all rows equal)
@@ -716,12 +1136,20 @@ def run_c5(args):
                         "peak_bytes": int(peak), "peak_states": peak / S,
                         "autograd_estimate_bytes": int(len(gates) * S)}
     main = out["per_sample_input"]
-    _line(args, {"workload": "n=20 bsz=64, 10 x (RY, RZ per wire, shared params; CZ ladder), 400 params, "
-                             "sum of 50 weighted Pauli strings, fwd + adjoint bwd", "n_wires": n, "global_batch": bsz},
-          main["circuits_per_s"], main["ms_per_step"] * args.steps, {"variants": out})
+    return _line(args, {"workload": "n=20 bsz=64, 10 x (RY, RZ per wire, shared params; CZ ladder), 400 params, "
+                                    "sum of 50 weighted Pauli strings, fwd + adjoint bwd", "n_wires": n,
+                        "global_batch": bsz},
+                 main["circuits_per_s"], main["ms_per_step"] * args.steps, {"variants": out}, emit)
 
 
-def run_c4(args):
+def c4_workload(rng):
+    """256 circuits: (n, layers) with n ~ U{8..20}, L ~ U{2..40}, and their RY / RZ angles."""
+    specs = [(int(rng.integers(8, 21)), int(rng.integers(2, 41))) for _ in range(256)]
+    angles = [(rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n))) for n, L in specs]
+    return specs, angles
+
+
+def run_c4(args, emit=True):
     """Uneven batching: 256 independent circuits, n ~ U{8..20}, L ~ U{2..40} layers of
     (RY, RZ on every wire, angles ~ U[-pi, pi); CZ ladder), output <Z_0> of each, run as
     one persistent kernel (tqk_batch_run) with the launch shape picked by the autotuner
@@ -736,8 +1164,7 @@ def run_c4(args):
 
     dev = torch.device("cuda")
     rng = np.random.default_rng(0)
-    specs = [(int(rng.integers(8, 21)), int(rng.integers(2, 41))) for _ in range(256)]
-    angles = [(rng.uniform(-np.pi, np.pi, (L, n)), rng.uniform(-np.pi, np.pi, (L, n))) for n, L in specs]
+    specs, angles = c4_workload(rng)
     cb = B.CircuitBatch()
     for (n, _), (ry, rz) in zip(specs, angles):
         cb.add_layered(n, ry, rz)
@@ -800,7 +1227,21 @@ def run_c4(args):
     torch.cuda.synchronize()
     per_circuit_engine = (time.perf_counter() - t0) / len(sample)
     cfg = pb.config
-    _line(args, {"workload": "256 circuits, n~U{8..20}, L~U{2..40} x (RY, RZ per wire; CZ ladder), <Z_0> each, one "
+    # the batch kernel against its bounds: every planned op sweeps its circuit's tile in
+    # shared memory (read + write each amplitude: 16 B per amplitude per op); circuits
+    # wider than the tile stream their state through HBM once per pass (16 B per amplitude)
+    per_launch_s = ms / args.steps / 1e3
+    smem_bytes = sum(int(c["num_ops"]) * (1 << int(c["n"])) * 16 for c in pb.circ)
+    hbm_bytes = sum(int(c["num_passes"]) * (1 << int(c["n"])) * 16 for c in pb.circ if int(c["state_off"]) >= 0)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    smem_peak = 128 * sms * 2.07e9 / 1e9  # 128 B per clock per SM at the 2070 MHz maximum SM clock
+    hbm_peak, hbm_kind = _peaks()
+    batch_kernel = {"smem_bytes_per_launch": smem_bytes, "smem_GB/s": smem_bytes / per_launch_s / 1e9,
+                    "smem_peak_GB/s": smem_peak, "smem_frac": smem_bytes / per_launch_s / 1e9 / smem_peak,
+                    "smem_peak_source": "nominal: 128 B/clock/SM x SMs x 2070 MHz",
+                    "hbm_bytes_per_launch": hbm_bytes, "hbm_GB/s": hbm_bytes / per_launch_s / 1e9,
+                    "hbm_frac": hbm_bytes / per_launch_s / 1e9 / hbm_peak, "hbm_peak_source": f"{hbm_kind} hbm_gbs"}
+    return _line(args, {"workload": "256 circuits, n~U{8..20}, L~U{2..40} x (RY, RZ per wire; CZ ladder), <Z_0> each, one "
                              "persistent kernel in a CUDA graph", "circuits": 256, "n_range": [8, 20],
                  "layers_range": [2, 40],
                  "launch_shape": {"tile_bits": cfg.tile_bits, "threads": cfg.threads, "ctas_per_sm": cfg.ctas_per_sm,
@@ -810,11 +1251,14 @@ def run_c4(args):
                    "d2h_bytes_per_step": 256 * 8 + 257 * 8,
                    "includes": "new angles host->device, graph replay, <Z> and latencies device->host"},
            "latency_ms": {"p50": float(np.percentile(res.latency_ms, 50)), "p99": float(np.percentile(res.latency_ms, 99)),
-                          "max": float(res.latency_ms.max())},
+                          "max": float(res.latency_ms.max()),
+                          "definition": "each circuit's completion time (%globaltimer) after its launch started"},
+           "batch_kernel": batch_kernel,
            "default_launch_shape": {"circuits_per_s": 256 * args.steps / (dms / 1e3), "tile_bits": 14, "threads": 512,
                                     "ctas_per_sm": 1, "graph": False},
            "engine_one_circuit_at_a_time": {"circuits_per_s": 1.0 / per_circuit_engine,
-                                            "sample": f"{len(sample)} of the 256 circuits, fused method, sequential"}})
+                                            "sample": f"{len(sample)} of the 256 circuits, fused method, sequential"}},
+                 emit)
 
 
 def main():

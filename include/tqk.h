@@ -101,11 +101,16 @@ int tqk_sample(const void* state, int64_t bsz, int n, const double* uniforms, in
  * P_j is given by bit masks over the in-row index (bit n-1-w <-> wire w):
  * xmask = X|Y positions, zmask = Z|Y positions; the i^(#Y) factor is applied.
  * Replaces expval_joint_analytical (measurement/measurements.py:232-279), which
- * builds a dense 2^n x 2^n kron Hamiltonian.  Deterministic (fixed-order reduction). */
+ * builds a dense 2^n x 2^n kron Hamiltonian.  Deterministic (fixed-order reduction).
+ * Strings sharing one X-mask: one pass per 8 strings.  Several X-masks: strings are
+ * grouped (in order, up to 8 per group, while the group's X-masks span at most
+ * 13 - c dimensions above c contiguous low bits, c >= 4) and each group is one pass over
+ * cosets of that span staged in shared memory.  status: device int; TQK_TIMEOUT is
+ * written there (and the affected expvals are NaN) if a staged load did not complete. */
 int64_t tqk_pauli_expval_scratch_bytes(int64_t bsz, int n, int m);
 int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uint64_t* xmask,
                      const uint64_t* zmask, int m, double* out, void* scratch,
-                     int64_t scratch_bytes, void* stream);
+                     int64_t scratch_bytes, int* status, void* stream);
 
 /* Same result as tqk_pauli_expval, without caller scratch: the block partials live in
  * a 1 MiB array inside libtqk.so (one per device, shared by every call), so the call
@@ -123,11 +128,14 @@ int64_t tqk_pauli_expval_noalloc_capacity(void);
 int tqk_pauli_expval_noalloc(const void* state, int64_t bsz, int n, const uint64_t* xmask,
                              const uint64_t* zmask, int m, double* out, void* stream);
 
-/* out = sum_j coef[b*m + j] * P_j psi  (complex64 [bsz, 2^n]; coef float32 device).
- * The backward of the expvals above (cotangent of psi). */
+/* out = sum_j coef[b*m + j] * P_j psi  (complex64 [bsz, 2^n], not aliasing state; coef
+ * float32 device).  The backward of the expvals above (cotangent of psi); the strings
+ * are grouped as for tqk_pauli_expval, one coset pass per group (the first writes out,
+ * later ones add to it).  status: device int, TQK_TIMEOUT if a staged load did not
+ * complete (out is then incomplete). */
 int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const uint64_t* xmask,
                         const uint64_t* zmask, int m, const float* coef, void* out,
-                        void* stream);
+                        int* status, void* stream);
 
 /* ---------------------------------------------------------------- adjoint backward
  * One reverse step of the adjoint method for a gate applied with the matching forward

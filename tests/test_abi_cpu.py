@@ -77,14 +77,14 @@ def test_too_many_qubits_rejected(lib):
 
 
 def test_scratch_too_small_rejected(lib):
-    rc = lib.tqk_pauli_expval(16, 2, 10, _lib._u64([1]), _lib._u64([0]), 1, 16, 16, 8, None)
+    rc = lib.tqk_pauli_expval(16, 2, 10, _lib._u64([1]), _lib._u64([0]), 1, 16, 16, 8, 16, None)
     assert rc == 7
     assert lib.tqk_pauli_expval_scratch_bytes(2, 10, 1) > 8
 
 
 def test_pauli_mask_beyond_n_rejected(lib):
     need = lib.tqk_pauli_expval_scratch_bytes(1, 3, 1)
-    rc = lib.tqk_pauli_expval(16, 1, 3, _lib._u64([8]), _lib._u64([0]), 1, 16, 16, need, None)
+    rc = lib.tqk_pauli_expval(16, 1, 3, _lib._u64([8]), _lib._u64([0]), 1, 16, 16, need, 16, None)
     assert rc == 1
 
 

@@ -24,3 +24,28 @@ def test_plain_pass_summary_weights_the_gate_mix():
     assert abs(out["uniform_2S_GB/s"] - 2 * S / t / 1e9) < 1e-6
     assert abs(out["frac"] - out["GB/s"] / 6800.0) < 1e-12
     assert abs(sum(b.PLAIN_GATE_MIX.values()) - 1.0) < 1e-12
+
+
+def test_reference_arm_runs_upstream_on_the_host():
+    """``bench.py --impl reference`` times upstream itself (baseline/_ref) when it is
+    installed: one JSON line with kind "reference", the CPU model and positive rates."""
+    import json
+    import subprocess
+    import sys
+
+    import pytest
+
+    from oracle import upstream as U
+
+    if not U.available():
+        pytest.skip("upstream torchquantum is not installed (baseline/_ref)")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--n", "8",
+                        "--depth", "12", "--steps", "2", "--warmup", "1"], capture_output=True, text=True,
+                       timeout=300, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "reference" and cb["cpu_model"] and cb["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0

@@ -115,7 +115,7 @@ def test_dense_k_wire_adjoint_vs_fd(kw):
                     vals.append(O.expval_pauli(s, "ZXIYIIZI", n).sum())
                 d = (vals[0] - vals[1]) / (2 * eps)
                 gnum[i, j] += d * unit
-    assert np.abs(ut.grad.cpu().numpy()[0] - gnum).max() < 1e-4
+    assert np.abs(ut.grad.cpu().numpy()[0] - gnum).max() < 1e-5
 
 
 @pytest.mark.parametrize(
@@ -253,7 +253,7 @@ def test_autotuned_fusion_vs_oracle(tmp_path, monkeypatch):
             assert seg.fuse_width in (4, 5, 6) and any(getattr(op, "members", None) for op in seg.exec_ops)
     ref = O.run(n, bsz, W.oracle_gates(gates, theta))
     assert np.abs(res["fused"][0] - ref).max() < 1e-5
-    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-4
+    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-5
     assert any(k.startswith("fusion2|") for k in A._MEM)
     A.clear()
 

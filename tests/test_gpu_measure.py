@@ -102,11 +102,11 @@ def test_reset_vs_oracle():
 
 
 @pytest.mark.parametrize("n,bsz,m", [(6, 5, 3), (10, 3, 20), (14, 2, 17), (22, 2, 9), (24, 1, 9)])
-def test_row_sweep_expvals(n, bsz, m):
-    """Strings with several X-masks at n <= 24 take the row sweep (k_expval_rows: every
-    string's partner read per amplitude pair, rows one after another): against the oracle
-    where it is cheap, and against the per-X-mask passes of the no-allocation entry point
-    at every size, including diagonal strings, X-mask 1 and chunks of 8 with a remainder."""
+def test_coset_expvals_vs_per_mask_passes(n, bsz, m):
+    """Strings with several X-masks take the coset passes (partners staged in shared
+    memory): against the oracle where it is cheap, and against the per-X-mask passes of
+    the no-allocation entry point at every size, including diagonal strings, X-mask 1 and
+    groups of 8 with a remainder."""
     import ctypes
 
     from torchquantum_gb300 import _lib
@@ -116,7 +116,7 @@ def test_row_sweep_expvals(n, bsz, m):
     strings = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(m - 2)]
     strings += ["Z" * n, "I" * (n - 1) + "Y"]
     xs, zs = zip(*[pauli_masks(p, n) for p in strings])
-    assert len(set(xs)) > 1 and _lib.expval_passes(list(xs), n) == (m + 7) // 8
+    assert len(set(xs)) > 1 and _lib.expval_passes(list(xs), n) == len(_lib.coset_groups(list(xs), n))
     s = rng.normal(size=(bsz, 1 << n)) + 1j * rng.normal(size=(bsz, 1 << n))
     s /= np.linalg.norm(s, axis=1, keepdims=True)
     st = torch.tensor(s, dtype=torch.complex64, device="cuda")
@@ -133,3 +133,57 @@ def test_row_sweep_expvals(n, bsz, m):
         want = np.stack([O.expval_pauli(s64, p, n) for p in strings], -1)
         assert np.abs(got.cpu().numpy() - want).max() < 1e-6
         assert np.abs(per_mask.cpu().numpy() - want).max() < 1e-6
+
+
+@pytest.mark.parametrize("n,bsz,m", [(3, 2, 6), (13, 2, 12), (14, 3, 20), (16, 2, 30), (17, 1, 9)])
+def test_coset_passes_vs_oracle(n, bsz, m):
+    """Coset passes (strings with different X-masks: partners staged in shared memory,
+    groups of <= 8 strings spanning <= 13 - c dimensions above c contiguous bits): the
+    expvals and the backward seed sum_j c_j P_j psi against the oracle, including a
+    diagonal string, X-mask 1, strings whose masks share the top bits, and several groups."""
+    from torchquantum_gb300 import _lib
+    from torchquantum_gb300.measurement import pauli_masks
+
+    rng = np.random.default_rng(70 + n)
+    strings = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(m - 3)]
+    strings += ["Z" * n, "I" * (n - 1) + "X", "X" + "I" * (n - 1)]
+    xs, zs = zip(*[pauli_masks(p, n) for p in strings])
+    groups = _lib.coset_groups(list(xs), n)
+    assert sum(len(g) for g, _, _ in groups) == m
+    s = rng.normal(size=(bsz, 1 << n)) + 1j * rng.normal(size=(bsz, 1 << n))
+    s /= np.linalg.norm(s, axis=1, keepdims=True)
+    st = torch.tensor(s, dtype=torch.complex64, device="cuda")
+    got = _lib.pauli_expval(st, n, list(xs), list(zs)).cpu().numpy()
+    s64 = st.cpu().numpy().astype(np.complex128)
+    want = np.stack([O.expval_pauli(s64, p, n) for p in strings], -1)
+    assert np.abs(got - want).max() < 1e-6
+    coef = rng.normal(size=(bsz, m)).astype(np.float32)
+    seed = _lib.pauli_apply_sum(st, n, list(xs), list(zs), torch.tensor(coef, device="cuda")).cpu().numpy()
+    want_seed = sum(coef[:, j:j + 1].astype(np.float64) * O.apply_pauli(s64, p, n) for j, p in enumerate(strings))
+    assert np.abs(seed - want_seed).max() < 1e-5
+    _lib.check_status(st.device)
+
+
+def test_coset_pass_at_bench_size_matches_per_mask_passes():
+    """n = 24, bsz = 4: 8 random strings in one coset pass against the per-X-mask passes
+    of the no-allocation entry point (each string's partner stream read from HBM)."""
+    from torchquantum_gb300 import _lib
+    from torchquantum_gb300.measurement import pauli_masks
+
+    n, bsz = 24, 4
+    rng = np.random.default_rng(24)
+    strings = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(8)]
+    xs, zs = zip(*[pauli_masks(p, n) for p in strings])
+    assert _lib.expval_passes(list(xs), n) == 1
+    g = torch.Generator(device="cuda").manual_seed(5)
+    st = torch.randn(bsz, 1 << n, dtype=torch.complex64, device="cuda", generator=g)
+    st /= st.abs().pow(2).sum(1, keepdim=True).sqrt()
+    got = _lib.pauli_expval(st, n, list(xs), list(zs))
+    lib = _lib.load()
+    ref = torch.full((bsz, 8), float("nan"), dtype=torch.float64, device="cuda")
+    rc = lib.tqk_pauli_expval_noalloc(st.data_ptr(), bsz, n, _lib._u64(list(xs)), _lib._u64(list(zs)), 8,
+                                      ref.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, lib.tqk_last_error().decode()
+    torch.cuda.synchronize()
+    assert (got - ref).abs().max().item() < 2e-6
+    _lib.check_status(st.device)

@@ -105,8 +105,8 @@ def test_vqe_gradients_vs_plain_and_fd(per_sample):
     gates, theta, x, paulis, w = _vqe(n, bsz, layers, 10, seed=5 + per_sample, per_sample=per_sample)
     lf, gf = _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, "fused")
     lp, gp = _engine_loss_grad(n, bsz, gates, theta, x, paulis, w, "plain")
-    assert abs(lf - lp) < 1e-4 * max(1.0, abs(lp))
-    assert np.abs(gf - gp).max() < 1e-4
+    assert abs(lf - lp) < 1e-5 * max(1.0, abs(lp))
+    assert np.abs(gf - gp).max() < 1e-5
     rng = np.random.default_rng(0)
     h = 1e-3
     for j in rng.choice(theta.shape[1], size=6, replace=False):
@@ -114,7 +114,7 @@ def test_vqe_gradients_vs_plain_and_fd(per_sample):
         tp[0, j] += h
         tm[0, j] -= h
         fd = (_oracle_loss(n, bsz, gates, tp, x, paulis, w) - _oracle_loss(n, bsz, gates, tm, x, paulis, w)) / (2 * h)
-        assert abs(gf[j] - fd) < 1e-4 * max(1.0, abs(fd)), (j, gf[j], fd)
+        assert abs(gf[j] - fd) < 1e-5 * max(1.0, abs(fd)), (j, gf[j], fd)
 
 
 def test_vqe_full_size_memory():
@@ -141,5 +141,5 @@ def test_vqe_full_size_memory():
         res[mode] = (loss, g, peak, blocks[0])
     assert res[False][3] == 0 and res[False][2] < 8 * state_bytes
     assert res[True][3] > 0 and res[True][2] < (res[True][3] + 8) * state_bytes
-    assert abs(res[True][0] - res[False][0]) < 1e-4 * max(1.0, abs(res[False][0]))
-    assert np.abs(res[True][1] - res[False][1]).max() < 1e-4 * max(1.0, np.abs(res[False][1]).max())
+    assert abs(res[True][0] - res[False][0]) < 1e-5 * max(1.0, abs(res[False][0]))
+    assert np.abs(res[True][1] - res[False][1]).max() < 1e-5 * max(1.0, np.abs(res[False][1]).max())

@@ -52,7 +52,7 @@ def test_static_matches_dynamic(k):
             assert any(getattr(op, "members", None) for sg in q._tape for op in sg.exec_ops)
     m.static_off()
     assert np.abs(res[True][0] - res[False][0]).max() < 1e-5
-    assert np.abs(res[True][1] - res[False][1]).max() < 1e-4
+    assert np.abs(res[True][1] - res[False][1]).max() < 1e-5
 
 
 def test_get_unitary_and_op_history_replay():

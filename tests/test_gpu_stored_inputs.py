@@ -131,7 +131,7 @@ def test_circuit_with_stored_inputs_matches_recompute():
     assert all(not getattr(op, "kept_input", False) for op in tc0)
     assert np.array_equal(s1, s0)
     assert np.abs(s1 - O.run(n, bsz, W.oracle_gates(gates, theta))).max() < 1e-5
-    assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
+    assert np.abs(g1 - g0).max() < 1e-5 * max(1.0, np.abs(g0).max())
     # a backward that does not retain the graph releases the stored inputs, like torch's
     # own saved tensors (the segments keep only weak references)
     q2, _, g2 = _circuit_run(n, bsz, gates, theta, paulis, True)
@@ -175,7 +175,7 @@ def test_mixed_segment_with_stored_inputs():
             assert any(getattr(op, "kept_input", False) for op in ops)
             assert any(getattr(op, "members", None) is None for op in ops)
     for a, b in zip(res["fused"], res["plain"]):
-        assert np.abs(a - b).max() < 1e-4 * max(1.0, np.abs(b).max())
+        assert np.abs(a - b).max() < 1e-5 * max(1.0, np.abs(b).max())
 
 
 def test_auto_mode_stores_only_when_needed(monkeypatch):
@@ -231,7 +231,7 @@ def test_out_of_memory_midway_falls_back_in_place(monkeypatch):
     flags = [getattr(op, "kept_input", False) for sg in q._tape for op in sg.blocks if op.tc]
     assert sum(flags) == 3 and len(flags) > 3
     assert np.array_equal(s1, s0)
-    assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
+    assert np.abs(g1 - g0).max() < 1e-5 * max(1.0, np.abs(g0).max())
 
 
 def _two_reads(n, bsz, gates, theta, paulis, init, checkpoint):
@@ -273,7 +273,7 @@ def test_two_reads_and_initial_state_gradient():
     g1, s1, k1 = _two_reads(n, bsz, gates, theta, paulis, init, True)
     g0, s0, k0 = _two_reads(n, bsz, gates, theta, paulis, init, False)
     assert k1 > 0 and k0 == 0
-    assert np.abs(g1 - g0).max() < 1e-4 * max(1.0, np.abs(g0).max())
+    assert np.abs(g1 - g0).max() < 1e-5 * max(1.0, np.abs(g0).max())
     assert np.abs(s1 - s0).max() < 1e-5 * max(1.0, np.abs(s0).max())
 
 
@@ -306,4 +306,4 @@ def test_first_block_from_zero_state(per_row):
             first = q._tape[0].exec_ops[0]
             assert getattr(first, "tc", False) and first.zero_input and first.block_batch == (bsz if per_row else 1)
     assert np.abs(res["fused"][0] - res["plain"][0]).max() < 1e-5
-    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-4 * max(1.0, np.abs(res["plain"][1]).max())
+    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-5 * max(1.0, np.abs(res["plain"][1]).max())

@@ -121,17 +121,22 @@ def test_stored_inputs_move_to_the_autograd_node():
     assert a.stored_ref() is None and program.Segment.take_stored_inputs(seg) == []
 
 
-def test_expval_pass_count_follows_the_row_sweep_rule():
-    """_lib.expval_passes mirrors tqk_pauli_expval: several X-masks on rows of at most 2^24
-    amplitudes -> one row sweep per 8 strings; otherwise one pass per X-mask (8 strings
-    each)."""
+def test_expval_pass_count_follows_the_coset_grouping():
+    """_lib.expval_passes mirrors tqk_pauli_expval: one X-mask for every string -> one pass
+    per 8 strings; several X-masks -> one coset pass per group, a group taking strings in
+    order while it holds <= 8 and its X-masks above the lowest 4 bits span <= 9 dimensions
+    (13 - 4; rows of n < 13 bits: everything fits one stage)."""
     from torchquantum_gb300 import _lib
 
-    xs = [1, 2, 3, 4, 5, 6, 7, 8, 9, 10]
-    assert _lib.expval_passes(xs, 20) == 2 and _lib.expval_passes(xs, 24) == 2
-    assert _lib.expval_passes(xs, 25) == 10
+    xs = [1, 2, 3, 4, 5, 6, 7, 8, 9, 10]  # all below bit 4: rank 0 above the chunk
+    assert _lib.expval_passes(xs, 20) == 2 and _lib.expval_passes(xs, 25) == 2
     assert _lib.expval_passes([0] * 9, 20) == 2  # one X-mask: grouped passes
-    assert _lib.expval_passes([0, 0, 3], 26) == 2
+    assert _lib.expval_passes([0, 0, 3], 26) == 1
+    hi = [1 << (4 + k) for k in range(12)]  # independent above the chunk: 8 per group (<= 9 dims)
+    assert [len(g) for g, _, _ in _lib.coset_groups(hi, 20)] == [8, 4]
+    assert _lib.expval_passes(hi, 12) == 2  # n < 13: a whole row is one stage, 8 strings per pass
+    for g, c, r in _lib.coset_groups(hi, 24):
+        assert c + r == 13
 
 
 def test_stored_input_policy(monkeypatch):

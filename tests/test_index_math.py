@@ -1,10 +1,15 @@
 """CPU model of the kernels' thread -> amplitude index mapping (csrc/apply.cu,
 csrc/measure.cu).  For every launch shape the host code picks, checks that each
 access is inside the row, that float4 accesses are 16-byte aligned, and that the
-gate's amplitude groups are covered exactly once."""
+gate's amplitude groups are covered exactly once; for the coset passes of the Pauli
+strings, that the staged cosets partition each row and that the stage-coordinate
+partner and sign rules reproduce the in-row ones."""
 import itertools
 
+import numpy as np
 import pytest
+
+from oracle import statevec as O
 
 
 def insert_zero_bits(g, pos):
@@ -229,8 +234,9 @@ def test_expval_pass_sign_algebra():
 
 
 def test_apply_sum_sign_algebra():
-    """k_pauli_apply_sum's per-string step (sign from one popcount plus ny >> 1, quarter
-    turn for odd ny, odd index flipped by z & 1) against sum_s c_s P_s psi."""
+    """The backward seed's per-string step (k_coset<true>: sign from one popcount plus
+    ny >> 1, quarter turn for odd ny, the odd index of a pair flipped by z & 1) against
+    sum_s c_s P_s psi, in in-row coordinates."""
     import numpy as np
 
     rng = np.random.default_rng(1)
@@ -252,3 +258,109 @@ def test_apply_sum_sign_algebra():
                 got[i + 1] += c1 * rot * psi[(i + 1) ^ x]
         want = sum(c * np.array(_pauli_apply(psi, int(x), int(z))) for x, z, c in zip(xs, zs, cs))
         assert np.abs(got - want).max() < 1e-10
+
+
+# ------------------------------------------------------------------ coset passes (measure.cu)
+def _reduced_basis(vectors):
+    """Reduced echelon basis (ascending pivots), as gf2_reduced_basis in measure.cu."""
+    basis = []  # [pivot, vector]
+    for v in vectors:
+        for piv, b in basis:
+            if (v >> piv) & 1:
+                v ^= b
+        if v == 0:
+            continue
+        q = v.bit_length() - 1
+        basis = [[piv, b ^ v if (b >> q) & 1 else b] for piv, b in basis]
+        basis.append([q, v])
+    basis.sort()
+    return [b for _, b in basis], [piv for piv, _ in basis]
+
+
+def _coset_model(n, xs, zs, group, c):
+    """For one coset pass: list over (coset t) of (global in-row index of each stage
+    coordinate u, per-string partner stage coordinate, per-string sign bit of u), built
+    from the same algebra as k_coset / coset_params."""
+    basis, piv = _reduced_basis([xs[j] >> c for j in group])
+    r = len(basis)
+    lmask = (1 << c) - 1
+    consts = []
+    for j in group:
+        xh, zh = xs[j] >> c, zs[j] >> c
+        a = sum(1 << k for k in range(r) if (xh >> piv[k]) & 1)
+        beta = sum(1 << k for k in range(r) if bin(basis[k] & zh).count("1") & 1)
+        consts.append(((a << c) | (xs[j] & lmask), (beta << c) | (zs[j] & lmask), zh))
+    out = []
+    for t in range(1 << (n - c - r)):
+        rep = t
+        for q in piv:
+            rep = ((rep >> q) << (q + 1)) | (rep & ((1 << q) - 1))
+        gidx = []
+        for u in range(1 << (c + r)):
+            a, l = u >> c, u & lmask
+            h = rep
+            for k in range(r):
+                if (a >> k) & 1:
+                    h ^= basis[k]
+            gidx.append((h << c) | l)
+        rho = [bin(rep & zh).count("1") & 1 for _, _, zh in consts]
+        out.append((gidx, consts, rho))
+    return out, r
+
+
+@pytest.mark.parametrize("n,m,seed", [(5, 4, 0), (9, 6, 1), (14, 8, 2), (15, 12, 3), (16, 20, 4)])
+def test_coset_partition_partners_and_signs(n, m, seed):
+    from torchquantum_gb300 import _lib
+
+    rng = np.random.default_rng(seed)
+    xs = [int(v) for v in rng.integers(0, 1 << n, size=m)]
+    zs = [int(v) for v in rng.integers(0, 1 << n, size=m)]
+    xs[0] = 0  # a diagonal string
+    for group, c, r in _lib.coset_groups(xs, n):
+        model, r2 = _coset_model(n, xs, zs, group, c)
+        assert r2 == r and c + r == min(n, 13) and len(group) <= 8
+        seen = np.zeros(1 << n, dtype=np.int64)
+        for gidx, consts, rho in model:
+            g = np.array(gidx)
+            seen[g] += 1
+            for s, j in enumerate(group):
+                xsu, gam, _ = consts[s]
+                for u in range(len(gidx)):
+                    assert gidx[u ^ xsu] == gidx[u] ^ xs[j]  # partner on chip
+                    assert (bin(gidx[u] & zs[j]).count("1") & 1) == (rho[s] ^ (bin(u & gam).count("1") & 1))
+        assert (seen == 1).all()  # the cosets partition the row
+
+
+@pytest.mark.parametrize("n,m,seed", [(6, 5, 10), (14, 9, 11)])
+def test_coset_expvals_and_seed_match_the_oracle(n, m, seed):
+    """Expvals and the backward seed assembled from the coset model (the kernel's sign
+    bits: expvals ny >> 1, seed (ny & 1) ^ (ny >> 1)) equal the oracle's."""
+    from torchquantum_gb300 import _lib
+
+    rng = np.random.default_rng(seed)
+    strings = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(m)]
+    masks = [O.pauli_masks(p, n) for p in strings]
+    xs, zs = [x for x, _, _ in masks], [z for _, z, _ in masks]
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    coef = rng.normal(size=m)
+    ev = np.zeros(m)
+    seed_out = np.zeros(1 << n, dtype=np.complex128)
+    for group, c, r in _lib.coset_groups(xs, n):
+        model, _ = _coset_model(n, xs, zs, group, c)
+        for gidx, consts, rho in model:
+            g = np.array(gidx)
+            stage = psi[g]
+            for s, j in enumerate(group):
+                xsu, gam, _ = consts[s]
+                ny = bin(xs[j] & zs[j]).count("1") & 3
+                for u in range(len(gidx)):
+                    pb = rho[s] ^ (bin(u & gam).count("1") & 1)
+                    w = np.conj(stage[u]) * stage[u ^ xsu]
+                    part = w.imag if ny & 1 else w.real
+                    ev[j] += part * (-1) ** (pb ^ (ny >> 1))
+                    term = stage[u ^ xsu] * (1j if ny & 1 else 1)
+                    seed_out[g[u]] += coef[j] * (-1) ** (pb ^ (ny & 1) ^ (ny >> 1)) * term
+    want = np.array([O.expval_pauli(psi[None], p, n)[0] for p in strings])
+    assert np.abs(ev - want).max() < 1e-9
+    want_seed = sum(cj * O.apply_pauli(psi[None], p, n)[0] for cj, p in zip(coef, strings))
+    assert np.abs(seed_out - want_seed).max() < 1e-9

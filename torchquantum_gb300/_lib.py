@@ -49,8 +49,8 @@ _SIGS = {
     "tqk_reset": (_int, [_vp, _i64, _int, _i32p, _int, _vp, _i64, _vp]),
     "tqk_probs": (_int, [_vp, _i64, _int, _vp, _vp]),
     "tqk_pauli_expval_scratch_bytes": (_i64, [_i64, _int, _int]),
-    "tqk_pauli_expval": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _i64, _vp]),
-    "tqk_pauli_apply_sum": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _vp]),
+    "tqk_pauli_expval": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _i64, _vp, _vp]),
+    "tqk_pauli_apply_sum": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp, _vp, _vp]),
     "tqk_adjoint_matrix": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp, _vp]),
     "tqk_adjoint_controlled": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _i32p, _int, _vp, _i64, _vp, _vp, _vp]),
     "tqk_adjoint_phase": (_int, [_vp, _vp, _i64, _int, _i32p, _int, _vp, _i64, _vp, _vp]),
@@ -201,19 +201,56 @@ def probs(state, n):
     return out
 
 
-ROWS_MAX_WIRES = 24  # tqk_pauli_expval sweeps rows of up to 2^24 amplitudes through L2
+COSET_TILE_BITS = 13     # a coset pass stages 2^min(n, 13) amplitudes
+COSET_MIN_CHUNK_BITS = 4  # in contiguous runs of at least 2^4 amplitudes
+MAX_STRINGS_PER_PASS = 8
+
+
+def gf2_rank(vectors) -> int:
+    """Rank over GF(2) of integer bit vectors."""
+    basis = []  # (pivot bit, vector), reduced
+    for v in vectors:
+        for piv, b in basis:
+            if (v >> piv) & 1:
+                v ^= b
+        if v:
+            q = v.bit_length() - 1
+            basis = [(piv, b ^ v if (b >> q) & 1 else b) for piv, b in basis]
+            basis.append((q, v))
+    return len(basis)
+
+
+def coset_groups(xmasks, n: int):
+    """The coset passes tqk_pauli_expval (several X-masks) and tqk_pauli_apply_sum make:
+    strings in order, a group growing while it holds at most 8 strings and its X-masks'
+    parts above the lowest c bits span at most T - c dimensions for c = min(4, T),
+    T = min(n, 13).  Returns [(string indices, c, rank)] with the widest such c."""
+    T = min(n, COSET_TILE_BITS)
+    cmin = min(COSET_MIN_CHUNK_BITS, T)
+    groups, cur = [], []
+    for j in range(len(xmasks)):
+        if cur and (len(cur) == MAX_STRINGS_PER_PASS
+                    or gf2_rank([xmasks[i] >> cmin for i in cur + [j]]) > T - cmin):
+            groups.append(cur)
+            cur = []
+        cur.append(j)
+    if cur:
+        groups.append(cur)
+    out = []
+    for g in groups:
+        c = cmin
+        while c < T and gf2_rank([xmasks[i] >> (c + 1) for i in g]) <= T - (c + 1):
+            c += 1
+        out.append((g, c, gf2_rank([xmasks[i] >> c for i in g])))
+    return out
 
 
 def expval_passes(xmasks, n: int = 64) -> int:
-    """Passes tqk_pauli_expval makes: with several X-masks and rows of at most 2^24
-    amplitudes, one row sweep per 8 strings; otherwise strings grouped by X-mask, at most
-    8 per pass."""
-    if n <= ROWS_MAX_WIRES and len(set(xmasks)) > 1:
-        return (len(xmasks) + 7) // 8
-    counts = {}
-    for x in xmasks:
-        counts[x] = counts.get(x, 0) + 1
-    return sum((c + 7) // 8 for c in counts.values())
+    """Passes tqk_pauli_expval makes: with several X-masks one coset pass per group
+    (``coset_groups``); with one X-mask for all strings, one pass per 8 strings."""
+    if len(set(xmasks)) > 1:
+        return len(coset_groups(list(xmasks), n))
+    return (len(xmasks) + 7) // 8
 
 
 def pauli_expval(state, n, xmasks, zmasks):
@@ -225,7 +262,8 @@ def pauli_expval(state, n, xmasks, zmasks):
     nbytes = lib.tqk_pauli_expval_scratch_bytes(bsz, n, m)
     scratch = torch.empty(max(8, nbytes), dtype=torch.uint8, device=state.device)
     _check(lib.tqk_pauli_expval(state.data_ptr(), bsz, n, _u64(xmasks), _u64(zmasks), m, out.data_ptr(),
-                                scratch.data_ptr(), nbytes, _stream(state)), launches=2 * expval_passes(xmasks, n))
+                                scratch.data_ptr(), nbytes, status_word(state.device).data_ptr(), _stream(state)),
+           launches=2 * expval_passes(xmasks, n))
     return out
 
 
@@ -233,7 +271,8 @@ def pauli_apply_sum(state, n, xmasks, zmasks, coef):
     """sum_j coef[:, j] * P_j psi; coef float32 [bsz, m] (contiguous, same device)."""
     out = torch.empty_like(state)
     _check(load().tqk_pauli_apply_sum(state.data_ptr(), state.shape[0], n, _u64(xmasks), _u64(zmasks), len(xmasks),
-                                      coef.data_ptr(), out.data_ptr(), _stream(state)), launches=(len(xmasks) + 63) // 64)
+                                      coef.data_ptr(), out.data_ptr(), status_word(state.device).data_ptr(),
+                                      _stream(state)), launches=len(coset_groups(list(xmasks), n)))
     return out
 
 

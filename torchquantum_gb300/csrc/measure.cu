@@ -3,26 +3,25 @@
 // <psi|P|psi> for P = (x) sigma_w is evaluated from two bit masks over the in-row
 // index: xmask (X or Y on the wire) and zmask (Z or Y), with
 //   (P psi)_i = i^{#Y} (-1)^{popcount((i ^ x) & z)} psi_{i ^ x}.
-// Strings with several xmasks on rows of up to 2^24 amplitudes are evaluated 8 at a
-// time in one sweep of the rows through L2 (k_expval_rows: each amplitude's partners
-// for all 8 strings, the rows in order so that DRAM reads the state once); otherwise
-// strings that share an xmask are evaluated in one pass over the state (each amplitude
-// pair (i, i^x) is read once for all of them).  Each thread accumulates in float32,
-// blocks reduce in float64 and write one partial per (row, block, string) to scratch;
-// a second kernel adds the partials in a fixed order, so results are bitwise
-// reproducible run to run.  The backward seed sum_s c_s P_s psi (k_pauli_apply_sum)
-// reads each output's partners for up to 64 strings in one pass.
+// Strings that all share one xmask are evaluated 8 at a time in one pass over the state
+// (each amplitude pair (i, i^x) is read once for all of them).  Strings with several
+// xmasks are grouped and each group is one coset pass (k_coset): the row is cut into
+// cosets of the span of the group's xmasks, staged in shared memory by bulk copies, so
+// all partners are read on chip and DRAM reads the state once per group.  Each thread
+// accumulates in float32, blocks reduce in float64 and write one partial per (row,
+// block or coset, string) to scratch; a second kernel adds the partials in a fixed
+// order, so results are bitwise reproducible run to run.  The backward seed
+// sum_s c_s P_s psi (k_coset<true>) uses the same coset passes.
 #include <atomic>
 #include <mutex>
 #include <vector>
 
+#include "bulk.cuh"
 #include "common.cuh"
 
 namespace tqk {
 
 constexpr int kMaxStringsPerPass = 8;
-constexpr int kMaxApplyStrings = 64;
-constexpr int kApplyChunk = 8;  // apply_sum partner loads issued together
 
 // Blocks per row for the reduction passes: enough to fill the GPU, bounded so the
 // partials stay small.  Depends only on (bsz, n) so scratch size is a pure function.
@@ -174,101 +173,6 @@ __global__ void __launch_bounds__(256) k_expval_pair(const ExpvalParams p) {
   block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
 }
 
-// Strings with different X-masks in one launch, the rows swept one after another by the
-// whole grid.  While a row of up to kRowsMaxAmps amplitudes is being swept it stays in L2,
-// so the partner reads psi[i ^ x_s] of every string are served from L2 and each row is
-// read from DRAM about once -- one pass per X-mask reads it once per mask.  Each thread
-// takes the two amplitudes i, i + 1 and adds Re(conj(psi_j) (P_s psi)_j) for both:
-//   (P psi)_j = i^ny (-1)^popcount((j ^ x) & z) psi_{j ^ x},
-// with the sign of j = i + 1 that of j = i times (-1)^(z & 1), and Re(i^ny u) = u_r, -u_i,
-// -u_r, u_i for ny = 0..3 (one popcount per string per thread).
-constexpr int kRowsBlocks = 152 * 4;             // CTAs of the row sweep (partials per row)
-constexpr int64_t kRowsMaxAmps = 1ll << 24;       // rows of up to 128 MB (about the L2)
-
-struct RowsParams {
-  const float2* state;
-  int n;
-  int ns;
-  int64_t bsz;
-  uint64_t x[kMaxStringsPerPass], z[kMaxStringsPerPass];
-  int ny[kMaxStringsPerPass];
-  double* partial;  // [bsz][gridDim.x][kMaxStringsPerPass]
-};
-
-template <int NS, typename I>
-__global__ void __launch_bounds__(256) k_expval_rows(const RowsParams p) {
-  I xs[NS], zs[NS];
-  float z0[NS];
-  uint32_t ny[NS];
-#pragma unroll
-  for (int s = 0; s < NS; ++s) {
-    xs[s] = s < p.ns ? static_cast<I>(p.x[s]) : I(0);
-    zs[s] = s < p.ns ? static_cast<I>(p.z[s]) : I(0);
-    z0[s] = (zs[s] & I(1)) ? -1.f : 1.f;
-    ny[s] = s < p.ns ? static_cast<uint32_t>(p.ny[s]) : 0u;
-  }
-  const I half = static_cast<I>((1ll << p.n) >> 1);
-  const I stride = static_cast<I>(gridDim.x * blockDim.x);
-  for (int64_t b = 0; b < p.bsz; ++b) {
-    const float2* row = p.state + (b << p.n);
-    float acc[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) acc[s] = 0.f;
-    for (I t = static_cast<I>(blockIdx.x * blockDim.x + threadIdx.x); t < half; t += stride) {
-      const I i = t * 2;
-      const float4 v = ld4(row + i);
-      float4 w[NS];
-#pragma unroll
-      for (int s = 0; s < NS; ++s)
-        if (s < p.ns) w[s] = ld4(row + ((i ^ xs[s]) & ~I(1)));
-      const float2 a0 = lo2(v), a1 = hi2(v);
-#pragma unroll
-      for (int s = 0; s < NS; ++s)
-        if (s < p.ns) {
-          const bool sw = (xs[s] & I(1)) != 0;
-          const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
-          const float ur = fmaf(z0[s], a1.x * b1.x + a1.y * b1.y, a0.x * b0.x + a0.y * b0.y);
-          const float ui = fmaf(z0[s], a1.x * b1.y - a1.y * b1.x, a0.x * b0.y - a0.y * b0.x);
-          const uint32_t neg = ((ny[s] + 1u) >> 1) & 1u;  // ny = 1, 2
-          acc[s] += flip_if_odd((ny[s] & 1u) ? ui : ur, popc_t<I>((i ^ xs[s]) & zs[s]) + neg);
-        }
-    }
-    block_reduce_store<NS>(acc, p.partial + (b * gridDim.x + blockIdx.x) * kMaxStringsPerPass, p.ns);
-    __syncthreads();  // the reduction's shared buffer is reused for the next row
-  }
-}
-
-// CTAs of the row sweep for rows of 2^n amplitudes (0: rows too long to stay in L2).
-static int64_t rows_blocks(int n) {
-  const int64_t amps = 1ll << n;
-  if (amps > kRowsMaxAmps) return 0;
-  const int64_t cap = (amps / 2 + 255) / 256;
-  return cap < kRowsBlocks ? cap : kRowsBlocks;
-}
-
-// Launch with every CTA resident at once (a CTA of a second wave would start the first
-// row after the others finished the last one); returns the grid size (partials per row).
-template <int NS, typename I>
-unsigned launch_rows_ns(const RowsParams& p, int64_t max_blocks, cudaStream_t st) {
-  int dev = 0, sms = 0, fit = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_expval_rows<NS, I>, 256, 0) != cudaSuccess || fit < 1)
-    fit = 1;
-  int64_t grid = static_cast<int64_t>(sms) * fit;
-  if (grid > max_blocks) grid = max_blocks;
-  k_expval_rows<NS, I><<<static_cast<unsigned>(grid), 256, 0, st>>>(p);
-  return static_cast<unsigned>(grid);
-}
-
-template <typename I>
-unsigned launch_rows(const RowsParams& p, int64_t max_blocks, cudaStream_t st) {
-  if (p.ns <= 1) return launch_rows_ns<1, I>(p, max_blocks, st);
-  if (p.ns <= 2) return launch_rows_ns<2, I>(p, max_blocks, st);
-  if (p.ns <= 4) return launch_rows_ns<4, I>(p, max_blocks, st);
-  return launch_rows_ns<8, I>(p, max_blocks, st);
-}
-
 // The two kernels above store block partials contiguously as [row][block][slot];
 // this kernel reduces them in block order into out[row*m + col].
 // Launch the pass kernel with the smallest accumulator count that holds p.ns strings.
@@ -326,67 +230,399 @@ __global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* 
   if (threadIdx.x < ns) out[b * m + cols.c[threadIdx.x]] = red[threadIdx.x][0];
 }
 
-struct ApplySumParams {
+// ------------------------------------------------------------------ coset passes
+// Strings with different X-masks are evaluated from shared memory: the in-row index space
+// is cut into cosets of the subgroup the strings' X-masks span, one coset per pipeline
+// stage, so every partner amplitude psi[i ^ x_s] of every string of the group is read on
+// chip and DRAM reads each amplitude once per pass.
+//
+// Chunks: the lowest c index bits stay contiguous (runs of 2^c amplitudes, moved by bulk
+// copies).  The high parts x_s >> c of the group's X-masks span an r-dimensional space;
+// b_0..b_{r-1} is its reduced echelon basis (pivot bits p_0 < ... < p_{r-1}, each present
+// in its own basis vector only).  Coset t of a row is rep(t) + span{b_k} over the high
+// index bits, rep(t) = t with zeros inserted at the pivot bits; stage slot a (r bits)
+// holds the chunk at high index h(t, a) = rep(t) ^ sum_k a_k b_k, so a stage is 2^(c + r)
+// amplitudes.  In stage coordinates u = (a << c) | l the partner of u under string s is
+// u ^ xs_s, xs_s = (a_s << c) | (x_s mod 2^c), a_s the basis coefficients of x_s >> c.
+// Signs: for the in-row index i of u, parity(i & z_s) = rho_s(t) ^ parity(u & gam_s) with
+// gam_s = (beta_s << c) | (z_s mod 2^c), beta_s bit k = parity(b_k & (z_s >> c)) and
+// rho_s(t) = parity(rep(t) & (z_s >> c)).
+// Grouping (host): strings are taken in order while some c in [min(4, T), T] has
+// c + r <= T, T = min(n, 13), and the group holds at most 8 strings; the widest such c is
+// used, which makes c + r = T: every stage is 2^T amplitudes (64 KB at n >= 13) and a row
+// has 2^(n - T) cosets.
+//
+// CTA: one producer warp (bulk copies of a stage's chunks completing on the stage's full
+// mbarrier) and eight consumer warps; three stages in flight.  Expvals: each consumer
+// thread accumulates Re(conj(psi_u) (P_s psi)_u) in float32 over its amplitudes of the
+// coset, the CTA reduces in float64 and writes one partial per (coset, string); the
+// partials are summed per row in a fixed order (k_expval_finish).  Backward seed: each
+// consumer thread forms sum_s c_s (P_s psi)_u for two amplitudes and stores them to the
+// output row (added to what is there for groups after the first).
+// Every mbarrier wait is bounded: on expiry the CTA records TQK_TIMEOUT in the status
+// word, stops issuing copies and waiting, writes NaN expval partials (the seed skips its
+// stores), waits (bounded) for its copies in flight and exits.
+constexpr int kCosetTileBits = 13;
+constexpr int kCosetMinChunkBits = 4;
+constexpr int kCosetMaxRank = kCosetTileBits - kCosetMinChunkBits;
+constexpr int kCosetStages = 3;
+constexpr int kCosetConsumerWarps = 8;
+constexpr int kCosetConsumers = 32 * kCosetConsumerWarps;
+constexpr int kCosetThreads = kCosetConsumers + 32;
+
+struct CosetParams {
   const float2* state;
-  float2* out;
-  int n;
-  int ns;
-  uint64_t x[kMaxApplyStrings], z[kMaxApplyStrings];
-  int ny[kMaxApplyStrings];
-  const float* coef;  // [bsz][m] + col0
-  int m, col0;
-  int accumulate;
+  float2* out;       // seed: output rows; expvals: unused
+  const float* coef; // seed: [bsz][m] weights; column col[s]
+  double* partial;   // expvals: [bsz * cosets][kMaxStringsPerPass]
+  int* status;
+  int64_t bsz, cosets;  // cosets per row = 2^(n - c - r)
+  int n, c, r, tb;      // tb = c + r
+  int m, accumulate, ns;
+  uint32_t basis[kCosetMaxRank];
+  int piv[kCosetMaxRank];  // ascending
+  uint32_t xs[kMaxStringsPerPass], gam[kMaxStringsPerPass], zh[kMaxStringsPerPass];
+  uint32_t fl[kMaxStringsPerPass];   // constant sign bit (expvals: ny >> 1; seed: (ny & 1) ^ (ny >> 1))
+  uint32_t odd[kMaxStringsPerPass];  // ny & 1
+  int col[kMaxStringsPerPass];
 };
 
-// out[i] (+)= sum_s c_s (P_s psi)[i], (P_s psi)[i] = i^ny (-1)^popcount((i ^ x) & z) psi[i ^ x]
-// (the sign algebra above: one popcount per string for the two outputs of a thread).
-template <typename I>
-__global__ void __launch_bounds__(256) k_pauli_apply_sum(const ApplySumParams p) {
-  const int64_t b = blockIdx.y;
-  const I half = static_cast<I>((1ll << p.n) >> 1);
-  const I t = static_cast<I>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= half) return;
-  const float2* row = p.state + (b << p.n);
-  float2* orow = p.out + (b << p.n);
-  const I i = t * 2;
-  float2 o0 = make_float2(0.f, 0.f), o1 = make_float2(0.f, 0.f);
-  if (p.accumulate) {
-    const float4 v = ld4(orow + i);
-    o0 = lo2(v);
-    o1 = hi2(v);
+__device__ __forceinline__ void mbar_init_count(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bulk::smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bulk::smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ float4 lds4(const float2* p) { return *reinterpret_cast<const float4*>(p); }
+
+// rep(t): t with a zero inserted at each pivot bit (ascending)
+__device__ __forceinline__ uint32_t coset_rep(uint32_t t, const CosetParams& p) {
+  for (int k = 0; k < p.r; ++k) {
+    const int q = p.piv[k];
+    t = ((t >> q) << (q + 1)) | (t & ((1u << q) - 1u));
   }
-  // partner loads of up to kApplyChunk strings issued together, then the arithmetic
-  for (int s0 = 0; s0 < p.ns; s0 += kApplyChunk) {
-    float4 w[kApplyChunk];
+  return t;
+}
+
+template <bool SEED, int NS>
+__global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p) {
+  extern __shared__ __align__(128) unsigned char coset_smem[];
+  __shared__ __align__(8) uint64_t full[kCosetStages], empty[kCosetStages];
+  __shared__ uint32_t slot_h[kCosetStages][1 << kCosetMaxRank];
+  __shared__ float red[2][kCosetConsumerWarps][kMaxStringsPerPass];
+  __shared__ int quit;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t tile = 1u << p.tb;
+  float2* const stage0 = reinterpret_cast<float2*>(coset_smem);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kCosetStages; ++s) {
+      mbar_init_count(&full[s], 1);
+      mbar_init_count(&empty[s], kCosetConsumerWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    quit = 0;
+  }
+  __syncthreads();
+  const int64_t total = p.bsz * p.cosets;
+  volatile int* vquit = &quit;
+  int issued[kCosetStages] = {0, 0, 0};  // producer: loads issued per stage
+  if (warp == kCosetConsumerWarps) {
+    // ---------------- producer
+    const uint32_t chunk_bytes = 8u << p.c;
+    const int nslots = 1 << p.r;
+    int it = 0;
+    for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
+      const int st = it % kCosetStages;
+      const uint32_t round = static_cast<uint32_t>(it / kCosetStages);
+      if (*vquit) continue;
+      if (round > 0 && !bulk::mbar_wait(&empty[st], (round - 1) & 1u)) {
+        if (lane == 0) {
+          atomicExch(p.status, TQK_TIMEOUT);
+          *vquit = 1;
+        }
+        continue;
+      }
+      const int64_t b = item / p.cosets;
+      const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
+      for (int a = lane; a < nslots; a += 32) {
+        uint32_t h = rep;
+        for (int k = 0; k < p.r; ++k)
+          if ((a >> k) & 1) h ^= p.basis[k];
+        slot_h[st][a] = h;
+      }
+      __syncwarp();
+      if (lane == 0) bulk::mbar_expect(&full[st], tile * 8u);
+      __syncwarp();
+      const float2* row = p.state + (static_cast<uint64_t>(b) << p.n);
+      float2* dst = stage0 + static_cast<size_t>(st) * tile;
+      for (int a = lane; a < nslots; a += 32)
+        bulk::bulk_load(dst + (static_cast<size_t>(a) << p.c), row + (static_cast<uint64_t>(slot_h[st][a]) << p.c),
+                        chunk_bytes, &full[st]);
+      issued[st]++;
+    }
+  } else {
+    // ---------------- consumers
+    const int ct = threadIdx.x;
+    uint32_t xs[NS], gam[NS], odd[NS];
 #pragma unroll
-    for (int u = 0; u < kApplyChunk; ++u)
-      if (s0 + u < p.ns) w[u] = ld4(row + ((i ^ static_cast<I>(p.x[s0 + u])) & ~I(1)));
+    for (int s = 0; s < NS; ++s) {
+      xs[s] = s < p.ns ? p.xs[s] : 0u;
+      gam[s] = s < p.ns ? p.gam[s] : 0u;
+      odd[s] = s < p.ns ? p.odd[s] : 0u;
+    }
+    const uint32_t lmask = (1u << p.c) - 1u;
+    int it = 0;
+    for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
+      const int st = it % kCosetStages;
+      const uint32_t round = static_cast<uint32_t>(it / kCosetStages);
+      const int64_t b = item / p.cosets;
+      const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
+      uint32_t rho[NS];
+      float cf[NS];
 #pragma unroll
-    for (int u = 0; u < kApplyChunk; ++u) {
-      const int s = s0 + u;
-      if (s >= p.ns) break;
-      const I x = static_cast<I>(p.x[s]), z = static_cast<I>(p.z[s]);
-      const int ny = p.ny[s];
-      const bool sw = (x & I(1)) != 0;
-      const float2 src0 = sw ? hi2(w[u]) : lo2(w[u]), src1 = sw ? lo2(w[u]) : hi2(w[u]);
-      // i^ny: a quarter turn for odd ny, a sign for ny >= 2 (folded into the parity)
-      const float c0 = flip_if_odd(__ldg(p.coef + b * p.m + p.col0 + s),
-                                   popc_t<I>((i ^ x) & z) + static_cast<uint32_t>(ny >> 1));
-      const float c1 = (z & I(1)) ? -c0 : c0;
-      if (ny & 1) {
-        o0.x = fmaf(-c0, src0.y, o0.x);
-        o0.y = fmaf(c0, src0.x, o0.y);
-        o1.x = fmaf(-c1, src1.y, o1.x);
-        o1.y = fmaf(c1, src1.x, o1.y);
-      } else {
-        o0.x = fmaf(c0, src0.x, o0.x);
-        o0.y = fmaf(c0, src0.y, o0.y);
-        o1.x = fmaf(c1, src1.x, o1.x);
-        o1.y = fmaf(c1, src1.y, o1.y);
+      for (int s = 0; s < NS; ++s) {
+        rho[s] = s < p.ns ? ((static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u) : 0u;
+        cf[s] = (SEED && s < p.ns) ? __ldg(p.coef + b * p.m + p.col[s]) : 0.f;
+      }
+      bool ok = *vquit == 0;
+      if (ok && !bulk::mbar_wait(&full[st], round & 1u)) {
+        ok = false;
+        if (lane == 0) {
+          atomicExch(p.status, TQK_TIMEOUT);
+          *vquit = 1;
+        }
+      }
+      const float2* stg = stage0 + static_cast<size_t>(st) * tile;
+      float acc[NS];
+#pragma unroll
+      for (int s = 0; s < NS; ++s) acc[s] = 0.f;
+      if (ok) {
+        for (uint32_t q = ct; q < (tile >> 1); q += kCosetConsumers) {
+          const uint32_t u = q << 1;
+          float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+          if (!SEED) {
+            const float4 v = lds4(stg + u);
+            a0 = lo2(v);
+            a1 = hi2(v);
+          }
+          float2 o0 = make_float2(0.f, 0.f), o1 = o0;
+#pragma unroll
+          for (int s = 0; s < NS; ++s) {
+            if (s >= p.ns) break;
+            const float4 w = lds4(stg + ((u ^ xs[s]) & ~1u));
+            const bool sw = (xs[s] & 1u) != 0;
+            const float2 b0 = sw ? hi2(w) : lo2(w), b1 = sw ? lo2(w) : hi2(w);
+            const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
+            if (SEED) {
+              const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);
+              if (odd[s]) {
+                o0.x = fmaf(-c0, b0.y, o0.x);
+                o0.y = fmaf(c0, b0.x, o0.y);
+                o1.x = fmaf(-c1, b1.y, o1.x);
+                o1.y = fmaf(c1, b1.x, o1.y);
+              } else {
+                o0.x = fmaf(c0, b0.x, o0.x);
+                o0.y = fmaf(c0, b0.y, o0.y);
+                o1.x = fmaf(c1, b1.x, o1.x);
+                o1.y = fmaf(c1, b1.y, o1.y);
+              }
+            } else {
+              float c0, c1;
+              if (odd[s]) {
+                c0 = a0.x * b0.y - a0.y * b0.x;
+                c1 = a1.x * b1.y - a1.y * b1.x;
+              } else {
+                c0 = a0.x * b0.x + a0.y * b0.y;
+                c1 = a1.x * b1.x + a1.y * b1.y;
+              }
+              acc[s] += flip_if_odd(c0 + flip_if_odd(c1, gam[s] & 1u), pb);
+            }
+          }
+          if (SEED) {
+            float2* dst = p.out + (static_cast<uint64_t>(b) << p.n) +
+                          (static_cast<uint64_t>(slot_h[st][u >> p.c]) << p.c) + (u & lmask);
+            if (p.accumulate) {
+              const float4 old = ld4(dst);
+              o0.x += old.x;
+              o0.y += old.y;
+              o1.x += old.z;
+              o1.y += old.w;
+            }
+            st4(dst, pack4(o0, o1));
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);
+      if (!SEED) {
+        // CTA sum of each string's accumulators: warps in float32, the warps' sums in
+        // float64 in a fixed order; red is double-buffered by item parity
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+        if (lane == 0)
+#pragma unroll
+          for (int s = 0; s < NS; ++s) red[it & 1][warp][s] = acc[s];
+        asm volatile("bar.sync 1, %0;" ::"n"(kCosetConsumers) : "memory");
+        if (warp == 0 && lane < p.ns) {
+          double sum = 0.0;
+          for (int w = 0; w < kCosetConsumerWarps; ++w) sum += static_cast<double>(red[it & 1][w][lane]);
+          p.partial[item * kMaxStringsPerPass + lane] = (*vquit == 0) ? sum : __longlong_as_double(0x7ff8000000000000ll);
+        }
       }
     }
   }
-  st4(orow + i, pack4(o0, o1));
+  __syncthreads();
+  // after a timeout, wait (bounded) for this CTA's copies still in flight before exiting
+  if (quit && warp == kCosetConsumerWarps && lane == 0) {
+    for (int st = 0; st < kCosetStages; ++st)
+      if (issued[st] > 0) bulk::mbar_wait(&full[st], static_cast<uint32_t>(issued[st] - 1) & 1u);
+  }
+}
+
+// Host plan of one coset pass.
+struct CosetGroup {
+  int c, r, ns;
+  uint32_t basis[kCosetMaxRank];
+  int piv[kCosetMaxRank];
+  int idx[kMaxStringsPerPass];
+};
+
+// Reduced echelon basis of the vectors (GF(2)); returns the rank, or -1 past max_rank.
+static int gf2_reduced_basis(const uint32_t* v, int cnt, uint32_t* basis, int* piv, int max_rank) {
+  int r = 0;
+  for (int i = 0; i < cnt; ++i) {
+    uint32_t x = v[i];
+    for (int k = 0; k < r; ++k)
+      if ((x >> piv[k]) & 1u) x ^= basis[k];
+    if (x == 0) continue;
+    if (r == max_rank) return -1;
+    const int q = 31 - __builtin_clz(x);
+    for (int k = 0; k < r; ++k)
+      if ((basis[k] >> q) & 1u) basis[k] ^= x;
+    basis[r] = x;
+    piv[r] = q;
+    ++r;
+  }
+  for (int i = 1; i < r; ++i)  // ascending pivots
+    for (int j = i; j > 0 && piv[j - 1] > piv[j]; --j) {
+      const int tp = piv[j];
+      piv[j] = piv[j - 1];
+      piv[j - 1] = tp;
+      const uint32_t tb = basis[j];
+      basis[j] = basis[j - 1];
+      basis[j - 1] = tb;
+    }
+  return r;
+}
+
+// Rank of {x_j >> c} (j in idx), or -1 when it exceeds max_rank.
+static int coset_rank(const uint64_t* xmask, const int* idx, int cnt, int c, int max_rank, uint32_t* basis,
+                      int* piv) {
+  uint32_t v[kMaxStringsPerPass];
+  for (int i = 0; i < cnt; ++i) v[i] = static_cast<uint32_t>(xmask[idx[i]] >> c);
+  return gf2_reduced_basis(v, cnt, basis, piv, max_rank);
+}
+
+// Greedy grouping of the strings (in order) into coset passes; fills the groups' c and
+// basis.  n <= 34, so x >> c fits 32 bits for c >= 4 (and c = n for n <= 4).
+static void coset_plan(int n, const uint64_t* xmask, int m, std::vector<CosetGroup>& groups) {
+  const int T = n < kCosetTileBits ? n : kCosetTileBits;
+  const int cmin = T < kCosetMinChunkBits ? T : kCosetMinChunkBits;
+  groups.clear();
+  CosetGroup g;
+  g.ns = 0;
+  uint32_t basis[kCosetMaxRank];
+  int piv[kCosetMaxRank];
+  for (int j = 0; j < m; ++j) {
+    if (g.ns > 0) {
+      g.idx[g.ns] = j;
+      const bool fits = g.ns < kMaxStringsPerPass && coset_rank(xmask, g.idx, g.ns + 1, cmin, T - cmin, basis, piv) >= 0;
+      if (!fits) {
+        groups.push_back(g);
+        g.ns = 0;
+      }
+    }
+    g.idx[g.ns++] = j;
+  }
+  if (g.ns > 0) groups.push_back(g);
+  for (CosetGroup& gr : groups) {
+    int c = cmin;
+    while (c < T && coset_rank(xmask, gr.idx, gr.ns, c + 1, T - (c + 1), basis, piv) >= 0) ++c;
+    gr.c = c;
+    gr.r = coset_rank(xmask, gr.idx, gr.ns, c, T - c, gr.basis, gr.piv);
+  }
+}
+
+static int coset_tile_bits(int n) { return n < kCosetTileBits ? n : kCosetTileBits; }
+
+// Stage coordinates of the group's strings; per-string sign constants.
+static void coset_params(const CosetGroup& g, int n, const uint64_t* xmask, const uint64_t* zmask, bool seed,
+                         CosetParams& p) {
+  p.n = n;
+  p.c = g.c;
+  p.r = g.r;
+  p.tb = g.c + g.r;
+  p.cosets = 1ll << (n - p.tb);
+  p.ns = g.ns;
+  for (int k = 0; k < kCosetMaxRank; ++k) {
+    p.basis[k] = k < g.r ? g.basis[k] : 0u;
+    p.piv[k] = k < g.r ? g.piv[k] : 0;
+  }
+  const uint32_t lmask = (1u << g.c) - 1u;
+  for (int s = 0; s < kMaxStringsPerPass; ++s) {
+    if (s >= g.ns) {
+      p.xs[s] = p.gam[s] = p.zh[s] = p.fl[s] = p.odd[s] = 0u;
+      p.col[s] = 0;
+      continue;
+    }
+    const int j = g.idx[s];
+    const uint32_t xh = static_cast<uint32_t>(xmask[j] >> g.c), zh = static_cast<uint32_t>(zmask[j] >> g.c);
+    uint32_t a = 0, beta = 0;
+    for (int k = 0; k < g.r; ++k) {
+      if ((xh >> g.piv[k]) & 1u) a |= 1u << k;
+      if (__builtin_popcount(g.basis[k] & zh) & 1) beta |= 1u << k;
+    }
+    const int ny = __builtin_popcountll(xmask[j] & zmask[j]) & 3;
+    p.xs[s] = (a << g.c) | (static_cast<uint32_t>(xmask[j]) & lmask);
+    p.gam[s] = (beta << g.c) | (static_cast<uint32_t>(zmask[j]) & lmask);
+    p.zh[s] = zh;
+    p.odd[s] = static_cast<uint32_t>(ny & 1);
+    p.fl[s] = seed ? static_cast<uint32_t>((ny & 1) ^ (ny >> 1)) : static_cast<uint32_t>(ny >> 1);
+    p.col[s] = j;
+  }
+}
+
+template <bool SEED, int NS>
+static int launch_coset_ns(const CosetParams& p, cudaStream_t st) {
+  static std::atomic<uint64_t> configured{0};  // devices whose attribute is set
+  const size_t smem = static_cast<size_t>(kCosetStages) * (8ull << p.tb);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(configured.load() & bit)) {
+    // the largest dynamic request (2^13-amplitude stages)
+    if (cudaFuncSetAttribute(k_coset<SEED, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kCosetStages * (8ull << kCosetTileBits))) != cudaSuccess)
+      return fail(TQK_CUDA_ERROR, "coset pass: cannot reserve %d bytes of shared memory",
+                  static_cast<int>(kCosetStages * (8ull << kCosetTileBits)));
+    configured.fetch_or(bit);
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t total = p.bsz * p.cosets;
+  const int64_t grid = total < sms ? total : sms;
+  k_coset<SEED, NS><<<static_cast<unsigned>(grid), kCosetThreads, smem, st>>>(p);
+  return TQK_OK;
+}
+
+template <bool SEED>
+static int launch_coset(const CosetParams& p, cudaStream_t st) {
+  if (p.ns <= 1) return launch_coset_ns<SEED, 1>(p, st);
+  if (p.ns <= 2) return launch_coset_ns<SEED, 2>(p, st);
+  if (p.ns <= 4) return launch_coset_ns<SEED, 4>(p, st);
+  return launch_coset_ns<SEED, 8>(p, st);
 }
 
 __global__ void __launch_bounds__(256) k_probs(const float2* state, float* out, int64_t total_half) {
@@ -413,22 +649,24 @@ extern "C" int tqk_probs(const void* state, int64_t bsz, int n, float* out, void
 }
 
 extern "C" int64_t tqk_pauli_expval_scratch_bytes(int64_t bsz, int n, int m) {
-  // partials [bsz][nblk][kMaxStringsPerPass] per pass (passes reuse the region; the
-  // stream orders them)
-  int64_t nblk = reduce_blocks_per_row(bsz, n);
-  const int64_t rb = rows_blocks(n);  // the row sweep's partials, when it may be used
-  if (rb > nblk) nblk = rb;
+  // partials per pass, reused by every pass (the stream orders them): the per-X-mask pass
+  // writes [bsz][blocks per row][8], a coset pass [bsz][2^(n - T)][8] (one per coset)
   (void)m;
-  return bsz * nblk * kMaxStringsPerPass * (int64_t)sizeof(double);
+  const int64_t nblk = reduce_blocks_per_row(bsz, n);
+  const int64_t cosets = 1ll << (n - coset_tile_bits(n));
+  const int64_t per_row = nblk > cosets ? nblk : cosets;
+  return bsz * per_row * kMaxStringsPerPass * static_cast<int64_t>(sizeof(double));
 }
 
 extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uint64_t* xmask, const uint64_t* zmask,
-                                int m, double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+                                int m, double* out, void* scratch, int64_t scratch_bytes, int* status,
+                                void* stream) {
   const char* what = "tqk_pauli_expval";
   int rc = check_state(state, bsz, n, what);
   if (rc) return rc;
   if (m <= 0) return TQK_OK;
   if (!xmask || !zmask || !out) return fail(TQK_BAD_POINTER, "%s: null mask/output pointer", what);
+  if (status == nullptr) return fail(TQK_BAD_POINTER, "%s: null status word", what);
   if (scratch == nullptr || scratch_bytes < tqk_pauli_expval_scratch_bytes(bsz, n, m))
     return fail(TQK_SCRATCH_TOO_SMALL, "%s: scratch of %lld bytes needed", what,
                 (long long)tqk_pauli_expval_scratch_bytes(bsz, n, m));
@@ -438,30 +676,29 @@ extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uin
   cudaStream_t st = as_stream(stream);
   const int64_t nblk = reduce_blocks_per_row(bsz, n);
   double* partial = static_cast<double*>(scratch);
-  // several X-masks and rows that stay in L2: sweep the rows once per 8 strings
-  const int64_t rb = rows_blocks(n);
   bool several = false;
   for (int j = 1; j < m && !several; ++j) several = xmask[j] != xmask[0];
-  if (rb > 0 && several) {
-    for (int j0 = 0; j0 < m; j0 += kMaxStringsPerPass) {
-      RowsParams p;
+  if (several) {
+    // strings with different X-masks: coset passes (every partner read on chip)
+    std::vector<CosetGroup> groups;
+    coset_plan(n, xmask, m, groups);
+    for (const CosetGroup& g : groups) {
+      CosetParams p;
+      coset_params(g, n, xmask, zmask, false, p);
       p.state = static_cast<const float2*>(state);
-      p.n = n;
-      p.bsz = bsz;
+      p.out = nullptr;
+      p.coef = nullptr;
       p.partial = partial;
-      p.ns = (m - j0) < kMaxStringsPerPass ? (m - j0) : kMaxStringsPerPass;
-      FinishCols cols;
-      for (int s = 0; s < kMaxStringsPerPass; ++s) {
-        const bool on = s < p.ns;
-        p.x[s] = on ? xmask[j0 + s] : 0;
-        p.z[s] = on ? zmask[j0 + s] : 0;
-        p.ny[s] = on ? __builtin_popcountll(xmask[j0 + s] & zmask[j0 + s]) & 3 : 0;
-        cols.c[s] = on ? j0 + s : 0;
-      }
-      const unsigned grid = n <= 31 ? launch_rows<uint32_t>(p, rb, st) : launch_rows<uint64_t>(p, rb, st);
+      p.status = status;
+      p.bsz = bsz;
+      p.m = m;
+      p.accumulate = 0;
+      if ((rc = launch_coset<false>(p, st))) return rc;
       if ((rc = launch_status(what))) return rc;
-      k_expval_finish<<<(unsigned)bsz, kFinishThreads, 0, st>>>(partial, grid, p.ns, kMaxStringsPerPass,
-                                                                        cols, m, out, bsz);
+      FinishCols cols;
+      for (int s = 0; s < kMaxStringsPerPass; ++s) cols.c[s] = s < g.ns ? g.idx[s] : 0;
+      k_expval_finish<<<(unsigned)bsz, kFinishThreads, 0, st>>>(partial, p.cosets, g.ns, kMaxStringsPerPass, cols,
+                                                                m, out, bsz);
       if ((rc = launch_status(what))) return rc;
     }
     return TQK_OK;
@@ -510,34 +747,34 @@ extern "C" int tqk_pauli_expval(const void* state, int64_t bsz, int n, const uin
 }
 
 extern "C" int tqk_pauli_apply_sum(const void* state, int64_t bsz, int n, const uint64_t* xmask,
-                                   const uint64_t* zmask, int m, const float* coef, void* out, void* stream) {
+                                   const uint64_t* zmask, int m, const float* coef, void* out, int* status,
+                                   void* stream) {
   const char* what = "tqk_pauli_apply_sum";
   int rc = check_state(state, bsz, n, what);
   if (rc) return rc;
   if ((rc = check_state(out, bsz, n, what))) return rc;
   if (m <= 0) return fail(TQK_BAD_SHAPE, "%s: need at least one string", what);
   if (!xmask || !zmask || !coef) return fail(TQK_BAD_POINTER, "%s: null pointer", what);
+  if (status == nullptr) return fail(TQK_BAD_POINTER, "%s: null status word", what);
+  if (out == state) return fail(TQK_BAD_POINTER, "%s: out must not alias the state", what);
+  const uint64_t lim = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+  for (int j = 0; j < m; ++j)
+    if ((xmask[j] | zmask[j]) & ~lim) return fail(TQK_BAD_WIRES, "%s: string %d has bits beyond n_wires=%d", what, j, n);
   cudaStream_t st = as_stream(stream);
-  const int64_t half = (1ll << n) >> 1;
-  for (int j0 = 0; j0 < m; j0 += kMaxApplyStrings) {
-    ApplySumParams p;
+  std::vector<CosetGroup> groups;
+  coset_plan(n, xmask, m, groups);
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    CosetParams p;
+    coset_params(groups[gi], n, xmask, zmask, true, p);
     p.state = static_cast<const float2*>(state);
     p.out = static_cast<float2*>(out);
-    p.n = n;
-    p.ns = (m - j0) < kMaxApplyStrings ? (m - j0) : kMaxApplyStrings;
-    for (int s = 0; s < p.ns; ++s) {
-      p.x[s] = xmask[j0 + s];
-      p.z[s] = zmask[j0 + s];
-      p.ny[s] = __builtin_popcountll(xmask[j0 + s] & zmask[j0 + s]) & 3;
-    }
     p.coef = coef;
+    p.partial = nullptr;
+    p.status = status;
+    p.bsz = bsz;
     p.m = m;
-    p.col0 = j0;
-    p.accumulate = j0 > 0;
-    const int threads = threads_for(half);
-    dim3 grid((unsigned)((half + threads - 1) / threads), (unsigned)bsz, 1);
-    if (n <= 31) k_pauli_apply_sum<uint32_t><<<grid, threads, 0, st>>>(p);
-    else k_pauli_apply_sum<uint64_t><<<grid, threads, 0, st>>>(p);
+    p.accumulate = gi > 0;
+    if ((rc = launch_coset<true>(p, st))) return rc;
     if ((rc = launch_status(what))) return rc;
   }
   return TQK_OK;
