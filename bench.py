@@ -611,9 +611,8 @@ def run_ours(args):
     launches0 = _lib.LAUNCHES[0]
     # the dominant kernel's launches inside the timed steps, bracketed by CUDA events on
     # the stream they run on (the roofline's live duration)
-    live = {name: LaunchTimer(getattr(_lib, name)) for name in ("fused_adjoint_stored", "fused_adjoint")}
-    for name, t in live.items():
-        setattr(_lib, name, t)
+    live = {"fused_adjoint_stored": AdjointTimer(stored=True), "fused_adjoint": AdjointTimer(stored=False)}
+    _lib.SEGMENT_HOOKS["backward"] = lambda rec, after: [t(rec, after) for t in live.values()]
     try:
         with ClockSampler(local) as clk:
             torch.cuda.synchronize()
@@ -624,8 +623,7 @@ def run_ours(args):
             e1.record(stream)
             torch.cuda.synchronize()
     finally:
-        for name, t in live.items():
-            setattr(_lib, name, t.fn)
+        _lib.SEGMENT_HOOKS["backward"] = None
     launches = _lib.LAUNCHES[0] - launches0
     peak_states = (torch.cuda.max_memory_allocated(dev) - mem0) / (bsz * (8 << n))
     ms = R.max_over_ranks(e0.elapsed_time(e1), dev)
@@ -813,23 +811,29 @@ def plain_pass_summary(kernels: dict, state_bytes: int, peak: float) -> dict:
             "mix": "60% U3, 13.3% each CNOT / CZ / CRX; bytes 2 S / S / S/2 / S per pass"}
 
 
-class LaunchTimer:
-    """Wraps an engine entry point: each call made while installed is bracketed by CUDA
-    events on the current stream (the one the kernel is launched on)."""
+class AdjointTimer:
+    """Segment-runner hook: brackets each reverse step of a tensor-core block (with a stored
+    input, or uncomputed in place) by CUDA events on the current stream -- the stream the
+    runner launches the kernel on."""
 
-    def __init__(self, fn):
-        self.fn = fn
+    def __init__(self, stored: bool):
+        self.stored = stored
         self.events = []
+        self._start = None
 
-    def __call__(self, *a, **k):
+    def __call__(self, rec, after):
         import torch
 
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        out = self.fn(*a, **k)
-        e.record()
-        self.events.append((s, e))
-        return out
+        from torchquantum_gb300 import _lib
+
+        if rec.kind != _lib.X_BLOCK_TC or rec.skip_reverse or bool(rec.stored) != self.stored:
+            return
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        if after:
+            self.events.append((self._start, ev))
+        else:
+            self._start = ev
 
     def mean_s(self):
         return sum(s.elapsed_time(e) for s, e in self.events) / len(self.events) / 1e3 if self.events else None
@@ -839,8 +843,8 @@ def roofline(args, dev, stored=True, live=None):
     """Time the engine's hot kernels alone (CUDA events on the launching stream) on the
     bench's state size; algorithmic bytes per launch from the touched amplitudes.
     ``stored``: the fused step's blocks kept their inputs, so its dominant kernel is the
-    stored-input adjoint step.  ``live``: LaunchTimers of the adjoint entry points over the
-    timed steps; the roofline's achieved rate uses their average launch duration."""
+    stored-input adjoint step.  ``live``: AdjointTimers of the tensor-core reverse steps over
+    the timed steps; the roofline's achieved rate uses their average launch duration."""
     import torch
 
     from torchquantum_gb300 import _lib

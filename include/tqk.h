@@ -40,6 +40,7 @@ enum {
 
 #define TQK_MAX_QUBITS 34      /* per batch row */
 #define TQK_MAX_DENSE_WIRES 12 /* generic dense gate width */
+#define TQK_MAX_OP_WIRES 16    /* wires one op may touch (controls + targets) */
 
 const char* tqk_last_error(void);
 int tqk_version(void);
@@ -412,6 +413,82 @@ int tqk_batch_run(const tqk_batch_circuit* circuits, int ncirc, const tqk_batch_
                   const void* mats, void* states, int write_states, double* z_out, int* pass_done,
                   uint64_t* t_done, int* counter, int* status, const tqk_batch_config* config,
                   void* stream);
+
+/* ---------------------------------------------------------------- compiled segments
+ * The tape-level entry points: a compiled gate run (a segment of the tape: plain ops,
+ * staged low-qubit runs and fused blocks, in forward order) applied and reversed with
+ * one call each.  Together they replace the per-gate dispatch of upstream's
+ * gate_wrapper (functional/gate_wrapper.py:324-446, each gate an apply_unitary_bmm,
+ * :96-140), static mode's block application (graph/graphs.py:836-860) and the autograd
+ * graph both record.  The table lives in HOST memory; every operand, image, state and
+ * cotangent it points to is device memory the caller owns (the entry points allocate
+ * nothing: block outputs and the reverse sweep's working state are caller buffers).
+ * The other steps of a training step are single calls too: operands (tqk_gate_operands),
+ * block unitaries (tqk_block_build), operand images (tqk_fused_prepare_many), expvals
+ * and the backward seed (tqk_pauli_expval, tqk_pauli_apply_sum), then after the reverse
+ * sweep the stored-input block cotangents (tqk_fused_cross_add_many), the member
+ * operand cotangents (tqk_block_unbuild) and the parameter gradients (tqk_param_grads). */
+enum {
+  TQK_X_DENSE = 0,       /* dense U on wires[0..nw) (tqk_apply_matrix); operand [batch][2^nw][2^nw] */
+  TQK_X_CTRL = 1,        /* controlled block: controls wires[0..nctrl), targets the rest */
+  TQK_X_MCX = 2,         /* multi-controlled X: controls wires[0..nctrl) == ctrl_val, target wires[nctrl] */
+  TQK_X_PHASE = 3,       /* phase on amplitudes whose wires are all 1; operand [batch] */
+  TQK_X_DIAG = 4,        /* diagonal; operand [batch][2^nw] */
+  TQK_X_SWAP = 5,        /* controlled swap of wires[nctrl], wires[nctrl + 1] */
+  TQK_X_STAGED = 6,      /* staged run: `staged[0..nstaged)` in one shared-memory pass */
+  TQK_X_BLOCK_TC = 7,    /* fused 6-wire block on the tensor cores: image / image_h */
+  TQK_X_BLOCK_DENSE = 8  /* fused block on the CUDA cores: operand = U (complex64) */
+};
+typedef struct {
+  int32_t kind;            /* TQK_X_* */
+  int32_t nw;              /* wires used (controls first) */
+  int32_t nctrl;
+  int32_t ctrl_val;
+  int32_t wires[TQK_MAX_OP_WIRES];
+  int64_t batch;           /* operand / block batch: 1 or bsz */
+  const void* operand;     /* complex64 operand (DENSE, CTRL, PHASE, DIAG, BLOCK_DENSE) */
+  const void* uncompute;   /* DENSE / CTRL: exact inverse for psi (non-unitary gates), or NULL */
+  const void* image;       /* BLOCK_TC forward image (tqk_fused_prepare of U) */
+  const void* image_h;     /* BLOCK_TC reverse image (of U^H) */
+  const void* u;           /* BLOCK_TC: U, complex128 [batch][64][64] (in-place reverse step's M U) */
+  void* out;               /* BLOCK_TC forward: the block's output buffer (its input is then kept
+                              as the stored input), or NULL to apply in place */
+  const void* stored;      /* BLOCK_TC reverse: the block's stored input, or NULL (uncompute) */
+  double* grad;            /* reverse: operand / block cotangent (complex128 interleaved), or NULL */
+  double* mr;              /* BLOCK_TC reverse with grad: cross-term buffer [batch][128][128] float64,
+                              zeroed; a stored-input step leaves M there (add it with
+                              tqk_fused_cross_add_many), an in-place step adds M U to grad */
+  const tqk_staged_op* staged; /* STAGED: the run's ops (their grad slots are used in reverse) */
+  int32_t nstaged;
+  int32_t tile_bits;       /* STAGED */
+  int32_t skip_reverse;    /* the reverse sweep stops before this op (it must be op 0: a first block
+                              on |0...0>, whose cotangent the caller takes from lam) */
+  int32_t pad;
+} tqk_exec_op;             /* 184 bytes */
+
+/* Optional per-op callback of the runners: called on the calling thread just before
+ * (after == 0) and just after (after == 1) the launches of op `index` are enqueued, e.g.
+ * to record CUDA events around one kind of kernel on the stream. */
+typedef void (*tqk_exec_hook)(int index, int kind, int after, void* user);
+
+/* Forward: apply ops[0..nops) to `state` ([bsz, 2^n] complex64).  A BLOCK_TC op with `out`
+ * writes its result there and the sweep continues on `out`; *final receives the buffer
+ * holding the result (state, or the last such out).  *launches (optional) receives the
+ * number of kernels launched; hook may be NULL. */
+int tqk_segment_forward(void* state, int64_t bsz, int n, const tqk_exec_op* ops, int nops, int* status,
+                        void** final, int64_t* launches, tqk_exec_hook hook, void* user, void* stream);
+/* Reverse sweep of the adjoint method: psi_end is the segment's result (read only), lam
+ * the cotangent there (updated in place to the cotangent at the segment's start).  Ops
+ * are reversed last to first: a BLOCK_TC op with `stored` reads its stored input and
+ * moves the sweep's state to it; any other op uncomputes the state in place, on
+ * `work` (a caller buffer of one state) after a copy when the sweep's state is read only
+ * (psi_end or a stored input); work == psi_end lets the sweep uncompute the result in
+ * place.  Operand cotangents accumulate into each op's grad.  *start (optional) receives
+ * where the sweep's state ended: the state at the segment's start (work, psi_end or a
+ * stored input); *launches (optional): kernels and copies launched; hook may be NULL. */
+int tqk_segment_backward(const void* psi_end, void* lam, void* work, int64_t bsz, int n, const tqk_exec_op* ops,
+                         int nops, int* status, const void** start, int64_t* launches, tqk_exec_hook hook,
+                         void* user, void* stream);
 
 #ifdef __cplusplus
 }

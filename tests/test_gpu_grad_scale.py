@@ -20,9 +20,12 @@ Workloads:
   (400 shared angles) + CZ ladder after a per-sample RY input layer, loss = sum of 50
   weighted Pauli strings; gradients of the shared angles and of the inputs.
 
-Tolerance: 1e-5 absolute on every gradient (complex64 arithmetic; split-BF16 tensor-core
-products in the fused method), as for amplitudes and expvals.  Each case prints its
-errors (run with ``-s``).
+Tolerance: 1e-5 absolute between the fused and plain gradients, and against the
+complex128 central differences at the headline size.  For the differentiation workload
+the shared angles' gradients sum 64 rows x 50 strings over 2^20 amplitudes per row and
+complex64 arithmetic reaches about 1e-4 of the largest gradient (~0.13), for the plain
+method as for the fused one: there the bound against central differences is
+max(1e-5, 1e-4 x max |grad|).  Each case prints its errors (run with ``-s``).
 """
 import numpy as np
 import pytest
@@ -176,12 +179,20 @@ def test_differentiation_workload_gradients_full_size():
             st = TR.run(n, 1, og, dev)
             vals.append(sum(wj * TR.expval_pauli(st, p, n).sum().item() for wj, p in zip(w, paulis)))
         fd_x.append(_stencil(vals))
+    gscale = max(np.abs(gp).max(), np.abs(xp).max())
     print(f"\ndifferentiation workload n={n} bsz={bsz}: max |grad theta| {np.abs(gp).max():.3e}, "
           f"max |grad x| {np.abs(xp).max():.3e}")
+    errs = {}
     for key, (g, gx) in res.items():
         d_plain = max(np.abs(g - gp).max(), np.abs(gx - xp).max())
-        d_fd = max(max(abs(g[c] - f) for (_, c), f in zip(picks, fd_t)),
-                   max(abs(gx[b, wi] - f) for (b, wi), f in zip(xpicks, fd_x)))
-        print(f"  {key:15s} max |grad - plain| {d_plain:.2e}  max |grad - fd128| {d_fd:.2e} "
-              f"(6 shared angles, 4 inputs)")
-        assert d_plain < TOL and d_fd < TOL, key
+        d_fd_t = max(abs(g[c] - f) for (_, c), f in zip(picks, fd_t))
+        d_fd_x = max(abs(gx[b, wi] - f) for (b, wi), f in zip(xpicks, fd_x))
+        errs[key] = (d_plain, max(d_fd_t, d_fd_x))
+        print(f"  {key:15s} max |grad - plain| {d_plain:.2e}  max |grad - fd128| shared angles {d_fd_t:.2e}, "
+              f"inputs {d_fd_x:.2e}")
+    # the shared angles' gradients sum 64 rows x 50 weighted strings over 2^20 amplitudes
+    # each: complex64 arithmetic (plain and fused alike) reaches about 1e-4 of the largest
+    # gradient here, while fused and plain agree within the 1e-5 bar
+    for key, (d_plain, d_fd) in errs.items():
+        assert d_plain < TOL, key
+        assert d_fd < max(TOL, 1e-4 * gscale), key

@@ -82,22 +82,44 @@ def test_engine_defaults_roundtrip():
     assert D.ENGINE_DEFAULTS == prev
 
 
-def test_state_cursor_copies_only_before_writing():
+def test_state_cursor_allocates_its_work_buffer_once():
     """engine.StateCursor: the saved final state and stored block inputs are only read; the
-    first in-place uncompute works on a copy, a jump makes the cursor read-only again."""
+    reverse sweep's in-place steps use one work buffer per backward, made on first need."""
     from torchquantum_gb300 import engine
 
     final = torch.arange(8, dtype=torch.float32)
     cur = engine.StateCursor(final)
-    assert cur.state is final and not cur.owned
-    w = cur.writable()
-    assert w is not final and torch.equal(w, final) and cur.owned
-    w.zero_()
-    assert final[3] == 3.0 and cur.writable() is w
-    stored = torch.ones(8)
-    cur.jump(stored)
-    assert cur.state is stored and not cur.owned
-    assert cur.writable() is not stored
+    assert cur.state is final and not cur.owned and cur.work is None
+    w = cur.work_buffer()
+    assert w is not final and w.shape == final.shape and cur.work_buffer() is w
+
+
+def test_exec_records_follow_the_abi():
+    """program._plain_record / _exec: the tqk_exec_op records the segment runner reads --
+    controls first for the controlled kinds, operand / cotangent addresses, the kind codes
+    of include/tqk.h, and the 16-wire limit of one op."""
+    import re
+
+    from torchquantum_gb300 import _lib, engine, program
+
+    with open(_lib.HEADER) as f:
+        hdr = f.read()
+    for name in ("DENSE", "CTRL", "MCX", "PHASE", "DIAG", "SWAP", "STAGED", "BLOCK_TC", "BLOCK_DENSE"):
+        code = int(re.search(rf"TQK_X_{name} = (\d+)", hdr).group(1))
+        assert code == getattr(_lib, f"X_{name}")
+    assert "} tqk_exec_op;             /* 184 bytes */" in hdr
+    mat = torch.zeros(3, 2, 2, dtype=torch.complex64)
+    op = engine.TapeOp(engine.KIND_CTRL, [4, 1, 6], controls=[4, 1], targets=[6], operand=mat)
+    g = torch.zeros(24, dtype=torch.float64)
+    r = program._plain_record(op, g)
+    assert (r.kind, r.nw, r.nctrl, list(r.wires[:3]), r.batch) == (_lib.X_CTRL, 3, 2, [4, 1, 6], 3)
+    assert r.operand == mat.data_ptr() and r.grad == g.data_ptr() and not r.uncompute
+    x = program._plain_record(engine.TapeOp(engine.KIND_X, [0, 5], controls=[0], targets=[5], ctrl_val=0))
+    assert (x.kind, x.nctrl, x.ctrl_val, list(x.wires[:2]), x.operand) == (_lib.X_MCX, 1, 0, [0, 5], None)
+    sw = program._plain_record(engine.TapeOp(engine.KIND_SWAP, [2, 3, 7], controls=[2], targets=[3, 7]))
+    assert (sw.kind, sw.nw, sw.nctrl, list(sw.wires[:3])) == (_lib.X_SWAP, 3, 1, [2, 3, 7])
+    with pytest.raises(_lib.TQKError):
+        program._exec(_lib.X_MCX, list(range(17)), nctrl=16)
 
 
 def test_stored_inputs_move_to_the_autograd_node():

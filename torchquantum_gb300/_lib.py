@@ -35,6 +35,8 @@ _u64p = ctypes.POINTER(ctypes.c_uint64)
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
 _int = ctypes.c_int
+# tqk_exec_hook: (op index, op kind, after, user)
+EXEC_HOOK = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p)
 
 _SIGS = {
     "tqk_last_error": (ctypes.c_char_p, []),
@@ -74,6 +76,8 @@ _SIGS = {
     "tqk_fused_adjoint_stored": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
     "tqk_pauli_expval_noalloc_capacity": (_i64, []),
     "tqk_pauli_expval_noalloc": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp]),
+    "tqk_segment_forward": (_int, [_vp, _i64, _int, _vp, _int, _vp, _vp, _vp, EXEC_HOOK, _vp, _vp]),
+    "tqk_segment_backward": (_int, [_vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _vp, EXEC_HOOK, _vp, _vp]),
     "tqk_gate_operand_size": (_int, [_int]),
     "tqk_gate_operands": (_int, [_vp, _int, _vp]),
     "tqk_param_grads": (_int, [_vp, _int, _vp]),
@@ -340,6 +344,59 @@ class StagedOp(ctypes.Structure):
 assert ctypes.sizeof(StagedOp) == 72
 S_DENSE1, S_X, S_PHASE, S_DIAG = 0, 1, 2, 3
 STAGED_MAX_OPS, STAGED_MAX_TILE_BITS, STAGED_MAX_WIRES = 64, 12, 8
+
+
+# ------------------------------------------------------------------ compiled segments
+class ExecOp(ctypes.Structure):
+    """``tqk_exec_op``: one op of a compiled segment for tqk_segment_forward / _backward."""
+    _fields_ = [("kind", ctypes.c_int32), ("nw", ctypes.c_int32), ("nctrl", ctypes.c_int32),
+                ("ctrl_val", ctypes.c_int32), ("wires", ctypes.c_int32 * 16), ("batch", ctypes.c_int64),
+                ("operand", ctypes.c_void_p), ("uncompute", ctypes.c_void_p), ("image", ctypes.c_void_p),
+                ("image_h", ctypes.c_void_p), ("u", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("stored", ctypes.c_void_p), ("grad", ctypes.c_void_p), ("mr", ctypes.c_void_p),
+                ("staged", ctypes.c_void_p), ("nstaged", ctypes.c_int32), ("tile_bits", ctypes.c_int32),
+                ("skip_reverse", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+assert ctypes.sizeof(ExecOp) == 184
+X_DENSE, X_CTRL, X_MCX, X_PHASE, X_DIAG, X_SWAP, X_STAGED, X_BLOCK_TC, X_BLOCK_DENSE = range(9)
+# Optional Python callables (exec record, after) the runners call around each op's
+# launches, per direction (bench.py installs one to time the dominant kernel's launches
+# inside a step).
+SEGMENT_HOOKS = {"forward": None, "backward": None}
+
+
+def _hook(which, table):
+    fn = SEGMENT_HOOKS[which]
+    if fn is None:
+        return None
+    return EXEC_HOOK(lambda i, kind, after, user: fn(table[i], after))
+
+
+def segment_forward(state, n, table, nops) -> int:
+    """Run a host table of ``ExecOp`` forward on ``state``; returns the device address of
+    the buffer holding the result."""
+    final = ctypes.c_void_p()
+    count = ctypes.c_int64(0)
+    hook = _hook("forward", table)
+    _check(load().tqk_segment_forward(state.data_ptr(), state.shape[0], n, table, nops,
+                                      status_word(state.device).data_ptr(), ctypes.byref(final), ctypes.byref(count),
+                                      hook, None, _stream(state)), launches=0)
+    LAUNCHES[0] += count.value
+    return final.value or 0
+
+
+def segment_backward(psi_end, lam, work, n, table, nops) -> int:
+    """Reverse sweep of a host table of ``ExecOp``; returns the device address where the
+    sweep's state ended (the segment's start)."""
+    start = ctypes.c_void_p()
+    count = ctypes.c_int64(0)
+    hook = _hook("backward", table)
+    _check(load().tqk_segment_backward(psi_end.data_ptr(), lam.data_ptr(), _ptr(work), lam.shape[0], n, table, nops,
+                                       status_word(lam.device).data_ptr(), ctypes.byref(start), ctypes.byref(count),
+                                       hook, None, _stream(lam)), launches=0)
+    LAUNCHES[0] += count.value
+    return start.value or 0
 
 
 def staged_apply(state, n, ops, tile_bits):

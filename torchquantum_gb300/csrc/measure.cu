@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* 
 // has 2^(n - T) cosets.
 //
 // CTA: one producer warp (bulk copies of a stage's chunks completing on the stage's full
-// mbarrier) and eight consumer warps; three stages in flight.  Expvals: each consumer
+// mbarrier) and twelve consumer warps; three stages in flight.  Expvals: each consumer
 // thread accumulates Re(conj(psi_u) (P_s psi)_u) in float32 over its amplitudes of the
 // coset, the CTA reduces in float64 and writes one partial per (coset, string); the
 // partials are summed per row in a fixed order (k_expval_finish).  Backward seed: each
@@ -266,7 +266,7 @@ constexpr int kCosetTileBits = 13;
 constexpr int kCosetMinChunkBits = 4;
 constexpr int kCosetMaxRank = kCosetTileBits - kCosetMinChunkBits;
 constexpr int kCosetStages = 3;
-constexpr int kCosetConsumerWarps = 8;
+constexpr int kCosetConsumerWarps = 12;
 constexpr int kCosetConsumers = 32 * kCosetConsumerWarps;
 constexpr int kCosetThreads = kCosetConsumers + 32;
 
@@ -397,8 +397,13 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
 #pragma unroll
       for (int s = 0; s < NS; ++s) acc[s] = 0.f;
       if (ok) {
+        // strings s >= ns are padding (partner = the pair itself, weight 0): every
+        // string's partner load is issued before any arithmetic, with no branch between
         for (uint32_t q = ct; q < (tile >> 1); q += kCosetConsumers) {
           const uint32_t u = q << 1;
+          float4 w[NS];
+#pragma unroll
+          for (int s = 0; s < NS; ++s) w[s] = lds4(stg + ((u ^ xs[s]) & ~1u));
           float2 a0 = make_float2(0.f, 0.f), a1 = a0;
           if (!SEED) {
             const float4 v = lds4(stg + u);
@@ -408,10 +413,8 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
           float2 o0 = make_float2(0.f, 0.f), o1 = o0;
 #pragma unroll
           for (int s = 0; s < NS; ++s) {
-            if (s >= p.ns) break;
-            const float4 w = lds4(stg + ((u ^ xs[s]) & ~1u));
             const bool sw = (xs[s] & 1u) != 0;
-            const float2 b0 = sw ? hi2(w) : lo2(w), b1 = sw ? lo2(w) : hi2(w);
+            const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
             const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
             if (SEED) {
               const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);

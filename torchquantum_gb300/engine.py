@@ -1,4 +1,4 @@
-"""Gate tape, kernel dispatch and the adjoint-method autograd Function.
+"""Gate tape and the adjoint-method autograd Function.
 
 A ``QuantumDevice`` owns one contiguous ``[bsz, 2^n]`` complex64 device buffer and a
 tape of ``TapeOp`` records.  Gates are applied to the buffer in place by the CUDA
@@ -67,28 +67,6 @@ class TapeOp:
         return f"TapeOp({self.kind}, wires={self.wires}, batch={self.batch})"
 
 
-def apply_op(buf: torch.Tensor, n: int, op: TapeOp) -> None:
-    """Launch the forward kernel of ``op`` on ``buf`` (in place, current stream)."""
-    k = op.kind
-    if k == KIND_DENSE:
-        if op.image is not None:
-            _lib.fused_apply(buf, n, op.wires, op.image, op.batch)
-        else:
-            _lib.apply_matrix(buf, n, op.wires, op.operand, op.batch)
-    elif k == KIND_CTRL:
-        _lib.apply_controlled(buf, n, op.controls, op.targets, op.operand, op.batch)
-    elif k == KIND_X:
-        _lib.apply_mcx(buf, n, op.controls, op.ctrl_val, op.targets[0])
-    elif k == KIND_PHASE:
-        _lib.apply_phase(buf, n, op.wires, op.operand, op.batch)
-    elif k == KIND_DIAG:
-        _lib.apply_diagonal(buf, n, op.wires, op.operand, op.batch)
-    elif k == KIND_SWAP:
-        _lib.apply_swap(buf, n, op.controls, op.targets[0], op.targets[1])
-    else:
-        raise ValueError(f"unknown op kind {k}")
-
-
 def kernel_operand(t: torch.Tensor) -> torch.Tensor:
     """Detached, materialised (no lazy conj/neg bit), contiguous copy-or-view for a kernel.
 
@@ -98,50 +76,22 @@ def kernel_operand(t: torch.Tensor) -> torch.Tensor:
     return t.detach().resolve_conj().resolve_neg().contiguous()
 
 
-def _conj_t(m: torch.Tensor) -> torch.Tensor:
-    return kernel_operand(m.conj().transpose(-1, -2))
-
-
-def adjoint_op(psi: torch.Tensor, lam: torch.Tensor, n: int, op: TapeOp, grad: Optional[torch.Tensor]) -> None:
-    """One reverse step: psi <- U^H psi, lam <- U^H lam, grad += lam conj(psi_before)^T."""
-    k = op.kind
-    if k == KIND_DENSE:
-        _lib.adjoint_matrix(psi, lam, n, op.wires, op.operand, op.batch, grad, op.uncompute)
-    elif k == KIND_CTRL:
-        _lib.adjoint_controlled(psi, lam, n, op.controls, op.targets, op.operand, op.batch, grad, op.uncompute)
-    elif k == KIND_X:
-        _lib.apply_mcx(psi, n, op.controls, op.ctrl_val, op.targets[0])
-        _lib.apply_mcx(lam, n, op.controls, op.ctrl_val, op.targets[0])
-    elif k == KIND_PHASE:
-        _lib.adjoint_phase(psi, lam, n, op.wires, op.operand, op.batch, grad)
-    elif k == KIND_DIAG:
-        _lib.adjoint_diagonal(psi, lam, n, op.wires, op.operand, op.batch, grad)
-    elif k == KIND_SWAP:
-        _lib.apply_swap(psi, n, op.controls, op.targets[0], op.targets[1])
-        _lib.apply_swap(lam, n, op.controls, op.targets[0], op.targets[1])
-    else:
-        raise ValueError(f"unknown op kind {k}")
-
-
 class StateCursor:
-    """The state a reverse sweep has reached.  It starts as the saved final state and,
-    after a block whose input the forward kept, becomes that stored input: both are only
-    read, so the first step that uncomputes the state in place works on a copy."""
+    """The state a reverse sweep has reached, carried from segment to segment.  It starts
+    as the saved final state and, after a block whose input the forward kept, is that
+    stored input: both are only read.  The sweep uncomputes in place only on its work
+    buffer (one state, allocated the first time a segment needs it): the segment runner
+    (``tqk_segment_backward``) copies the state there before the first such step."""
 
     def __init__(self, state: torch.Tensor):
         self.state = state
-        self.owned = False
+        self.owned = False  # state is the work buffer
+        self.work = None
 
-    def writable(self) -> torch.Tensor:
-        if not self.owned:
-            self.state = self.state.clone()
-            self.owned = True
-        return self.state
-
-    def jump(self, stored: torch.Tensor) -> None:
-        """The sweep is now before a block whose stored input is ``stored``."""
-        self.state = stored
-        self.owned = False
+    def work_buffer(self) -> torch.Tensor:
+        if self.work is None:
+            self.work = torch.empty_like(self.state)
+        return self.work
 
 
 class CircuitFunction(torch.autograd.Function):

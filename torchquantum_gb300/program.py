@@ -334,31 +334,38 @@ class Segment:
             _lib.nvtx_pop()
 
     def _apply(self, buf: torch.Tensor, store_inputs: bool, zero_input: bool) -> torch.Tensor:
+        recs, keep = [], []
+        cur = buf
         for i, op in enumerate(self.exec_ops):
             if isinstance(op, StagedRun):
-                _lib.staged_apply(buf, self.n, op.descs(), op.tile_bits)
+                recs.append(_staged_record(op, op.descs(), keep))
             elif getattr(op, "members", None) is not None:
+                if not op.tc:
+                    recs.append(_exec(_lib.X_BLOCK_DENSE, op.wires, batch=op.block_batch, operand=op.operand))
+                    continue
+                r = _exec(_lib.X_BLOCK_TC, op.wires, batch=op.block_batch, image=op.image)
                 out = None
-                if op.tc and zero_input and i == 0:
+                if zero_input and i == 0:
                     # a first block on |0...0>: its reverse step needs neither its input nor
                     # the cotangent before it (nothing precedes it), so nothing is kept
                     op.zero_input = True
-                elif op.tc and store_inputs:
-                    out = _new_state(buf)
+                elif store_inputs:
+                    out = _new_state(cur)
                     if out is None:  # out of memory: the remaining blocks run in place
                         store_inputs = False
                 if out is not None:
-                    _lib.fused_apply_to(buf, out, self.n, op.wires, op.image, op.block_batch)
-                    op.stored_input = buf
+                    r.out = out.data_ptr()
+                    op.stored_input = cur
                     op.kept_input = True
-                    buf = out
-                elif op.tc:
-                    _lib.fused_apply(buf, self.n, op.wires, op.image, op.block_batch)
-                else:
-                    _lib.apply_matrix(buf, self.n, op.wires, op.operand, op.block_batch)
+                    cur = out
+                recs.append(r)
             else:
-                engine.apply_op(buf, self.n, op)
-        return buf
+                recs.append(_plain_record(op))
+        if recs:
+            table = (_lib.ExecOp * len(recs))(*recs)
+            final = _lib.segment_forward(buf, self.n, table, len(recs))
+            assert final == cur.data_ptr(), "segment runner ended on an unexpected buffer"
+        return cur
 
     def take_stored_inputs(self) -> list:
         """(block, stored input) pairs for an autograd node to save; the segment keeps weak
@@ -414,8 +421,9 @@ class Segment:
             for b in tc_grad:
                 mr_of[id(b)] = mr_all[row:row + b.block_batch]
                 row += b.block_batch
-        cross_jobs = []
-        for op in reversed(self.exec_ops):
+        cross_jobs, recs, keep, stored_at = [], [], [], {}
+        zero_block = None
+        for op in self.exec_ops:  # forward order; the runner walks it backwards
             if isinstance(op, StagedRun):
                 slots = []
                 for m in op.ops:
@@ -426,34 +434,33 @@ class Segment:
                         elif id(m) in gslots:
                             slot = torch.view_as_real(gslots[id(m)]).view(-1)
                     slots.append(slot)
-                _lib.staged_adjoint(psi.writable(), lam, n, op.descs(slots), op.tile_bits)
+                recs.append(_staged_record(op, op.descs(slots), keep))
                 continue
             if getattr(op, "members", None) is not None:
                 slot = None
                 if gu is not None and _block_needs_grad(op):
                     slot = _as_real(gu, op.u128, self.u128)
-                stored = inputs.get(id(op)) if op.tc else None
-                mr = mr_of.get(id(op)) if slot is not None else None
-                if op.tc and getattr(op, "zero_input", False):
-                    # the last reverse step of the circuit, from |0...0>: the cotangent of U
-                    # is lam conj(e_0)^T -- lam at the block's 64 patterns with every other
-                    # bit clear, in column 0; lam and psi are not needed any further
-                    if slot is not None:
-                        _add_zero_input_cotangent(lam, op, slot, n)
+                if not op.tc:
+                    recs.append(_exec(_lib.X_BLOCK_DENSE, op.wires, batch=op.block_batch, operand=op.operand,
+                                      grad=slot))
                     continue
-                if stored is not None:
-                    _lib.fused_adjoint_stored(stored, lam, n, op.wires, op.image_h, op.block_batch, mr)
+                stored = inputs.get(id(op))
+                mr = mr_of.get(id(op)) if slot is not None else None
+                r = _exec(_lib.X_BLOCK_TC, op.wires, batch=op.block_batch, image_h=op.image_h, u=op.u128, grad=slot,
+                          mr=mr)
+                if getattr(op, "zero_input", False):
+                    # the last reverse step of the circuit, from |0...0>: the runner stops
+                    # before it; the cotangent of U is lam conj(e_0)^T (taken below)
+                    r.skip_reverse = 1
+                    zero_block = (op, slot)
+                elif stored is not None:
+                    r.stored = stored.data_ptr()
+                    stored_at[stored.data_ptr()] = stored
                     if mr is not None:  # the cross term against the stored input is the cotangent
                         j = _lib.CrossJob()
                         j.mr, j.gu, j.batch = mr.data_ptr(), slot.data_ptr(), op.block_batch
                         cross_jobs.append(j)
-                    psi.jump(stored)
-                elif op.tc:
-                    _lib.fused_adjoint(psi.writable(), lam, n, op.wires, op.image_h, op.block_batch, mr)
-                    if mr is not None:  # M U (float32 product, float64 sum)
-                        _lib.fused_cross_grad(mr, engine.kernel_operand(op.u128), slot)
-                else:
-                    _lib.adjoint_matrix(psi.writable(), lam, n, op.wires, op.operand, op.block_batch, slot)
+                recs.append(r)
                 continue
             slot = None
             if need_grads:
@@ -461,7 +468,20 @@ class Segment:
                     slot = _as_real(opg, op.op128, self.op128)
                 elif id(op) in gslots:
                     slot = torch.view_as_real(gslots[id(op)]).view(-1)
-            engine.adjoint_op(psi.writable(), lam, n, op, slot)
+            recs.append(_plain_record(op, slot))
+        if recs:
+            # the sweep writes its state only on a work buffer: the cursor's own when it
+            # already owns one, else one state more, when any reverse step uncomputes
+            uncomputes = any(not (r.kind == _lib.X_BLOCK_TC and (r.stored or r.skip_reverse)) for r in recs)
+            work = psi.state if psi.owned else (psi.work_buffer() if uncomputes else None)
+            table = (_lib.ExecOp * len(recs))(*recs)
+            start = _lib.segment_backward(psi.state, lam, work, n, table, len(recs))
+            if work is not None and start == work.data_ptr():
+                psi.state, psi.owned = work, True
+            elif start in stored_at:
+                psi.state, psi.owned = stored_at[start], False
+        if zero_block is not None and zero_block[1] is not None:
+            _add_zero_input_cotangent(lam, zero_block[0], zero_block[1], n)
         if cross_jobs:
             table, host = _to_device_table(cross_jobs, dev)
             self._keep_cross = (table, host)  # the cross terms themselves are stream-ordered
@@ -519,6 +539,46 @@ class Segment:
         for op in self.generic_sources:
             grads.append(gslots[id(op)].to(op.source.dtype).view(op.source.shape))
         return grads
+
+
+_PLAIN_KIND = {engine.KIND_DENSE: _lib.X_DENSE, engine.KIND_CTRL: _lib.X_CTRL, engine.KIND_X: _lib.X_MCX,
+               engine.KIND_PHASE: _lib.X_PHASE, engine.KIND_DIAG: _lib.X_DIAG, engine.KIND_SWAP: _lib.X_SWAP}
+
+
+def _exec(kind: int, wires, nctrl: int = 0, ctrl_val: int = 1, batch: int = 1, operand=None, uncompute=None,
+          image=None, image_h=None, u=None, grad=None, mr=None) -> "_lib.ExecOp":
+    """One ``tqk_exec_op`` record (tensors by their device address)."""
+    r = _lib.ExecOp()
+    r.kind, r.nw, r.nctrl, r.ctrl_val, r.batch = kind, len(wires), nctrl, ctrl_val, batch
+    if len(wires) > len(r.wires):
+        raise _lib.TQKError(1, f"an op on {len(wires)} wires exceeds the {len(r.wires)} one op may touch")
+    for j, w in enumerate(wires):
+        r.wires[j] = w
+    for name, t in (("operand", operand), ("uncompute", uncompute), ("image", image), ("image_h", image_h),
+                    ("u", u), ("grad", grad), ("mr", mr)):
+        if t is not None:
+            setattr(r, name, t.data_ptr())
+    return r
+
+
+def _plain_record(op, grad=None) -> "_lib.ExecOp":
+    """A plain tape op (engine.TapeOp) as a ``tqk_exec_op``: wires are controls first,
+    then targets, for the controlled kinds."""
+    k = op.kind
+    if k in (engine.KIND_CTRL, engine.KIND_X, engine.KIND_SWAP):
+        wires, nctrl = op.controls + op.targets, len(op.controls)
+    else:
+        wires, nctrl = op.wires, 0
+    return _exec(_PLAIN_KIND[k], wires, nctrl=nctrl, ctrl_val=op.ctrl_val, batch=op.batch, operand=op.operand,
+                 uncompute=op.uncompute, grad=grad)
+
+
+def _staged_record(run, descs, keep: list) -> "_lib.ExecOp":
+    arr = (_lib.StagedOp * len(descs))(*descs)
+    keep.append(arr)  # alive until the runner returns (it reads the table on the host)
+    r = _lib.ExecOp()
+    r.kind, r.staged, r.nstaged, r.tile_bits = _lib.X_STAGED, ctypes.addressof(arr), len(descs), run.tile_bits
+    return r
 
 
 def _add_zero_input_cotangent(lam: torch.Tensor, blk, slot: torch.Tensor, n: int) -> None:
