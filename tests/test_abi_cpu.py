@@ -93,3 +93,29 @@ def test_product_refuses_cpu_device():
 
     with pytest.raises(RuntimeError, match="CUDA devices only"):
         tq.QuantumDevice(n_wires=2, device="cpu")
+
+
+def test_segment_entry_points_marshal_without_launching(lib):
+    """The tape-level entry points through ctypes with an empty table: arguments marshal
+    (NULL hook included) and nothing is launched; a bad table is rejected on the host."""
+    import ctypes
+
+    final = ctypes.c_void_p()
+    count = ctypes.c_int64(-1)
+    rc = lib.tqk_segment_forward(16, 1, 4, None, 0, 16, ctypes.byref(final), ctypes.byref(count), _lib.EXEC_HOOK(),
+                                 None, None)
+    assert rc == 0 and final.value == 16 and count.value == 0
+    start = ctypes.c_void_p()
+    rc = lib.tqk_segment_backward(16, 32, None, 1, 4, None, 0, 16, ctypes.byref(start), ctypes.byref(count),
+                                  _lib.EXEC_HOOK(), None, None)
+    assert rc == 0 and start.value == 16
+    bad = (_lib.ExecOp * 1)()
+    bad[0].kind = 99
+    rc = lib.tqk_segment_forward(16, 1, 4, bad, 1, 16, ctypes.byref(final), None, _lib.EXEC_HOOK(), None, None)
+    assert rc == 2 and b"unknown kind" in lib.tqk_last_error()
+    called = []
+    hook = _lib.EXEC_HOOK(lambda i, kind, after, user: called.append((i, kind, after)))
+    two = (_lib.ExecOp * 2)()
+    two[1].skip_reverse = 1
+    rc = lib.tqk_segment_backward(16, 32, None, 1, 4, two, 2, 16, None, None, hook, None, None)
+    assert rc == 2 and b"only op 0" in lib.tqk_last_error() and called == []

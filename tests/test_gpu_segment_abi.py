@@ -13,7 +13,6 @@ exec tables and buffers owned by the test.
 """
 import ctypes
 
-import numpy as np
 import pytest
 import torch
 
@@ -42,11 +41,6 @@ def _compile(method, n=16, bsz=2):
     return q, q._tape[0], final
 
 
-def _slot(t, keep):
-    keep.append(t)
-    return t
-
-
 def _replay(sg, n, bsz):
     """Forward through tqk_segment_forward from |0...0> with the test's own block output
     buffers; returns (final state, [(op, stored input)])."""
@@ -72,7 +66,8 @@ def _replay(sg, n, bsz):
     table = (_lib.ExecOp * len(recs))(*recs)
     final = ctypes.c_void_p()
     rc = lib.tqk_segment_forward(state.data_ptr(), bsz, n, table, len(recs), _lib.status_word("cuda").data_ptr(),
-                                 ctypes.byref(final), None, None, None, torch.cuda.current_stream().cuda_stream)
+                                 ctypes.byref(final), None, _lib.EXEC_HOOK(), None,
+                                 torch.cuda.current_stream().cuda_stream)
     assert rc == 0, lib.tqk_last_error().decode()
     assert final.value == cur.data_ptr()
     return cur, dict((id(op), t) for op, t in stored)
@@ -120,8 +115,8 @@ def _backward_tape_level(sg, final, lam, stored, n):
     start = ctypes.c_void_p()
     lib = _lib.load()
     rc = lib.tqk_segment_backward(final.data_ptr(), lam.data_ptr(), work.data_ptr(), lam.shape[0], n, table,
-                                  len(recs), _lib.status_word("cuda").data_ptr(), ctypes.byref(start), None, None,
-                                  None, torch.cuda.current_stream().cuda_stream)
+                                  len(recs), _lib.status_word("cuda").data_ptr(), ctypes.byref(start), None,
+                                  _lib.EXEC_HOOK(), None, torch.cuda.current_stream().cuda_stream)
     assert rc == 0, lib.tqk_last_error().decode()
     return g, mr
 

@@ -362,5 +362,32 @@ def test_coset_expvals_and_seed_match_the_oracle(n, m, seed):
                     seed_out[g[u]] += coef[j] * (-1) ** (pb ^ (ny & 1) ^ (ny >> 1)) * term
     want = np.array([O.expval_pauli(psi[None], p, n)[0] for p in strings])
     assert np.abs(ev - want).max() < 1e-9
+    # the expval kernel's halved rule: per pair (u, u + 1) of stage coordinates, a string
+    # with xs = 0 adds both |psi|^2 terms, xs = 1 adds twice the u-side term, any other xs
+    # adds twice both terms when bit hb (the highest of xs) of u is clear, else nothing
+    half = np.zeros(m)
+    for group, c, r in _lib.coset_groups(xs, n):
+        model, _ = _coset_model(n, xs, zs, group, c)
+        for gidx, consts, rho in model:
+            stage = psi[np.array(gidx)]
+            for s, j in enumerate(group):
+                xsu, gam, _ = consts[s]
+                ny = bin(xs[j] & zs[j]).count("1") & 3
+                hb = xsu.bit_length() - 1
+                for u in range(0, len(gidx), 2):
+                    pb = rho[s] ^ (bin(u & gam).count("1") & 1)
+                    sgn0 = (-1) ** (pb ^ (ny >> 1))
+                    sgn1 = sgn0 * (-1 if gam & 1 else 1)
+                    if xsu == 0:
+                        half[j] += sgn0 * abs(stage[u]) ** 2 + sgn1 * abs(stage[u + 1]) ** 2
+                    elif xsu == 1:
+                        w0 = np.conj(stage[u]) * stage[u + 1]
+                        half[j] += 2 * sgn0 * (w0.imag if ny & 1 else w0.real)
+                    elif not (u >> hb) & 1:
+                        w0 = np.conj(stage[u]) * stage[u ^ xsu]
+                        w1 = np.conj(stage[u + 1]) * stage[(u + 1) ^ xsu]
+                        part = (w0.imag, w1.imag) if ny & 1 else (w0.real, w1.real)
+                        half[j] += 2 * (sgn0 * part[0] + sgn1 * part[1])
+    assert np.abs(half - want).max() < 1e-9
     want_seed = sum(cj * O.apply_pauli(psi[None], p, n)[0] for cj, p in zip(coef, strings))
     assert np.abs(seed_out - want_seed).max() < 1e-9

@@ -369,7 +369,7 @@ SEGMENT_HOOKS = {"forward": None, "backward": None}
 def _hook(which, table):
     fn = SEGMENT_HOOKS[which]
     if fn is None:
-        return None
+        return EXEC_HOOK()  # a NULL function pointer
     return EXEC_HOOK(lambda i, kind, after, user: fn(table[i], after))
 
 

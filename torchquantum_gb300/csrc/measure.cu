@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* 
 // has 2^(n - T) cosets.
 //
 // CTA: one producer warp (bulk copies of a stage's chunks completing on the stage's full
-// mbarrier) and twelve consumer warps; three stages in flight.  Expvals: each consumer
+// mbarrier) and fifteen consumer warps; three stages in flight.  Expvals: each consumer
 // thread accumulates Re(conj(psi_u) (P_s psi)_u) in float32 over its amplitudes of the
 // coset, the CTA reduces in float64 and writes one partial per (coset, string); the
 // partials are summed per row in a fixed order (k_expval_finish).  Backward seed: each
@@ -266,7 +266,7 @@ constexpr int kCosetTileBits = 13;
 constexpr int kCosetMinChunkBits = 4;
 constexpr int kCosetMaxRank = kCosetTileBits - kCosetMinChunkBits;
 constexpr int kCosetStages = 3;
-constexpr int kCosetConsumerWarps = 12;
+constexpr int kCosetConsumerWarps = 15;
 constexpr int kCosetConsumers = 32 * kCosetConsumerWarps;
 constexpr int kCosetThreads = kCosetConsumers + 32;
 
@@ -284,6 +284,8 @@ struct CosetParams {
   uint32_t xs[kMaxStringsPerPass], gam[kMaxStringsPerPass], zh[kMaxStringsPerPass];
   uint32_t fl[kMaxStringsPerPass];   // constant sign bit (expvals: ny >> 1; seed: (ny & 1) ^ (ny >> 1))
   uint32_t odd[kMaxStringsPerPass];  // ny & 1
+  uint32_t kind[kMaxStringsPerPass]; // expvals: 0 diagonal (xs = 0), 1 xs = 1, 2 other, 3 padding
+  uint32_t hb[kMaxStringsPerPass];   // expvals, kind 2: highest set bit of xs
   int col[kMaxStringsPerPass];
 };
 
@@ -325,7 +327,7 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
   __syncthreads();
   const int64_t total = p.bsz * p.cosets;
   volatile int* vquit = &quit;
-  int issued[kCosetStages] = {0, 0, 0};  // producer: loads issued per stage
+  int last_issued = -1;  // producer: the last pipeline iteration whose loads it issued
   if (warp == kCosetConsumerWarps) {
     // ---------------- producer
     const uint32_t chunk_bytes = 8u << p.c;
@@ -358,17 +360,19 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
       for (int a = lane; a < nslots; a += 32)
         bulk::bulk_load(dst + (static_cast<size_t>(a) << p.c), row + (static_cast<uint64_t>(slot_h[st][a]) << p.c),
                         chunk_bytes, &full[st]);
-      issued[st]++;
+      last_issued = it;
     }
   } else {
     // ---------------- consumers
     const int ct = threadIdx.x;
-    uint32_t xs[NS], gam[NS], odd[NS];
+    uint32_t xs[NS], gam[NS], odd[NS], kind[NS], hb[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
       xs[s] = s < p.ns ? p.xs[s] : 0u;
       gam[s] = s < p.ns ? p.gam[s] : 0u;
       odd[s] = s < p.ns ? p.odd[s] : 0u;
+      kind[s] = s < p.ns ? p.kind[s] : 3u;
+      hb[s] = s < p.ns ? p.hb[s] : 0u;
     }
     const uint32_t lmask = (1u << p.c) - 1u;
     int it = 0;
@@ -396,7 +400,7 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
       float acc[NS];
 #pragma unroll
       for (int s = 0; s < NS; ++s) acc[s] = 0.f;
-      if (ok) {
+      if (ok && SEED) {
         // strings s >= ns are padding (partner = the pair itself, weight 0): every
         // string's partner load is issued before any arithmetic, with no branch between
         for (uint32_t q = ct; q < (tile >> 1); q += kCosetConsumers) {
@@ -404,32 +408,64 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
           float4 w[NS];
 #pragma unroll
           for (int s = 0; s < NS; ++s) w[s] = lds4(stg + ((u ^ xs[s]) & ~1u));
-          float2 a0 = make_float2(0.f, 0.f), a1 = a0;
-          if (!SEED) {
-            const float4 v = lds4(stg + u);
-            a0 = lo2(v);
-            a1 = hi2(v);
-          }
           float2 o0 = make_float2(0.f, 0.f), o1 = o0;
 #pragma unroll
           for (int s = 0; s < NS; ++s) {
             const bool sw = (xs[s] & 1u) != 0;
             const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
             const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
-            if (SEED) {
-              const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);
-              if (odd[s]) {
-                o0.x = fmaf(-c0, b0.y, o0.x);
-                o0.y = fmaf(c0, b0.x, o0.y);
-                o1.x = fmaf(-c1, b1.y, o1.x);
-                o1.y = fmaf(c1, b1.x, o1.y);
-              } else {
-                o0.x = fmaf(c0, b0.x, o0.x);
-                o0.y = fmaf(c0, b0.y, o0.y);
-                o1.x = fmaf(c1, b1.x, o1.x);
-                o1.y = fmaf(c1, b1.y, o1.y);
-              }
+            const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);
+            if (odd[s]) {
+              o0.x = fmaf(-c0, b0.y, o0.x);
+              o0.y = fmaf(c0, b0.x, o0.y);
+              o1.x = fmaf(-c1, b1.y, o1.x);
+              o1.y = fmaf(c1, b1.x, o1.y);
             } else {
+              o0.x = fmaf(c0, b0.x, o0.x);
+              o0.y = fmaf(c0, b0.y, o0.y);
+              o1.x = fmaf(c1, b1.x, o1.x);
+              o1.y = fmaf(c1, b1.y, o1.y);
+            }
+          }
+          float2* dst = p.out + (static_cast<uint64_t>(b) << p.n) +
+                        (static_cast<uint64_t>(slot_h[st][u >> p.c]) << p.c) + (u & lmask);
+          if (p.accumulate) {
+            const float4 old = ld4(dst);
+            o0.x += old.x;
+            o0.y += old.y;
+            o1.x += old.z;
+            o1.y += old.w;
+          }
+          st4(dst, pack4(o0, o1));
+        }
+      } else if (ok) {
+        // expvals: a pair of amplitudes (u, u ^ xs) is visited once, from the side whose
+        // bit hb (the highest of xs) is clear, and counted twice (P is Hermitian, so both
+        // sides contribute the same real part); for hb >= 6 the whole warp takes or skips
+        // a string together.  xs = 0: |psi|^2 terms; xs = 1: the partner is the pair's
+        // other amplitude.  Partner loads are issued before the arithmetic.
+        for (uint32_t q = ct; q < (tile >> 1); q += kCosetConsumers) {
+          const uint32_t u = q << 1;
+          const float4 v = lds4(stg + u);
+          const float2 a0 = lo2(v), a1 = hi2(v);
+          float4 w[NS];
+#pragma unroll
+          for (int s = 0; s < NS; ++s) {
+            const bool take = kind[s] == 2u && ((u >> hb[s]) & 1u) == 0u;
+            w[s] = take ? lds4(stg + ((u ^ xs[s]) & ~1u)) : v;
+          }
+#pragma unroll
+          for (int s = 0; s < NS; ++s) {
+            const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
+            if (kind[s] == 0u) {
+              const float p0 = a0.x * a0.x + a0.y * a0.y, p1 = a1.x * a1.x + a1.y * a1.y;
+              acc[s] += flip_if_odd(p0 + flip_if_odd(p1, gam[s] & 1u), pb);
+            } else if (kind[s] == 1u) {
+              const float c0 = odd[s] ? a0.x * a1.y - a0.y * a1.x : a0.x * a1.x + a0.y * a1.y;
+              acc[s] += 2.f * flip_if_odd(c0, pb);
+            } else if (kind[s] == 2u && ((u >> hb[s]) & 1u) == 0u) {
+              const bool sw = (xs[s] & 1u) != 0;
+              const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
               float c0, c1;
               if (odd[s]) {
                 c0 = a0.x * b0.y - a0.y * b0.x;
@@ -438,20 +474,8 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
                 c0 = a0.x * b0.x + a0.y * b0.y;
                 c1 = a1.x * b1.x + a1.y * b1.y;
               }
-              acc[s] += flip_if_odd(c0 + flip_if_odd(c1, gam[s] & 1u), pb);
+              acc[s] += 2.f * flip_if_odd(c0 + flip_if_odd(c1, gam[s] & 1u), pb);
             }
-          }
-          if (SEED) {
-            float2* dst = p.out + (static_cast<uint64_t>(b) << p.n) +
-                          (static_cast<uint64_t>(slot_h[st][u >> p.c]) << p.c) + (u & lmask);
-            if (p.accumulate) {
-              const float4 old = ld4(dst);
-              o0.x += old.x;
-              o0.y += old.y;
-              o1.x += old.z;
-              o1.y += old.w;
-            }
-            st4(dst, pack4(o0, o1));
           }
         }
       }
@@ -479,8 +503,10 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
   __syncthreads();
   // after a timeout, wait (bounded) for this CTA's copies still in flight before exiting
   if (quit && warp == kCosetConsumerWarps && lane == 0) {
-    for (int st = 0; st < kCosetStages; ++st)
-      if (issued[st] > 0) bulk::mbar_wait(&full[st], static_cast<uint32_t>(issued[st] - 1) & 1u);
+    for (int st = 0; st < kCosetStages; ++st) {
+      const int last = last_issued - ((last_issued - st) % kCosetStages + kCosetStages) % kCosetStages;
+      if (last >= 0) bulk::mbar_wait(&full[st], static_cast<uint32_t>(last / kCosetStages) & 1u);
+    }
   }
 }
 
@@ -576,7 +602,8 @@ static void coset_params(const CosetGroup& g, int n, const uint64_t* xmask, cons
   const uint32_t lmask = (1u << g.c) - 1u;
   for (int s = 0; s < kMaxStringsPerPass; ++s) {
     if (s >= g.ns) {
-      p.xs[s] = p.gam[s] = p.zh[s] = p.fl[s] = p.odd[s] = 0u;
+      p.xs[s] = p.gam[s] = p.zh[s] = p.fl[s] = p.odd[s] = p.hb[s] = 0u;
+      p.kind[s] = 3u;
       p.col[s] = 0;
       continue;
     }
@@ -593,6 +620,8 @@ static void coset_params(const CosetGroup& g, int n, const uint64_t* xmask, cons
     p.zh[s] = zh;
     p.odd[s] = static_cast<uint32_t>(ny & 1);
     p.fl[s] = seed ? static_cast<uint32_t>((ny & 1) ^ (ny >> 1)) : static_cast<uint32_t>(ny >> 1);
+    p.kind[s] = p.xs[s] == 0u ? 0u : (p.xs[s] == 1u ? 1u : 2u);
+    p.hb[s] = p.xs[s] == 0u ? 0u : static_cast<uint32_t>(31 - __builtin_clz(p.xs[s]));
     p.col[s] = j;
   }
 }
