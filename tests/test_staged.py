@@ -143,37 +143,31 @@ def test_staged_abi_rejects_target_outside_tile():
         _lib.staged_apply(psi, n, [d], 13)
 
 
-def _cell_index(bits, c):
-    """Host model of staged.cu's cell_index: c with zeros inserted at the (ascending) cell
-    bits, then every combination r of the cell bits (bit d of r sets cell bit d)."""
-    base = c
-    for q in bits:
-        base = ((base >> q) << (q + 1)) | (base & ((1 << q) - 1))
-    return [base | sum(1 << bits[d] for d in range(len(bits)) if (r >> d) & 1) for r in range(1 << len(bits))]
+def _pair_base(q, lb):
+    """Host model of staged.cu's pair_base (index of the first pair of pair-pair q)."""
+    if lb == 0:
+        return q << 1
+    lowm = (1 << (lb - 1)) - 1
+    return ((q >> (lb - 1)) << (lb + 1)) | ((q & lowm) << 1)
 
 
 @pytest.mark.parametrize("m", [1, 2, 3, 5, 8, 12])
-def test_staged_cells_cover_the_tile_and_hold_every_pair(m):
-    """A sweep's cells (2^nd amplitudes spanned by its nd = min(3, m) cell bits) cover every
-    index of a 2^m tile exactly once; every pair (i, i | 2^q) along a cell bit q lies in one
-    cell at combinations (r, r | 2^d); cells with bit 0 start their pairs (r, r + 1) at even,
-    16-byte-aligned indices (checked on the CPU before any launch)."""
-    import itertools
-
-    rng = np.random.default_rng(m)
-    nd = min(3, m)
-    for _ in range(6):
-        bits = sorted(int(b) for b in rng.choice(m, size=nd, replace=False))
-        seen = np.zeros(1 << m, dtype=int)
-        for c in range(1 << (m - nd)):
-            idx = _cell_index(bits, c)
-            for i in idx:
-                seen[i] += 1
-            for d, q in enumerate(bits):
-                for r in range(1 << nd):
-                    if not (r >> d) & 1:
-                        assert idx[r | (1 << d)] == idx[r] | (1 << q) and not (idx[r] >> q) & 1
-            if bits[0] == 0:
-                assert all(idx[r] % 2 == 0 and idx[r + 1] == idx[r] + 1 for r in range(0, 1 << nd, 2))
-        assert (seen == 1).all()
-    assert list(itertools.chain(_cell_index([0, 1, 2], 0))) == list(range(8))
+def test_staged_pair_indexing_covers_every_pair_once(m):
+    """The staged kernels visit, for a target bit lb of a 2^m tile, every amplitude pair
+    (i, i | 2^lb) with bit lb of i clear exactly once, through 16-byte-aligned float4
+    accesses inside the tile (checked on the CPU before any launch)."""
+    tsz = 1 << m
+    for lb in range(m):
+        nq = tsz >> 1 if lb == 0 else tsz >> 2
+        seen = []
+        for q in range(nq):
+            i0 = _pair_base(q, lb)
+            assert i0 % 2 == 0 and (i0 >> lb) & 1 == 0
+            if lb == 0:
+                seen.append((i0, i0 + 1))
+            else:
+                i1 = i0 | (1 << lb)
+                assert i1 < tsz and i1 % 2 == 0
+                seen += [(i0, i1), (i0 + 1, i1 + 1)]
+        want = [(i, i | (1 << lb)) for i in range(tsz) if not (i >> lb) & 1]
+        assert sorted(seen) == want

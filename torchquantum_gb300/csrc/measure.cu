@@ -306,6 +306,57 @@ __device__ __forceinline__ uint32_t coset_rep(uint32_t t, const CosetParams& p) 
   return t;
 }
 
+// One string's sum over a staged coset, each amplitude pair (u, u + 1) with bit h of u
+// clear (npairs = pairs to visit) against its partner pair ((u ^ x) & ~1); SW: x is odd, so
+// the partner pair is in swapped order; ODD: odd number of Y factors (imaginary part).
+// Returns the thread's float32 partial of the half sum.
+template <bool SW, bool ODD>
+__device__ __forceinline__ float coset_string_sum(const float2* stg, uint32_t npairs, uint32_t h, uint32_t x,
+                                                  uint32_t gam, uint32_t rho, int ct) {
+  const uint32_t lo = (1u << h) - 1u;
+  const uint32_t g1 = gam & 1u;
+  float a = 0.f;
+#pragma unroll 2
+  for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
+    const uint32_t v2 = j << 1;
+    const uint32_t u = ((v2 >> h) << (h + 1)) | (v2 & lo);
+    const float4 v = lds4(stg + u);
+    const float4 w = lds4(stg + ((u ^ x) & ~1u));
+    const float2 a0 = lo2(v), a1 = hi2(v);
+    const float2 b0 = SW ? hi2(w) : lo2(w), b1 = SW ? lo2(w) : hi2(w);
+    const float c0 = ODD ? a0.x * b0.y - a0.y * b0.x : a0.x * b0.x + a0.y * b0.y;
+    const float c1 = ODD ? a1.x * b1.y - a1.y * b1.x : a1.x * b1.x + a1.y * b1.y;
+    a += flip_if_odd(c0 + flip_if_odd(c1, g1), static_cast<uint32_t>(__popc(u & gam)) + rho);
+  }
+  return a;
+}
+
+// Diagonal string (x = 0): sum of +-|psi_u|^2 over every pair of the coset.
+__device__ __forceinline__ float coset_diag_sum(const float2* stg, uint32_t npairs, uint32_t gam, uint32_t rho, int ct) {
+  const uint32_t g1 = gam & 1u;
+  float a = 0.f;
+  for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
+    const uint32_t u = j << 1;
+    const float4 v = lds4(stg + u);
+    const float p0 = v.x * v.x + v.y * v.y, p1 = v.z * v.z + v.w * v.w;
+    a += flip_if_odd(p0 + flip_if_odd(p1, g1), static_cast<uint32_t>(__popc(u & gam)) + rho);
+  }
+  return a;
+}
+
+// x = 1: each pair (u, u + 1) is its own partner; the u-side term (counted twice by the caller).
+__device__ __forceinline__ float coset_x1_sum(const float2* stg, uint32_t npairs, bool odd, uint32_t gam, uint32_t rho,
+                                              int ct) {
+  float a = 0.f;
+  for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
+    const uint32_t u = j << 1;
+    const float4 v = lds4(stg + u);
+    const float c0 = odd ? v.x * v.w - v.y * v.z : v.x * v.z + v.y * v.w;
+    a += flip_if_odd(c0, static_cast<uint32_t>(__popc(u & gam)) + rho);
+  }
+  return a;
+}
+
 template <bool SEED, int NS>
 __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p) {
   extern __shared__ __align__(128) unsigned char coset_smem[];
@@ -439,44 +490,24 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
           st4(dst, pack4(o0, o1));
         }
       } else if (ok) {
-        // expvals: a pair of amplitudes (u, u ^ xs) is visited once, from the side whose
-        // bit hb (the highest of xs) is clear, and counted twice (P is Hermitian, so both
-        // sides contribute the same real part); for hb >= 6 the whole warp takes or skips
-        // a string together.  xs = 0: |psi|^2 terms; xs = 1: the partner is the pair's
-        // other amplitude.  Partner loads are issued before the arithmetic.
-        for (uint32_t q = ct; q < (tile >> 1); q += kCosetConsumers) {
-          const uint32_t u = q << 1;
-          const float4 v = lds4(stg + u);
-          const float2 a0 = lo2(v), a1 = hi2(v);
-          float4 w[NS];
+        // expvals, one string at a time (its orientation and Y parity fixed for the loop):
+        // a pair of amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the
+        // side whose bit hb (the highest of xs) is clear -- enumerated directly by inserting
+        // a zero at hb -- and counted twice (P is Hermitian: both sides contribute the same
+        // real part).  xs = 0: |psi|^2 terms; xs = 1: the partner is the pair's other amplitude.
 #pragma unroll
-          for (int s = 0; s < NS; ++s) {
-            const bool take = kind[s] == 2u && ((u >> hb[s]) & 1u) == 0u;
-            w[s] = take ? lds4(stg + ((u ^ xs[s]) & ~1u)) : v;
-          }
-#pragma unroll
-          for (int s = 0; s < NS; ++s) {
-            const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
-            if (kind[s] == 0u) {
-              const float p0 = a0.x * a0.x + a0.y * a0.y, p1 = a1.x * a1.x + a1.y * a1.y;
-              acc[s] += flip_if_odd(p0 + flip_if_odd(p1, gam[s] & 1u), pb);
-            } else if (kind[s] == 1u) {
-              const float c0 = odd[s] ? a0.x * a1.y - a0.y * a1.x : a0.x * a1.x + a0.y * a1.y;
-              acc[s] += 2.f * flip_if_odd(c0, pb);
-            } else if (kind[s] == 2u && ((u >> hb[s]) & 1u) == 0u) {
-              const bool sw = (xs[s] & 1u) != 0;
-              const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
-              float c0, c1;
-              if (odd[s]) {
-                c0 = a0.x * b0.y - a0.y * b0.x;
-                c1 = a1.x * b1.y - a1.y * b1.x;
-              } else {
-                c0 = a0.x * b0.x + a0.y * b0.y;
-                c1 = a1.x * b1.x + a1.y * b1.y;
-              }
-              acc[s] += 2.f * flip_if_odd(c0 + flip_if_odd(c1, gam[s] & 1u), pb);
-            }
-          }
+        for (int s = 0; s < NS; ++s) {
+          if (kind[s] == 3u) continue;  // padding
+          float a;
+          if (kind[s] == 0u) a = coset_diag_sum(stg, tile >> 1, gam[s], rho[s], ct);
+          else if (kind[s] == 1u) a = 2.f * coset_x1_sum(stg, tile >> 1, odd[s] != 0u, gam[s], rho[s], ct);
+          else if (xs[s] & 1u)
+            a = 2.f * (odd[s] ? coset_string_sum<true, true>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
+                              : coset_string_sum<true, false>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
+          else
+            a = 2.f * (odd[s] ? coset_string_sum<false, true>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
+                              : coset_string_sum<false, false>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
+          acc[s] = a;
         }
       }
       __syncwarp();

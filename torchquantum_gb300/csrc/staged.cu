@@ -8,20 +8,14 @@
 // the tile back.  Controls and the wires of diagonal ops may be anywhere: they are read
 // from the amplitude's global index (tile base | local index).
 //
-// Inside a tile the run is applied in sweeps: up to 3 consecutive ops whose target bits
-// number at most 3 (phase and diagonal ops join any sweep) act on cells of 8 amplitudes
-// (the sweep's 3 cell bits in every combination) that one thread holds in registers, so
-// the tile crosses shared memory once per sweep instead of once per op.
-//
 // Tiles are contiguous, so one thread moves each with the bulk-copy engine (TMA:
 // cp.async.bulk into shared memory on an mbarrier, cp.async.bulk back to HBM); the wait
 // for a load is bounded and reports TQK_TIMEOUT through the caller's status word.
 //
-// The adjoint pass holds the psi and lam tiles of the same amplitudes and walks the
-// sweeps (and each sweep's ops) in reverse: psi <- U^H psi, lam <- U^H lam and, for ops
-// with a cotangent slot, sum lam_in conj(psi_out) accumulated per op in registers over a
-// thread's cells, then per sweep over the CTA (warp shuffles, float64 in shared memory
-// across every tile the CTA handles; one atomic per value per CTA at the end).
+// The adjoint pass holds the psi and lam tiles of the same amplitudes and walks the run
+// in reverse: psi <- U^H psi, lam <- U^H lam and, for ops with a cotangent slot,
+// sum lam_in conj(psi_out) accumulated per op (warp shuffles, then float64 in shared
+// memory across every tile the CTA handles; one atomic per value per CTA at the end).
 #include <stdint.h>
 
 #include "bulk.cuh"
@@ -49,17 +43,6 @@ __device__ __forceinline__ bool load_tile(uint64_t* bar, uint32_t use, int nreg,
   return false;
 }
 
-// Consecutive ops applied in one shared-memory sweep: every op's target bit is one of the
-// sweep's cell bits, so the ops act inside cells of 2^nd amplitudes (the cell bits set in
-// every combination) that one thread holds in registers.
-constexpr int kMaxSweepOps = 3;   // the adjoint keeps one cotangent accumulator set per op
-constexpr int kCellDims = 3;      // cells of up to 8 amplitudes
-struct Sweep {
-  int32_t first, count;  // ops [first, first + count)
-  int32_t nd;            // cell dimensions: min(3, tile bits)
-  int32_t bits[kCellDims];  // cell bit positions, ascending
-};
-
 struct SOp {
   int32_t kind;           // TQK_S_*
   int32_t lb;             // DENSE1 / X: target bit (inside the tile)
@@ -67,7 +50,7 @@ struct SOp {
   uint64_t cval;          // DENSE1 / X: required values of the control bits
   int32_t nd;             // DIAG: number of bits (1 or 2)
   int32_t dbits[2];       // DIAG: bit positions, most significant diag-index bit first
-  int32_t dim;            // DENSE1 / X: position of lb among its sweep's cell bits
+  int32_t pad;
   const float2* operand;  // DENSE1 [batch][4], PHASE [batch], DIAG [batch][2^nd]
   int64_t op_stride;      // float2 per row (0 when shared by every row)
   double* grad;           // complex128 cotangent (interleaved), or null
@@ -82,9 +65,7 @@ struct Params {
   int nops;
   int64_t tiles;          // tiles per row
   int* status;            // TQK_TIMEOUT if a tile load did not complete
-  int nsweeps;
   SOp ops[TQK_STAGED_MAX_OPS];
-  Sweep sweeps[TQK_STAGED_MAX_OPS];
 };
 
 // Per-tile view of an op: its control / phase condition split into the bits inside the
@@ -128,127 +109,86 @@ __device__ __forceinline__ int diag_local(const SOp& o, const Local& L, uint32_t
   return d;
 }
 
+// First index i0 (target bit lb clear) of pair-pair q: two adjacent pairs (i0, i0 + 2^lb)
+// and (i0 + 1, i0 + 1 + 2^lb) when lb >= 1; one pair (2q, 2q + 1) when lb == 0.
+__device__ __forceinline__ uint32_t pair_base(uint32_t q, int lb) {
+  if (lb == 0) return q << 1;
+  const uint32_t lowm = (1u << (lb - 1)) - 1u;
+  return ((q >> (lb - 1)) << (lb + 1)) | ((q & lowm) << 1);
+}
+
 __device__ __forceinline__ void mat2(const float2 (&M)[4], float2& a0, float2& a1) {
   const float2 y0 = cfma(M[0], a0, cmul(M[1], a1));
   a1 = cfma(M[2], a0, cmul(M[3], a1));
   a0 = y0;
 }
 
-// Operands of the ops for batch row b, copied once per CTA into shared memory.
-__device__ __forceinline__ void load_operands(const Params& p, int64_t b, float2 (*opnd)[4]) {
-  for (int i = threadIdx.x; i < p.nops * 4; i += kThreads) {
-    const SOp& o = p.ops[i >> 2];
-    const int e = i & 3;
-    const int cnt = o.kind == TQK_S_DENSE1 ? 4 : (o.kind == TQK_S_PHASE ? 1 : (o.kind == TQK_S_DIAG ? 1 << o.nd : 0));
-    opnd[i >> 2][e] = e < cnt ? __ldg(o.operand + b * o.op_stride + e) : make_float2(0.f, 0.f);
-  }
-}
-
-// In-tile indices of the 2^ND amplitudes of cell c: c with zeros inserted at the cell bits,
-// then every combination of the cell bits (combination r sets cell bit d for bit d of r).
-template <int ND>
-__device__ __forceinline__ void cell_index(const Sweep& sw, uint32_t c, uint32_t (&idx)[1 << ND]) {
-  uint32_t base = c;
-#pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    const int q = sw.bits[d];
-    base = ((base >> q) << (q + 1)) | (base & ((1u << q) - 1u));
-  }
-#pragma unroll
-  for (int r = 0; r < (1 << ND); ++r) {
-    uint32_t v = base;
-#pragma unroll
-    for (int d = 0; d < ND; ++d)
-      if ((r >> d) & 1) v |= 1u << sw.bits[d];
-    idx[r] = v;
-  }
-}
-
-// Cells with bit 0 among their bits hold amplitude pairs (r, r + 1) at adjacent even
-// indices: 16-byte accesses; otherwise 8-byte accesses (consecutive lanes then address
-// consecutive amplitudes).
-template <int ND>
-__device__ __forceinline__ void load_cell(const float2* t, const uint32_t (&idx)[1 << ND], bool vec,
-                                          float2 (&a)[1 << ND]) {
-  if (vec) {
-#pragma unroll
-    for (int r = 0; r < (1 << ND); r += 2) {
-      const float4 v = *reinterpret_cast<const float4*>(t + idx[r]);
-      a[r] = lo2(v);
-      a[r + 1] = hi2(v);
-    }
-  } else {
-#pragma unroll
-    for (int r = 0; r < (1 << ND); ++r) a[r] = t[idx[r]];
-  }
-}
-
-template <int ND>
-__device__ __forceinline__ void store_cell(float2* t, const uint32_t (&idx)[1 << ND], bool vec,
-                                           const float2 (&a)[1 << ND]) {
-  if (vec) {
-#pragma unroll
-    for (int r = 0; r < (1 << ND); r += 2) *reinterpret_cast<float4*>(t + idx[r]) = pack4(a[r], a[r + 1]);
-  } else {
-#pragma unroll
-    for (int r = 0; r < (1 << ND); ++r) t[idx[r]] = a[r];
-  }
-}
-
-// Forward of a dense / X op on the cell's pairs along cell dimension K.
-template <int ND, int K>
-__device__ __forceinline__ void pairs_fwd(bool x, const float2 (&M)[4], const Local& L,
-                                          const uint32_t (&idx)[1 << ND], float2 (&a)[1 << ND]) {
-#pragma unroll
-  for (int r = 0; r < (1 << ND); ++r) {
-    if ((r >> K) & 1) continue;
-    const int r1 = r | (1 << K);
-    if ((idx[r] & L.lmask) != L.lval) continue;
-    if (x) {
-      const float2 t = a[r];
-      a[r] = a[r1];
-      a[r1] = t;
-    } else {
-      mat2(M, a[r], a[r1]);
-    }
-  }
-}
-
-template <int ND>
-__device__ __forceinline__ void cell_fwd(const SOp& o, const Local& L, const float2* opd, const uint32_t (&idx)[1 << ND],
-                                         float2 (&a)[1 << ND]) {
+// Forward application of one op to the tile (amp, 2^m amplitudes at global index base).
+__device__ __forceinline__ void apply_fwd(const SOp& o, float2* amp, int m, uint64_t base, int64_t b) {
+  const Local L = localise(o, m, base);
   if (!L.active) return;  // uniform for the tile
+  const int tsz = 1 << m;
+  float4* amp4 = reinterpret_cast<float4*>(amp);
   if (o.kind == TQK_S_DENSE1 || o.kind == TQK_S_X) {
+    const int lb = o.lb;
     const bool x = o.kind == TQK_S_X;
     float2 M[4];
+    if (!x) {
+      const float2* src = o.operand + b * o.op_stride;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) M[e] = opd[e];
-    if (o.dim == 0) pairs_fwd<ND, 0>(x, M, L, idx, a);
-    else if (ND > 1 && o.dim == 1) pairs_fwd<ND, (ND > 1 ? 1 : 0)>(x, M, L, idx, a);
-    else if (ND > 2) pairs_fwd<ND, (ND > 2 ? 2 : 0)>(x, M, L, idx, a);
+      for (int e = 0; e < 4; ++e) M[e] = __ldg(src + e);
+    }
+    const uint32_t nq = lb == 0 ? static_cast<uint32_t>(tsz >> 1) : static_cast<uint32_t>(tsz >> 2);
+    for (uint32_t q = threadIdx.x; q < nq; q += kThreads) {
+      const uint32_t i0 = pair_base(q, lb);
+      if (lb == 0) {
+        if ((i0 & L.lmask) != L.lval) continue;
+        float4 v = amp4[i0 >> 1];
+        float2 a0 = lo2(v), a1 = hi2(v);
+        if (x) amp4[i0 >> 1] = pack4(a1, a0);
+        else {
+          mat2(M, a0, a1);
+          amp4[i0 >> 1] = pack4(a0, a1);
+        }
+        continue;
+      }
+      const uint32_t i1 = i0 | (1u << lb);
+      const bool ok0 = (i0 & L.lmask) == L.lval, ok1 = ((i0 | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 va = amp4[i0 >> 1], vb = amp4[i1 >> 1];
+      float2 a0 = lo2(va), b0 = lo2(vb), a1 = hi2(va), b1 = hi2(vb);  // pairs (a0, b0), (a1, b1)
+      if (x) {
+        if (ok0) { const float2 t = a0; a0 = b0; b0 = t; }
+        if (ok1) { const float2 t = a1; a1 = b1; b1 = t; }
+      } else {
+        if (ok0) mat2(M, a0, b0);
+        if (ok1) mat2(M, a1, b1);
+      }
+      amp4[i0 >> 1] = pack4(a0, a1);
+      amp4[i1 >> 1] = pack4(b0, b1);
+    }
   } else if (o.kind == TQK_S_PHASE) {
-    const float2 ph = opd[0];
-#pragma unroll
-    for (int r = 0; r < (1 << ND); ++r)
-      if ((idx[r] & L.lmask) == L.lval) a[r] = cmul(ph, a[r]);
+    const float2 ph = __ldg(o.operand + b * o.op_stride);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      const bool ok0 = (l & L.lmask) == L.lval, ok1 = ((l | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 v = amp4[q];
+      float2 a0 = lo2(v), a1 = hi2(v);
+      if (ok0) a0 = cmul(ph, a0);
+      if (ok1) a1 = cmul(ph, a1);
+      amp4[q] = pack4(a0, a1);
+    }
   } else {  // DIAG
+    const float2* dv = o.operand + b * o.op_stride;
+    float2 D[4];
 #pragma unroll
-    for (int r = 0; r < (1 << ND); ++r) a[r] = cmul(opd[diag_local(o, L, idx[r])], a[r]);
-  }
-}
-
-template <int ND>
-__device__ __forceinline__ void sweep_fwd(const Params& p, const Sweep& sw, float2* amp, const Local* locs,
-                                          const float2 (*opnd)[4]) {
-  const uint32_t ncells = 1u << (p.m - ND);
-  const bool vec = sw.bits[0] == 0;
-  for (uint32_t c = threadIdx.x; c < ncells; c += kThreads) {
-    uint32_t idx[1 << ND];
-    cell_index<ND>(sw, c, idx);
-    float2 a[1 << ND];
-    load_cell<ND>(amp, idx, vec, a);
-    for (int j = sw.first; j < sw.first + sw.count; ++j) cell_fwd<ND>(p.ops[j], locs[j], opnd[j], idx, a);
-    store_cell<ND>(amp, idx, vec, a);
+    for (int e = 0; e < 4; ++e) D[e] = e < (1 << o.nd) ? __ldg(dv + e) : make_float2(0.f, 0.f);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      float4 v = amp4[q];
+      amp4[q] = pack4(cmul(D[diag_local(o, L, l)], lo2(v)), cmul(D[diag_local(o, L, l | 1u)], hi2(v)));
+    }
   }
 }
 
@@ -256,13 +196,10 @@ __global__ void __launch_bounds__(kThreads) k_staged(const __grid_constant__ Par
   extern __shared__ float4 sm4[];
   __shared__ uint64_t full;
   __shared__ int abort_flag;
-  __shared__ Local locs[TQK_STAGED_MAX_OPS];
-  __shared__ float2 opnd[TQK_STAGED_MAX_OPS][4];
   float2* amp = reinterpret_cast<float2*>(sm4);
   const int64_t b = blockIdx.y;
   const uint32_t bytes = static_cast<uint32_t>(sizeof(float2)) << p.m;
   float2* row = p.psi + (b << p.n);
-  load_operands(p, b, opnd);
   if (threadIdx.x == 0) {
     mbar_init(&full);
     abort_flag = 0;
@@ -273,14 +210,10 @@ __global__ void __launch_bounds__(kThreads) k_staged(const __grid_constant__ Par
     const uint64_t base = (uint64_t)t << p.m;
     if (threadIdx.x == 0 && !load_tile(&full, use, 1, amp, row + base, nullptr, nullptr, bytes, p.status))
       abort_flag = 1;
-    if (threadIdx.x < p.nops) locs[threadIdx.x] = localise(p.ops[threadIdx.x], p.m, base);
     __syncthreads();
     if (abort_flag) break;  // uniform
-    for (int s = 0; s < p.nsweeps; ++s) {
-      const Sweep& sw = p.sweeps[s];
-      if (sw.nd == 3) sweep_fwd<3>(p, sw, amp, locs, opnd);
-      else if (sw.nd == 2) sweep_fwd<2>(p, sw, amp, locs, opnd);
-      else sweep_fwd<1>(p, sw, amp, locs, opnd);
+    for (int j = 0; j < p.nops; ++j) {
+      apply_fwd(p.ops[j], amp, p.m, base, b);
       __syncthreads();
     }
     fence_async_smem();  // the ops' shared-memory writes, visible to the bulk store
@@ -339,102 +272,109 @@ __device__ __forceinline__ void adj_pair(const float2 (&M)[4], float2& a0, float
   a1 = y1;
 }
 
-// Reverse of a dense / X op on the cell's pairs along cell dimension K (psi a, lam l).
-template <int ND, int K>
-__device__ __forceinline__ void pairs_adj(bool x, const float2 (&M)[4], const Local& L, const uint32_t (&idx)[1 << ND],
-                                          float2 (&a)[1 << ND], float2 (&l)[1 << ND], bool grad, float (&g)[8]) {
-#pragma unroll
-  for (int r = 0; r < (1 << ND); ++r) {
-    if ((r >> K) & 1) continue;
-    const int r1 = r | (1 << K);
-    if ((idx[r] & L.lmask) != L.lval) continue;
-    if (x) {
-      float2 t = a[r];
-      a[r] = a[r1];
-      a[r1] = t;
-      t = l[r];
-      l[r] = l[r1];
-      l[r1] = t;
-    } else {
-      adj_pair(M, a[r], a[r1], l[r], l[r1], grad, g);
-    }
-  }
-}
-
-// One op's reverse step on a cell: psi <- U^H psi, lam <- U^H lam, cotangent partials in g.
-template <int ND>
-__device__ __forceinline__ void cell_adj(const SOp& o, const Local& L, const float2* opd, const uint32_t (&idx)[1 << ND],
-                                         float2 (&a)[1 << ND], float2 (&l)[1 << ND], float (&g)[8]) {
+// One reverse step of op o on the psi / lam tiles; cotangent partials into acc (8 doubles).
+__device__ __forceinline__ void apply_adj(const SOp& o, float2* ps, float2* ls, int m, uint64_t base, int64_t b,
+                                          float (*red)[8], double* acc) {
+  const Local L = localise(o, m, base);
   if (!L.active) return;  // uniform for the tile
+  const int tsz = 1 << m;
   const bool grad = o.grad != nullptr;
+  float4* p4 = reinterpret_cast<float4*>(ps);
+  float4* l4 = reinterpret_cast<float4*>(ls);
+  float g[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) g[j] = 0.f;
   if (o.kind == TQK_S_DENSE1 || o.kind == TQK_S_X) {
+    const int lb = o.lb;
     const bool x = o.kind == TQK_S_X;
     float2 M[4];
+    if (!x) {
+      const float2* src = o.operand + b * o.op_stride;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) M[e] = opd[e];
-    if (o.dim == 0) pairs_adj<ND, 0>(x, M, L, idx, a, l, grad, g);
-    else if (ND > 1 && o.dim == 1) pairs_adj<ND, (ND > 1 ? 1 : 0)>(x, M, L, idx, a, l, grad, g);
-    else if (ND > 2) pairs_adj<ND, (ND > 2 ? 2 : 0)>(x, M, L, idx, a, l, grad, g);
+      for (int e = 0; e < 4; ++e) M[e] = __ldg(src + e);
+    }
+    const uint32_t nq = lb == 0 ? static_cast<uint32_t>(tsz >> 1) : static_cast<uint32_t>(tsz >> 2);
+    for (uint32_t q = threadIdx.x; q < nq; q += kThreads) {
+      const uint32_t i0 = pair_base(q, lb);
+      if (lb == 0) {
+        if ((i0 & L.lmask) != L.lval) continue;
+        float4 va = p4[i0 >> 1], vl = l4[i0 >> 1];
+        float2 a0 = lo2(va), a1 = hi2(va), l0 = lo2(vl), l1 = hi2(vl);
+        if (x) {
+          p4[i0 >> 1] = pack4(a1, a0);
+          l4[i0 >> 1] = pack4(l1, l0);
+        } else {
+          adj_pair(M, a0, a1, l0, l1, grad, g);
+          p4[i0 >> 1] = pack4(a0, a1);
+          l4[i0 >> 1] = pack4(l0, l1);
+        }
+        continue;
+      }
+      const uint32_t i1 = i0 | (1u << lb);
+      const bool ok0 = (i0 & L.lmask) == L.lval, ok1 = ((i0 | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 pa = p4[i0 >> 1], pb = p4[i1 >> 1], la = l4[i0 >> 1], lb4 = l4[i1 >> 1];
+      float2 a0 = lo2(pa), b0 = lo2(pb), a1 = hi2(pa), b1 = hi2(pb);
+      float2 c0 = lo2(la), d0 = lo2(lb4), c1 = hi2(la), d1 = hi2(lb4);
+      if (x) {
+        if (ok0) { float2 t = a0; a0 = b0; b0 = t; t = c0; c0 = d0; d0 = t; }
+        if (ok1) { float2 t = a1; a1 = b1; b1 = t; t = c1; c1 = d1; d1 = t; }
+      } else {
+        if (ok0) adj_pair(M, a0, b0, c0, d0, grad, g);
+        if (ok1) adj_pair(M, a1, b1, c1, d1, grad, g);
+      }
+      p4[i0 >> 1] = pack4(a0, a1);
+      p4[i1 >> 1] = pack4(b0, b1);
+      l4[i0 >> 1] = pack4(c0, c1);
+      l4[i1 >> 1] = pack4(d0, d1);
+    }
+    if (x) return;
   } else if (o.kind == TQK_S_PHASE) {
-    const float2 phc = cconj(opd[0]);
-#pragma unroll
-    for (int r = 0; r < (1 << ND); ++r) {
-      if ((idx[r] & L.lmask) != L.lval) continue;
-      a[r] = cmul(phc, a[r]);
-      if (grad) acc_c(g, 0, l[r], a[r]);
-      l[r] = cmul(phc, l[r]);
+    const float2 phc = cconj(__ldg(o.operand + b * o.op_stride));
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      const bool ok0 = (l & L.lmask) == L.lval, ok1 = ((l | 1u) & L.lmask) == L.lval;
+      if (!ok0 && !ok1) continue;
+      float4 vp = p4[q], vl = l4[q];
+      float2 a0 = lo2(vp), a1 = hi2(vp), c0 = lo2(vl), c1 = hi2(vl);
+      if (ok0) {
+        a0 = cmul(phc, a0);
+        if (grad) acc_c(g, 0, c0, a0);
+        c0 = cmul(phc, c0);
+      }
+      if (ok1) {
+        a1 = cmul(phc, a1);
+        if (grad) acc_c(g, 0, c1, a1);
+        c1 = cmul(phc, c1);
+      }
+      p4[q] = pack4(a0, a1);
+      l4[q] = pack4(c0, c1);
     }
   } else {  // DIAG (nd <= 2)
+    const float2* dv = o.operand + b * o.op_stride;
+    float2 D[4];
 #pragma unroll
-    for (int r = 0; r < (1 << ND); ++r) {
-      const int d = diag_local(o, L, idx[r]);
-      const float2 D = cconj(opd[d]);
-      const float2 y = cmul(D, a[r]);
+    for (int e = 0; e < 4; ++e) D[e] = e < (1 << o.nd) ? cconj(__ldg(dv + e)) : make_float2(0.f, 0.f);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(tsz >> 1); q += kThreads) {
+      const uint32_t l = q << 1;
+      const int d0 = diag_local(o, L, l), d1 = diag_local(o, L, l | 1u);
+      float4 vp = p4[q], vl = l4[q];
+      const float2 y0 = cmul(D[d0], lo2(vp)), y1 = cmul(D[d1], hi2(vp));
       if (grad) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (j == d) acc_c(g, j, l[r], y);
+        for (int j = 0; j < 4; ++j) {
+          if (j == d0) acc_c(g, j, lo2(vl), y0);
+          if (j == d1) acc_c(g, j, hi2(vl), y1);
+        }
       }
-      a[r] = y;
-      l[r] = cmul(D, l[r]);
+      p4[q] = pack4(y0, y1);
+      l4[q] = pack4(cmul(D[d0], lo2(vl)), cmul(D[d1], hi2(vl)));
     }
   }
+  if (grad) block_accumulate<8>(g, red, acc);
 }
 
-// A sweep in reverse (its ops last to first on every cell), then each op's cotangent
-// partials reduced over the CTA into its float64 accumulator.
-template <int ND>
-__device__ __forceinline__ void sweep_adj(const Params& p, const Sweep& sw, float2* ps, float2* ls, const Local* locs,
-                                          const float2 (*opnd)[4], float (*red)[8], double (*gacc)[8]) {
-  const uint32_t ncells = 1u << (p.m - ND);
-  const bool vec = sw.bits[0] == 0;
-  float g[kMaxSweepOps][8];
-#pragma unroll
-  for (int k = 0; k < kMaxSweepOps; ++k)
-#pragma unroll
-    for (int v = 0; v < 8; ++v) g[k][v] = 0.f;
-  for (uint32_t c = threadIdx.x; c < ncells; c += kThreads) {
-    uint32_t idx[1 << ND];
-    cell_index<ND>(sw, c, idx);
-    float2 a[1 << ND], l[1 << ND];
-    load_cell<ND>(ps, idx, vec, a);
-    load_cell<ND>(ls, idx, vec, l);
-#pragma unroll
-    for (int k = kMaxSweepOps - 1; k >= 0; --k)
-      if (k < sw.count) cell_adj<ND>(p.ops[sw.first + k], locs[sw.first + k], opnd[sw.first + k], idx, a, l, g[k]);
-    store_cell<ND>(ps, idx, vec, a);
-    store_cell<ND>(ls, idx, vec, l);
-  }
-#pragma unroll
-  for (int k = 0; k < kMaxSweepOps; ++k) {
-    if (k >= sw.count) break;
-    const SOp& o = p.ops[sw.first + k];
-    if (o.grad != nullptr && o.kind != TQK_S_X && locs[sw.first + k].active)  // uniform
-      block_accumulate<8>(g[k], red, gacc[sw.first + k]);
-  }
-}
-
-__global__ void __launch_bounds__(kThreads, 2) k_staged_adj(const __grid_constant__ Params p) {
+__global__ void __launch_bounds__(kThreads) k_staged_adj(const __grid_constant__ Params p) {
   extern __shared__ float4 sm4[];
   const int tsz = 1 << p.m;
   float2* ps = reinterpret_cast<float2*>(sm4);
@@ -443,14 +383,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_staged_adj(const __grid_constan
   __shared__ float red[kWarps][8];
   __shared__ uint64_t full;
   __shared__ int abort_flag;
-  __shared__ Local locs[TQK_STAGED_MAX_OPS];
-  __shared__ float2 opnd[TQK_STAGED_MAX_OPS][4];
   for (int i = threadIdx.x; i < TQK_STAGED_MAX_OPS * 8; i += kThreads) gacc[i / 8][i % 8] = 0.0;
   const int64_t b = blockIdx.y;
   const uint32_t bytes = static_cast<uint32_t>(sizeof(float2)) << p.m;
   float2* prow = p.psi + (b << p.n);
   float2* lrow = p.lam + (b << p.n);
-  load_operands(p, b, opnd);
   if (threadIdx.x == 0) {
     mbar_init(&full);
     abort_flag = 0;
@@ -461,14 +398,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_staged_adj(const __grid_constan
     const uint64_t base = (uint64_t)t << p.m;
     if (threadIdx.x == 0 && !load_tile(&full, use, 2, ps, prow + base, ls, lrow + base, bytes, p.status))
       abort_flag = 1;
-    if (threadIdx.x < p.nops) locs[threadIdx.x] = localise(p.ops[threadIdx.x], p.m, base);
     __syncthreads();
     if (abort_flag) break;  // uniform
-    for (int s = p.nsweeps - 1; s >= 0; --s) {
-      const Sweep& sw = p.sweeps[s];
-      if (sw.nd == 3) sweep_adj<3>(p, sw, ps, ls, locs, opnd, red, gacc);
-      else if (sw.nd == 2) sweep_adj<2>(p, sw, ps, ls, locs, opnd, red, gacc);
-      else sweep_adj<1>(p, sw, ps, ls, locs, opnd, red, gacc);
+    for (int j = p.nops - 1; j >= 0; --j) {
+      apply_adj(p.ops[j], ps, ls, p.m, base, b, red, gacc[j]);
       __syncthreads();
     }
     fence_async_smem();
@@ -565,49 +498,6 @@ int fill_staged(staged::Params& p, int64_t bsz, int n, const tqk_staged_op* ops,
   return TQK_OK;
 }
 
-// Sweeps: consecutive ops (at most kMaxSweepOps) whose dense / X target bits number at most
-// min(3, tile bits); phase and diagonal ops join any sweep.  Cell bits: the targets, then
-// the lowest other tile bits, ascending; each dense / X op records its target's position.
-void plan_sweeps(staged::Params& p) {
-  const int nd = p.m < staged::kCellDims ? p.m : staged::kCellDims;
-  p.nsweeps = 0;
-  int j = 0;
-  while (j < p.nops) {
-    staged::Sweep& sw = p.sweeps[p.nsweeps++];
-    sw.first = j;
-    sw.count = 0;
-    sw.nd = nd;
-    uint32_t tmask = 0;
-    while (j < p.nops && sw.count < staged::kMaxSweepOps) {
-      const staged::SOp& o = p.ops[j];
-      uint32_t t = tmask;
-      if (o.kind == TQK_S_DENSE1 || o.kind == TQK_S_X) t |= 1u << o.lb;
-      if (__builtin_popcount(t) > nd) break;
-      tmask = t;
-      ++sw.count;
-      ++j;
-    }
-    int nb = 0;
-    for (int q = 0; q < p.m && nb < nd; ++q)  // targets first ...
-      if ((tmask >> q) & 1u) sw.bits[nb++] = q;
-    for (int q = 0; q < p.m && nb < nd; ++q)  // ... then the lowest other bits
-      if (!((tmask >> q) & 1u)) sw.bits[nb++] = q;
-    for (int a = 1; a < nd; ++a)  // ascending
-      for (int c = a; c > 0 && sw.bits[c - 1] > sw.bits[c]; --c) {
-        const int t = sw.bits[c];
-        sw.bits[c] = sw.bits[c - 1];
-        sw.bits[c - 1] = t;
-      }
-    for (int k = sw.first; k < sw.first + sw.count; ++k) {
-      staged::SOp& o = p.ops[k];
-      o.dim = 0;
-      if (o.kind == TQK_S_DENSE1 || o.kind == TQK_S_X)
-        for (int d = 0; d < nd; ++d)
-          if (sw.bits[d] == o.lb) o.dim = d;
-    }
-  }
-}
-
 int launch_staged(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op* ops, int nops, int tile_bits,
                   int* status, bool adjoint, void* stream, const char* what) {
   int rc = check_state(psi, bsz, n, what);
@@ -616,7 +506,6 @@ int launch_staged(void* psi, void* lam, int64_t bsz, int n, const tqk_staged_op*
   staged::Params p;
   if ((rc = fill_staged(p, bsz, n, ops, nops, tile_bits, adjoint, what))) return rc;
   if (nops == 0) return TQK_OK;
-  plan_sweeps(p);
   if (status == nullptr) return fail(TQK_BAD_POINTER, "%s: null status word", what);
   p.psi = static_cast<float2*>(psi);
   p.lam = static_cast<float2*>(lam);
