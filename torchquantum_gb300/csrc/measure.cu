@@ -6,7 +6,7 @@
 // Strings that all share one xmask are evaluated 8 at a time in one pass over the state
 // (each amplitude pair (i, i^x) is read once for all of them).  Strings with several
 // xmasks are grouped and each group is one coset pass (k_coset): the row is cut into
-// cosets of the span of the group's xmasks, staged in shared memory by bulk copies, so
+// cosets of the span of the group's xmasks, staged in shared memory (16-byte cp.async copies), so
 // all partners are read on chip and DRAM reads the state once per group.  Each thread
 // accumulates in float32, blocks reduce in float64 and write one partial per (row,
 // block or coset, string) to scratch; a second kernel adds the partials in a fixed
@@ -236,8 +236,9 @@ __global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* 
 // stage, so every partner amplitude psi[i ^ x_s] of every string of the group is read on
 // chip and DRAM reads each amplitude once per pass.
 //
-// Chunks: the lowest c index bits stay contiguous (runs of 2^c amplitudes, moved by bulk
-// copies).  The high parts x_s >> c of the group's X-masks span an r-dimensional space;
+// Chunks: the lowest c index bits stay contiguous (runs of 2^c amplitudes, copied in
+// 16-byte pieces: bulk copies of runs this short are limited by the copy engine's
+// per-request cost, not by bandwidth).  The high parts x_s >> c of the group's X-masks span an r-dimensional space;
 // b_0..b_{r-1} is its reduced echelon basis (pivot bits p_0 < ... < p_{r-1}, each present
 // in its own basis vector only).  Coset t of a row is rep(t) + span{b_k} over the high
 // index bits, rep(t) = t with zeros inserted at the pivot bits; stage slot a (r bits)
@@ -252,8 +253,8 @@ __global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* 
 // used, which makes c + r = T: every stage is 2^T amplitudes (64 KB at n >= 13) and a row
 // has 2^(n - T) cosets.
 //
-// CTA: one producer warp (bulk copies of a stage's chunks completing on the stage's full
-// mbarrier) and fifteen consumer warps; three stages in flight.  Expvals: each consumer
+// CTA: one producer warp (16-byte cp.async copies of a stage's chunks, each lane arriving
+// on the stage's full mbarrier when its copies have landed) and fifteen consumer warps; three stages in flight.  Expvals: each consumer
 // thread accumulates Re(conj(psi_u) (P_s psi)_u) in float32 over its amplitudes of the
 // coset, the CTA reduces in float64 and writes one partial per (coset, string); the
 // partials are summed per row in a fixed order (k_expval_finish).  Backward seed: each
@@ -296,6 +297,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bulk::smem_addr(bar)) : "memory");
 }
 __device__ __forceinline__ float4 lds4(const float2* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(bulk::smem_addr(dst)), "l"(src) : "memory");
+}
+// Arrive on bar once every cp.async this thread issued so far has landed (the barrier's
+// expected count includes this thread).
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bulk::smem_addr(bar)) : "memory");
+}
 
 // rep(t): t with a zero inserted at each pivot bit (ascending)
 __device__ __forceinline__ uint32_t coset_rep(uint32_t t, const CosetParams& p) {
@@ -369,7 +378,7 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
   float2* const stage0 = reinterpret_cast<float2*>(coset_smem);
   if (threadIdx.x == 0) {
     for (int s = 0; s < kCosetStages; ++s) {
-      mbar_init_count(&full[s], 1);
+      mbar_init_count(&full[s], 32);  // the producer warp's lanes (cp.async arrive.noinc)
       mbar_init_count(&empty[s], kCosetConsumerWarps);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -381,8 +390,8 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
   int last_issued = -1;  // producer: the last pipeline iteration whose loads it issued
   if (warp == kCosetConsumerWarps) {
     // ---------------- producer
-    const uint32_t chunk_bytes = 8u << p.c;
     const int nslots = 1 << p.r;
+    const uint32_t pmask = (1u << (p.c - 1)) - 1u;  // 16-byte pieces per chunk, minus one
     int it = 0;
     for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
       const int st = it % kCosetStages;
@@ -404,13 +413,17 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
         slot_h[st][a] = h;
       }
       __syncwarp();
-      if (lane == 0) bulk::mbar_expect(&full[st], tile * 8u);
-      __syncwarp();
+      // 16-byte cp.async pieces (a warp instruction moves 512 contiguous bytes of one or
+      // two chunks); each lane's copies arrive on the stage's full barrier when complete
       const float2* row = p.state + (static_cast<uint64_t>(b) << p.n);
       float2* dst = stage0 + static_cast<size_t>(st) * tile;
-      for (int a = lane; a < nslots; a += 32)
-        bulk::bulk_load(dst + (static_cast<size_t>(a) << p.c), row + (static_cast<uint64_t>(slot_h[st][a]) << p.c),
-                        chunk_bytes, &full[st]);
+      const uint32_t npieces = tile >> 1;
+      for (uint32_t k = lane; k < npieces; k += 32) {
+        const uint32_t a = k >> (p.c - 1), off = (k & pmask) << 1;
+        cp_async16(dst + (static_cast<size_t>(a) << p.c) + off,
+                   row + (static_cast<uint64_t>(slot_h[st][a]) << p.c) + off);
+      }
+      cp_async_arrive(&full[st]);
       last_issued = it;
     }
   } else {
