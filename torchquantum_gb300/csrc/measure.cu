@@ -315,67 +315,69 @@ __device__ __forceinline__ uint32_t coset_rep(uint32_t t, const CosetParams& p) 
   return t;
 }
 
-// One string's sum over a staged coset, each amplitude pair (u, u + 1) with bit h of u
-// clear (npairs = pairs to visit) against its partner pair ((u ^ x) & ~1); SW: x is odd, so
-// the partner pair is in swapped order; ODD: odd number of Y factors (imaginary part).
-// Returns the thread's float32 partial of the half sum.
+// The coset stages (dynamic shared memory), indexed as float4 pairs of amplitudes so that
+// every access below is a 32-bit shared-memory load.
+extern __shared__ __align__(128) float4 coset_stage4[];
+
+// One string's sum over a staged coset (stage base b4, in float4 units), each amplitude pair
+// (u, u + 1) with bit h of u clear (npairs = pairs to visit) against its partner pair
+// ((u ^ x) & ~1); SW: x is odd, so the partner pair is in swapped order; ODD: odd number of Y
+// factors (imaginary part).  Returns the thread's float32 partial of the half sum.
 template <bool SW, bool ODD>
-__device__ __forceinline__ float coset_string_sum(const float2* stg, uint32_t npairs, uint32_t h, uint32_t x,
-                                                  uint32_t gam, uint32_t rho, int ct) {
+__device__ __forceinline__ float coset_string_sum(uint32_t b4, uint32_t npairs, uint32_t h, uint32_t x, uint32_t gam,
+                                                  uint32_t rho, int ct) {
   const uint32_t lo = (1u << h) - 1u;
   const uint32_t g1 = gam & 1u;
+  const uint32_t x4 = x >> 1;  // partner pair index = (u >> 1) ^ (x >> 1)
   float a = 0.f;
 #pragma unroll 2
   for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
-    const uint32_t v2 = j << 1;
-    const uint32_t u = ((v2 >> h) << (h + 1)) | (v2 & lo);
-    const float4 v = lds4(stg + u);
-    const float4 w = lds4(stg + ((u ^ x) & ~1u));
+    // pair index of u: j with a zero inserted at bit h - 1 (u = 2 x pair index, h >= 1)
+    const uint32_t pu = ((j >> (h - 1)) << h) | (j & (lo >> 1));
+    const float4 v = coset_stage4[b4 + pu];
+    const float4 w = coset_stage4[b4 + (pu ^ x4)];
     const float2 a0 = lo2(v), a1 = hi2(v);
     const float2 b0 = SW ? hi2(w) : lo2(w), b1 = SW ? lo2(w) : hi2(w);
     const float c0 = ODD ? a0.x * b0.y - a0.y * b0.x : a0.x * b0.x + a0.y * b0.y;
     const float c1 = ODD ? a1.x * b1.y - a1.y * b1.x : a1.x * b1.x + a1.y * b1.y;
-    a += flip_if_odd(c0 + flip_if_odd(c1, g1), static_cast<uint32_t>(__popc(u & gam)) + rho);
+    a += flip_if_odd(c0 + flip_if_odd(c1, g1), static_cast<uint32_t>(__popc((pu << 1) & gam)) + rho);
   }
   return a;
 }
 
 // Diagonal string (x = 0): sum of +-|psi_u|^2 over every pair of the coset.
-__device__ __forceinline__ float coset_diag_sum(const float2* stg, uint32_t npairs, uint32_t gam, uint32_t rho, int ct) {
+__device__ __forceinline__ float coset_diag_sum(uint32_t b4, uint32_t npairs, uint32_t gam, uint32_t rho, int ct) {
   const uint32_t g1 = gam & 1u;
   float a = 0.f;
   for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
-    const uint32_t u = j << 1;
-    const float4 v = lds4(stg + u);
+    const float4 v = coset_stage4[b4 + j];
     const float p0 = v.x * v.x + v.y * v.y, p1 = v.z * v.z + v.w * v.w;
-    a += flip_if_odd(p0 + flip_if_odd(p1, g1), static_cast<uint32_t>(__popc(u & gam)) + rho);
+    a += flip_if_odd(p0 + flip_if_odd(p1, g1), static_cast<uint32_t>(__popc((j << 1) & gam)) + rho);
   }
   return a;
 }
 
 // x = 1: each pair (u, u + 1) is its own partner; the u-side term (counted twice by the caller).
-__device__ __forceinline__ float coset_x1_sum(const float2* stg, uint32_t npairs, bool odd, uint32_t gam, uint32_t rho,
+__device__ __forceinline__ float coset_x1_sum(uint32_t b4, uint32_t npairs, bool odd, uint32_t gam, uint32_t rho,
                                               int ct) {
   float a = 0.f;
   for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
-    const uint32_t u = j << 1;
-    const float4 v = lds4(stg + u);
+    const float4 v = coset_stage4[b4 + j];
     const float c0 = odd ? v.x * v.w - v.y * v.z : v.x * v.z + v.y * v.w;
-    a += flip_if_odd(c0, static_cast<uint32_t>(__popc(u & gam)) + rho);
+    a += flip_if_odd(c0, static_cast<uint32_t>(__popc((j << 1) & gam)) + rho);
   }
   return a;
 }
 
 template <bool SEED, int NS>
 __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p) {
-  extern __shared__ __align__(128) unsigned char coset_smem[];
   __shared__ __align__(8) uint64_t full[kCosetStages], empty[kCosetStages];
   __shared__ uint32_t slot_h[kCosetStages][1 << kCosetMaxRank];
   __shared__ float red[2][kCosetConsumerWarps][kMaxStringsPerPass];
   __shared__ int quit;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t tile = 1u << p.tb;
-  float2* const stage0 = reinterpret_cast<float2*>(coset_smem);
+  float2* const stage0 = reinterpret_cast<float2*>(coset_stage4);
   if (threadIdx.x == 0) {
     for (int s = 0; s < kCosetStages; ++s) {
       mbar_init_count(&full[s], 32);  // the producer warp's lanes (cp.async arrive.noinc)
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
           *vquit = 1;
         }
       }
-      const float2* stg = stage0 + static_cast<size_t>(st) * tile;
+      const uint32_t b4 = static_cast<uint32_t>(st) * (tile >> 1);  // stage start, float4 units
       float acc[NS];
 #pragma unroll
       for (int s = 0; s < NS; ++s) acc[s] = 0.f;
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
           const uint32_t u = q << 1;
           float4 w[NS];
 #pragma unroll
-          for (int s = 0; s < NS; ++s) w[s] = lds4(stg + ((u ^ xs[s]) & ~1u));
+          for (int s = 0; s < NS; ++s) w[s] = coset_stage4[b4 + ((u ^ xs[s]) >> 1)];
           float2 o0 = make_float2(0.f, 0.f), o1 = o0;
 #pragma unroll
           for (int s = 0; s < NS; ++s) {
@@ -512,14 +514,14 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
         for (int s = 0; s < NS; ++s) {
           if (kind[s] == 3u) continue;  // padding
           float a;
-          if (kind[s] == 0u) a = coset_diag_sum(stg, tile >> 1, gam[s], rho[s], ct);
-          else if (kind[s] == 1u) a = 2.f * coset_x1_sum(stg, tile >> 1, odd[s] != 0u, gam[s], rho[s], ct);
+          if (kind[s] == 0u) a = coset_diag_sum(b4, tile >> 1, gam[s], rho[s], ct);
+          else if (kind[s] == 1u) a = 2.f * coset_x1_sum(b4, tile >> 1, odd[s] != 0u, gam[s], rho[s], ct);
           else if (xs[s] & 1u)
-            a = 2.f * (odd[s] ? coset_string_sum<true, true>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
-                              : coset_string_sum<true, false>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
+            a = 2.f * (odd[s] ? coset_string_sum<true, true>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
+                              : coset_string_sum<true, false>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
           else
-            a = 2.f * (odd[s] ? coset_string_sum<false, true>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
-                              : coset_string_sum<false, false>(stg, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
+            a = 2.f * (odd[s] ? coset_string_sum<false, true>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
+                              : coset_string_sum<false, false>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
           acc[s] = a;
         }
       }
