@@ -319,19 +319,20 @@ __device__ __forceinline__ uint32_t coset_rep(uint32_t t, const CosetParams& p) 
 // every access below is a 32-bit shared-memory load.
 extern __shared__ __align__(128) float4 coset_stage4[];
 
-// One string's sum over a staged coset (stage base b4, in float4 units), each amplitude pair
-// (u, u + 1) with bit h of u clear (npairs = pairs to visit) against its partner pair
+// One string's sum over a warp's segment of a staged coset (stage base b4, in float4 units;
+// the lane visits j = j0, j0 + 32, ... < j1), each amplitude pair (u, u + 1) with bit h of u
+// clear (j counts those pairs) against its partner pair
 // ((u ^ x) & ~1); SW: x is odd, so the partner pair is in swapped order; ODD: odd number of Y
 // factors (imaginary part).  Returns the thread's float32 partial of the half sum.
 template <bool SW, bool ODD>
-__device__ __forceinline__ float coset_string_sum(uint32_t b4, uint32_t npairs, uint32_t h, uint32_t x, uint32_t gam,
-                                                  uint32_t rho, int ct) {
+__device__ __forceinline__ float coset_string_sum(uint32_t b4, uint32_t j0, uint32_t j1, uint32_t h, uint32_t x,
+                                                  uint32_t gam, uint32_t rho) {
   const uint32_t lo = (1u << h) - 1u;
   const uint32_t g1 = gam & 1u;
   const uint32_t x4 = x >> 1;  // partner pair index = (u >> 1) ^ (x >> 1)
   float a = 0.f;
 #pragma unroll 2
-  for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
+  for (uint32_t j = j0; j < j1; j += 32) {
     // pair index of u: j with a zero inserted at bit h - 1 (u = 2 x pair index, h >= 1)
     const uint32_t pu = ((j >> (h - 1)) << h) | (j & (lo >> 1));
     const float4 v = coset_stage4[b4 + pu];
@@ -346,10 +347,10 @@ __device__ __forceinline__ float coset_string_sum(uint32_t b4, uint32_t npairs, 
 }
 
 // Diagonal string (x = 0): sum of +-|psi_u|^2 over every pair of the coset.
-__device__ __forceinline__ float coset_diag_sum(uint32_t b4, uint32_t npairs, uint32_t gam, uint32_t rho, int ct) {
+__device__ __forceinline__ float coset_diag_sum(uint32_t b4, uint32_t j0, uint32_t j1, uint32_t gam, uint32_t rho) {
   const uint32_t g1 = gam & 1u;
   float a = 0.f;
-  for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
+  for (uint32_t j = j0; j < j1; j += 32) {
     const float4 v = coset_stage4[b4 + j];
     const float p0 = v.x * v.x + v.y * v.y, p1 = v.z * v.z + v.w * v.w;
     a += flip_if_odd(p0 + flip_if_odd(p1, g1), static_cast<uint32_t>(__popc((j << 1) & gam)) + rho);
@@ -358,10 +359,10 @@ __device__ __forceinline__ float coset_diag_sum(uint32_t b4, uint32_t npairs, ui
 }
 
 // x = 1: each pair (u, u + 1) is its own partner; the u-side term (counted twice by the caller).
-__device__ __forceinline__ float coset_x1_sum(uint32_t b4, uint32_t npairs, bool odd, uint32_t gam, uint32_t rho,
-                                              int ct) {
+__device__ __forceinline__ float coset_x1_sum(uint32_t b4, uint32_t j0, uint32_t j1, bool odd, uint32_t gam,
+                                              uint32_t rho) {
   float a = 0.f;
-  for (uint32_t j = ct; j < npairs; j += kCosetConsumers) {
+  for (uint32_t j = j0; j < j1; j += 32) {
     const float4 v = coset_stage4[b4 + j];
     const float c0 = odd ? v.x * v.w - v.y * v.z : v.x * v.z + v.y * v.w;
     a += flip_if_odd(c0, static_cast<uint32_t>(__popc((j << 1) & gam)) + rho);
@@ -505,23 +506,33 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
           st4(dst, pack4(o0, o1));
         }
       } else if (ok) {
-        // expvals, one string at a time (its orientation and Y parity fixed for the loop):
-        // a pair of amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the
-        // side whose bit hb (the highest of xs) is clear -- enumerated directly by inserting
-        // a zero at hb -- and counted twice (P is Hermitian: both sides contribute the same
-        // real part).  xs = 0: |psi|^2 terms; xs = 1: the partner is the pair's other amplitude.
+        // expvals: the visits of all strings in a row (tile / 4 pairs per string, tile / 2 for
+        // x = 0 or 1) are cut into one contiguous segment per warp, so a warp takes one or two
+        // strings, each with its orientation and Y parity fixed for the loop.  A pair of
+        // amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the side whose bit
+        // hb (the highest of xs) is clear -- enumerated directly by inserting a zero at hb --
+        // and counted twice (P is Hermitian: both sides contribute the same real part).
+        uint32_t first[NS + 1];
+        first[0] = 0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+          first[s + 1] = first[s] + (kind[s] == 3u ? 0u : (kind[s] == 2u ? tile >> 2 : tile >> 1));
+        const uint32_t per = ((first[NS] + kCosetConsumerWarps - 1) / kCosetConsumerWarps + 31u) & ~31u;
+        const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(first[NS], w0 + per);
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-          if (kind[s] == 3u) continue;  // padding
+          const uint32_t lo = max(first[s], w0), hi = min(first[s + 1], w1);
+          if (lo >= hi) continue;  // uniform for the warp
+          const uint32_t j0 = lo - first[s] + lane, j1 = hi - first[s];
           float a;
-          if (kind[s] == 0u) a = coset_diag_sum(b4, tile >> 1, gam[s], rho[s], ct);
-          else if (kind[s] == 1u) a = 2.f * coset_x1_sum(b4, tile >> 1, odd[s] != 0u, gam[s], rho[s], ct);
+          if (kind[s] == 0u) a = coset_diag_sum(b4, j0, j1, gam[s], rho[s]);
+          else if (kind[s] == 1u) a = 2.f * coset_x1_sum(b4, j0, j1, odd[s] != 0u, gam[s], rho[s]);
           else if (xs[s] & 1u)
-            a = 2.f * (odd[s] ? coset_string_sum<true, true>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
-                              : coset_string_sum<true, false>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
+            a = 2.f * (odd[s] ? coset_string_sum<true, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
+                              : coset_string_sum<true, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
           else
-            a = 2.f * (odd[s] ? coset_string_sum<false, true>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct)
-                              : coset_string_sum<false, false>(b4, tile >> 2, hb[s], xs[s], gam[s], rho[s], ct));
+            a = 2.f * (odd[s] ? coset_string_sum<false, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
+                              : coset_string_sum<false, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
           acc[s] = a;
         }
       }
