@@ -253,12 +253,13 @@ __global__ void __launch_bounds__(kFinishThreads) k_expval_finish(const double* 
 // used, which makes c + r = T: every stage is 2^T amplitudes (64 KB at n >= 13) and a row
 // has 2^(n - T) cosets.
 //
-// CTA: one producer warp (16-byte cp.async copies of a stage's chunks, each lane arriving
-// on the stage's full mbarrier when its copies have landed) and fifteen consumer warps; three stages in flight.  Expvals: each consumer
-// thread accumulates Re(conj(psi_u) (P_s psi)_u) in float32 over its amplitudes of the
-// coset, the CTA reduces in float64 and writes one partial per (coset, string); the
-// partials are summed per row in a fixed order (k_expval_finish).  Backward seed: each
-// consumer thread forms sum_s c_s (P_s psi)_u for two amplitudes and stores them to the
+// CTA: sixteen warps and three stages.  At the top of each iteration every thread issues
+// its 16-byte cp.async pieces of the coset two iterations ahead into the stage the previous
+// iteration finished reading, and arrives on that stage's full mbarrier once they land;
+// then all wait for the current stage.  Expvals: each warp sums its segment of the strings'
+// pair visits in float32, the CTA reduces in float64 and writes one partial per (coset,
+// string); the partials are summed per row in a fixed order (k_expval_finish).  Backward
+// seed: each thread forms sum_s c_s (P_s psi)_u for two amplitudes and stores them to the
 // output row (added to what is there for groups after the first).
 // Every mbarrier wait is bounded: on expiry the CTA records TQK_TIMEOUT in the status
 // word, stops issuing copies and waiting, writes NaN expval partials (the seed skips its
@@ -267,9 +268,8 @@ constexpr int kCosetTileBits = 13;
 constexpr int kCosetMinChunkBits = 4;
 constexpr int kCosetMaxRank = kCosetTileBits - kCosetMinChunkBits;
 constexpr int kCosetStages = 3;
-constexpr int kCosetConsumerWarps = 15;
-constexpr int kCosetConsumers = 32 * kCosetConsumerWarps;
-constexpr int kCosetThreads = kCosetConsumers + 32;
+constexpr int kCosetWarps = 16;
+constexpr int kCosetThreads = 32 * kCosetWarps;
 
 struct CosetParams {
   const float2* state;
@@ -370,200 +370,183 @@ __device__ __forceinline__ float coset_x1_sum(uint32_t b4, uint32_t j0, uint32_t
   return a;
 }
 
+// Stage `st` <- the coset of pipeline iteration `item` (one call per thread: its 16-byte
+// pieces k = tid, tid + threads, ..., then an arrive on the stage's full barrier once they
+// have landed).  Slot a of the stage holds the chunk at high index rep ^ slot_hi[a].
+__device__ __forceinline__ void coset_issue(const CosetParams& p, int64_t item, int st, const uint32_t* slot_hi,
+                                            uint64_t* full) {
+  const uint32_t tile = 1u << p.tb;
+  const int64_t b = item / p.cosets;
+  const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
+  const uint32_t pmask = (1u << (p.c - 1)) - 1u;  // 16-byte pieces per chunk, minus one
+  const float2* row = p.state + (static_cast<uint64_t>(b) << p.n);
+  float2* dst = reinterpret_cast<float2*>(coset_stage4) + static_cast<size_t>(st) * tile;
+  for (uint32_t k = threadIdx.x; k < (tile >> 1); k += kCosetThreads) {
+    const uint32_t a = k >> (p.c - 1), off = (k & pmask) << 1;
+    cp_async16(dst + (static_cast<size_t>(a) << p.c) + off,
+               row + (static_cast<uint64_t>(rep ^ slot_hi[a]) << p.c) + off);
+  }
+  cp_async_arrive(&full[st]);
+}
+
 template <bool SEED, int NS>
 __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p) {
-  __shared__ __align__(8) uint64_t full[kCosetStages], empty[kCosetStages];
-  __shared__ uint32_t slot_h[kCosetStages][1 << kCosetMaxRank];
-  __shared__ float red[2][kCosetConsumerWarps][kMaxStringsPerPass];
+  __shared__ __align__(8) uint64_t full[kCosetStages];
+  __shared__ uint32_t slot_hi[1 << kCosetMaxRank];  // sum_k a_k b_k for slot a
+  __shared__ float red[2][kCosetWarps][kMaxStringsPerPass];
   __shared__ int quit;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t tile = 1u << p.tb;
-  float2* const stage0 = reinterpret_cast<float2*>(coset_stage4);
+  for (int a = threadIdx.x; a < (1 << p.r); a += kCosetThreads) {
+    uint32_t h = 0;
+    for (int k = 0; k < p.r; ++k)
+      if ((a >> k) & 1) h ^= p.basis[k];
+    slot_hi[a] = h;
+  }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kCosetStages; ++s) {
-      mbar_init_count(&full[s], 32);  // the producer warp's lanes (cp.async arrive.noinc)
-      mbar_init_count(&empty[s], kCosetConsumerWarps);
-    }
+    for (int st = 0; st < kCosetStages; ++st) mbar_init_count(&full[st], kCosetThreads);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     quit = 0;
   }
   __syncthreads();
   const int64_t total = p.bsz * p.cosets;
   volatile int* vquit = &quit;
-  int last_issued = -1;  // producer: the last pipeline iteration whose loads it issued
-  if (warp == kCosetConsumerWarps) {
-    // ---------------- producer
-    const int nslots = 1 << p.r;
-    const uint32_t pmask = (1u << (p.c - 1)) - 1u;  // 16-byte pieces per chunk, minus one
-    int it = 0;
-    for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
-      const int st = it % kCosetStages;
-      const uint32_t round = static_cast<uint32_t>(it / kCosetStages);
-      if (*vquit) continue;
-      if (round > 0 && !bulk::mbar_wait(&empty[st], (round - 1) & 1u)) {
-        if (lane == 0) {
-          atomicExch(p.status, TQK_TIMEOUT);
-          *vquit = 1;
-        }
-        continue;
-      }
-      const int64_t b = item / p.cosets;
-      const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
-      for (int a = lane; a < nslots; a += 32) {
-        uint32_t h = rep;
-        for (int k = 0; k < p.r; ++k)
-          if ((a >> k) & 1) h ^= p.basis[k];
-        slot_h[st][a] = h;
-      }
-      __syncwarp();
-      // 16-byte cp.async pieces (a warp instruction moves 512 contiguous bytes of one or
-      // two chunks); each lane's copies arrive on the stage's full barrier when complete
-      const float2* row = p.state + (static_cast<uint64_t>(b) << p.n);
-      float2* dst = stage0 + static_cast<size_t>(st) * tile;
-      const uint32_t npieces = tile >> 1;
-      for (uint32_t k = lane; k < npieces; k += 32) {
-        const uint32_t a = k >> (p.c - 1), off = (k & pmask) << 1;
-        cp_async16(dst + (static_cast<size_t>(a) << p.c) + off,
-                   row + (static_cast<uint64_t>(slot_h[st][a]) << p.c) + off);
-      }
-      cp_async_arrive(&full[st]);
-      last_issued = it;
+  // prologue: the first kCosetStages - 1 cosets in flight
+  int64_t issued = 0;  // pipeline iterations whose loads this CTA issued
+  for (; issued < kCosetStages - 1 && blockIdx.x + issued * gridDim.x < total; ++issued)
+    coset_issue(p, blockIdx.x + issued * gridDim.x, static_cast<int>(issued), slot_hi, full);
+  uint32_t xs[NS], gam[NS], odd[NS], kind[NS], hb[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    xs[s] = s < p.ns ? p.xs[s] : 0u;
+    gam[s] = s < p.ns ? p.gam[s] : 0u;
+    odd[s] = s < p.ns ? p.odd[s] : 0u;
+    kind[s] = s < p.ns ? p.kind[s] : 3u;
+    hb[s] = s < p.ns ? p.hb[s] : 0u;
+  }
+  const uint32_t lmask = (1u << p.c) - 1u;
+  int it = 0;
+  for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
+    const int st = it % kCosetStages;
+    // every thread finished reading the stage of iteration it - 1 (the barrier that closed
+    // it): refill it with the coset kCosetStages - 1 iterations ahead
+    const int64_t ahead = item + static_cast<int64_t>(kCosetStages - 1) * gridDim.x;
+    if (ahead < total && *vquit == 0) {
+      coset_issue(p, ahead, static_cast<int>(issued % kCosetStages), slot_hi, full);
+      ++issued;
     }
-  } else {
-    // ---------------- consumers
-    const int ct = threadIdx.x;
-    uint32_t xs[NS], gam[NS], odd[NS], kind[NS], hb[NS];
+    const int64_t b = item / p.cosets;
+    const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
+    uint32_t rho[NS];
+    float cf[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-      xs[s] = s < p.ns ? p.xs[s] : 0u;
-      gam[s] = s < p.ns ? p.gam[s] : 0u;
-      odd[s] = s < p.ns ? p.odd[s] : 0u;
-      kind[s] = s < p.ns ? p.kind[s] : 3u;
-      hb[s] = s < p.ns ? p.hb[s] : 0u;
+      rho[s] = s < p.ns ? ((static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u) : 0u;
+      cf[s] = (SEED && s < p.ns) ? __ldg(p.coef + b * p.m + p.col[s]) : 0.f;
     }
-    const uint32_t lmask = (1u << p.c) - 1u;
-    int it = 0;
-    for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
-      const int st = it % kCosetStages;
-      const uint32_t round = static_cast<uint32_t>(it / kCosetStages);
-      const int64_t b = item / p.cosets;
-      const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
-      uint32_t rho[NS];
-      float cf[NS];
-#pragma unroll
-      for (int s = 0; s < NS; ++s) {
-        rho[s] = s < p.ns ? ((static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u) : 0u;
-        cf[s] = (SEED && s < p.ns) ? __ldg(p.coef + b * p.m + p.col[s]) : 0.f;
+    bool ok = *vquit == 0;
+    if (ok && !bulk::mbar_wait(&full[st], static_cast<uint32_t>(it / kCosetStages) & 1u)) {
+      ok = false;
+      if (lane == 0) {
+        atomicExch(p.status, TQK_TIMEOUT);
+        *vquit = 1;
       }
-      bool ok = *vquit == 0;
-      if (ok && !bulk::mbar_wait(&full[st], round & 1u)) {
-        ok = false;
-        if (lane == 0) {
-          atomicExch(p.status, TQK_TIMEOUT);
-          *vquit = 1;
-        }
-      }
-      const uint32_t b4 = static_cast<uint32_t>(st) * (tile >> 1);  // stage start, float4 units
-      float acc[NS];
+    }
+    const uint32_t b4 = static_cast<uint32_t>(st) * (tile >> 1);  // stage start, float4 units
+    float acc[NS];
 #pragma unroll
-      for (int s = 0; s < NS; ++s) acc[s] = 0.f;
-      if (ok && SEED) {
-        // strings s >= ns are padding (partner = the pair itself, weight 0): every
-        // string's partner load is issued before any arithmetic, with no branch between
-        for (uint32_t q = ct; q < (tile >> 1); q += kCosetConsumers) {
-          const uint32_t u = q << 1;
-          float4 w[NS];
+    for (int s = 0; s < NS; ++s) acc[s] = 0.f;
+    if (ok && SEED) {
+      // strings s >= ns are padding (partner = the pair itself, weight 0): every
+      // string's partner load is issued before any arithmetic, with no branch between
+      for (uint32_t q = threadIdx.x; q < (tile >> 1); q += kCosetThreads) {
+        const uint32_t u = q << 1;
+        float4 w[NS];
 #pragma unroll
-          for (int s = 0; s < NS; ++s) w[s] = coset_stage4[b4 + ((u ^ xs[s]) >> 1)];
-          float2 o0 = make_float2(0.f, 0.f), o1 = o0;
-#pragma unroll
-          for (int s = 0; s < NS; ++s) {
-            const bool sw = (xs[s] & 1u) != 0;
-            const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
-            const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
-            const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);
-            if (odd[s]) {
-              o0.x = fmaf(-c0, b0.y, o0.x);
-              o0.y = fmaf(c0, b0.x, o0.y);
-              o1.x = fmaf(-c1, b1.y, o1.x);
-              o1.y = fmaf(c1, b1.x, o1.y);
-            } else {
-              o0.x = fmaf(c0, b0.x, o0.x);
-              o0.y = fmaf(c0, b0.y, o0.y);
-              o1.x = fmaf(c1, b1.x, o1.x);
-              o1.y = fmaf(c1, b1.y, o1.y);
-            }
-          }
-          float2* dst = p.out + (static_cast<uint64_t>(b) << p.n) +
-                        (static_cast<uint64_t>(slot_h[st][u >> p.c]) << p.c) + (u & lmask);
-          if (p.accumulate) {
-            const float4 old = ld4(dst);
-            o0.x += old.x;
-            o0.y += old.y;
-            o1.x += old.z;
-            o1.y += old.w;
-          }
-          st4(dst, pack4(o0, o1));
-        }
-      } else if (ok) {
-        // expvals: the visits of all strings in a row (tile / 4 pairs per string, tile / 2 for
-        // x = 0 or 1) are cut into one contiguous segment per warp, so a warp takes one or two
-        // strings, each with its orientation and Y parity fixed for the loop.  A pair of
-        // amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the side whose bit
-        // hb (the highest of xs) is clear -- enumerated directly by inserting a zero at hb --
-        // and counted twice (P is Hermitian: both sides contribute the same real part).
-        uint32_t first[NS + 1];
-        first[0] = 0;
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-          first[s + 1] = first[s] + (kind[s] == 3u ? 0u : (kind[s] == 2u ? tile >> 2 : tile >> 1));
-        const uint32_t per = ((first[NS] + kCosetConsumerWarps - 1) / kCosetConsumerWarps + 31u) & ~31u;
-        const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(first[NS], w0 + per);
+        for (int s = 0; s < NS; ++s) w[s] = coset_stage4[b4 + ((u ^ xs[s]) >> 1)];
+        float2 o0 = make_float2(0.f, 0.f), o1 = o0;
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-          const uint32_t lo = max(first[s], w0), hi = min(first[s + 1], w1);
-          if (lo >= hi) continue;  // uniform for the warp
-          const uint32_t j0 = lo - first[s] + lane, j1 = hi - first[s];
-          float a;
-          if (kind[s] == 0u) a = coset_diag_sum(b4, j0, j1, gam[s], rho[s]);
-          else if (kind[s] == 1u) a = 2.f * coset_x1_sum(b4, j0, j1, odd[s] != 0u, gam[s], rho[s]);
-          else if (xs[s] & 1u)
-            a = 2.f * (odd[s] ? coset_string_sum<true, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
-                              : coset_string_sum<true, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
-          else
-            a = 2.f * (odd[s] ? coset_string_sum<false, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
-                              : coset_string_sum<false, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
-          acc[s] = a;
+          const bool sw = (xs[s] & 1u) != 0;
+          const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
+          const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
+          const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);
+          if (odd[s]) {
+            o0.x = fmaf(-c0, b0.y, o0.x);
+            o0.y = fmaf(c0, b0.x, o0.y);
+            o1.x = fmaf(-c1, b1.y, o1.x);
+            o1.y = fmaf(c1, b1.x, o1.y);
+          } else {
+            o0.x = fmaf(c0, b0.x, o0.x);
+            o0.y = fmaf(c0, b0.y, o0.y);
+            o1.x = fmaf(c1, b1.x, o1.x);
+            o1.y = fmaf(c1, b1.y, o1.y);
+          }
         }
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[st]);
-      if (!SEED) {
-        // CTA sum of each string's accumulators: warps in float32, the warps' sums in
-        // float64 in a fixed order; red is double-buffered by item parity
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
-        if (lane == 0)
-#pragma unroll
-          for (int s = 0; s < NS; ++s) red[it & 1][warp][s] = acc[s];
-        asm volatile("bar.sync 1, %0;" ::"n"(kCosetConsumers) : "memory");
-        if (warp == 0 && lane < p.ns) {
-          double sum = 0.0;
-          for (int w = 0; w < kCosetConsumerWarps; ++w) sum += static_cast<double>(red[it & 1][w][lane]);
-          p.partial[item * kMaxStringsPerPass + lane] = (*vquit == 0) ? sum : __longlong_as_double(0x7ff8000000000000ll);
+        float2* dst = p.out + (static_cast<uint64_t>(b) << p.n) +
+                      (static_cast<uint64_t>(rep ^ slot_hi[u >> p.c]) << p.c) + (u & lmask);
+        if (p.accumulate) {
+          const float4 old = ld4(dst);
+          o0.x += old.x;
+          o0.y += old.y;
+          o1.x += old.z;
+          o1.y += old.w;
         }
+        st4(dst, pack4(o0, o1));
       }
+    } else if (ok) {
+      // expvals: the visits of all strings in a row (tile / 4 pairs per string, tile / 2 for
+      // x = 0 or 1) are cut into one contiguous segment per warp, so a warp takes one or two
+      // strings, each with its orientation and Y parity fixed for the loop.  A pair of
+      // amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the side whose bit
+      // hb (the highest of xs) is clear -- enumerated directly by inserting a zero at hb --
+      // and counted twice (P is Hermitian: both sides contribute the same real part).
+      uint32_t first[NS + 1];
+      first[0] = 0;
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+        first[s + 1] = first[s] + (kind[s] == 3u ? 0u : (kind[s] == 2u ? tile >> 2 : tile >> 1));
+      const uint32_t per = ((first[NS] + kCosetWarps - 1) / kCosetWarps + 31u) & ~31u;
+      const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(first[NS], w0 + per);
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        const uint32_t lo = max(first[s], w0), hi = min(first[s + 1], w1);
+        if (lo >= hi) continue;  // uniform for the warp
+        const uint32_t j0 = lo - first[s] + lane, j1 = hi - first[s];
+        float a;
+        if (kind[s] == 0u) a = coset_diag_sum(b4, j0, j1, gam[s], rho[s]);
+        else if (kind[s] == 1u) a = 2.f * coset_x1_sum(b4, j0, j1, odd[s] != 0u, gam[s], rho[s]);
+        else if (xs[s] & 1u)
+          a = 2.f * (odd[s] ? coset_string_sum<true, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
+                            : coset_string_sum<true, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
+        else
+          a = 2.f * (odd[s] ? coset_string_sum<false, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
+                            : coset_string_sum<false, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
+        acc[s] = a;
+      }
+    }
+    if (!SEED) {
+      // CTA sum of each string's accumulators: warps in float32, the warps' sums in
+      // float64 in a fixed order; red is double-buffered by item parity
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+      if (lane == 0)
+#pragma unroll
+        for (int s = 0; s < NS; ++s) red[it & 1][warp][s] = acc[s];
+    }
+    __syncthreads();  // the stage is read: the next iteration may refill it
+    if (!SEED && warp == 0 && lane < p.ns) {
+      double sum = 0.0;
+      for (int w = 0; w < kCosetWarps; ++w) sum += static_cast<double>(red[it & 1][w][lane]);
+      p.partial[item * kMaxStringsPerPass + lane] = (*vquit == 0) ? sum : __longlong_as_double(0x7ff8000000000000ll);
     }
   }
-  __syncthreads();
   // after a timeout, wait (bounded) for this CTA's copies still in flight before exiting
-  if (quit && warp == kCosetConsumerWarps && lane == 0) {
-    for (int st = 0; st < kCosetStages; ++st) {
-      const int last = last_issued - ((last_issued - st) % kCosetStages + kCosetStages) % kCosetStages;
-      if (last >= 0) bulk::mbar_wait(&full[st], static_cast<uint32_t>(last / kCosetStages) & 1u);
-    }
+  if (quit && threadIdx.x == 0) {
+    for (int64_t k = issued - (kCosetStages - 1); k < issued; ++k)
+      if (k >= 0) bulk::mbar_wait(&full[k % kCosetStages], static_cast<uint32_t>(k / kCosetStages) & 1u);
   }
 }
 
