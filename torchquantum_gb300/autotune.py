@@ -232,6 +232,10 @@ def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool,
     return total, tc_flags
 
 
+WIDE_BEAM = 32
+WIDE_BEAM_MIN_AMPS = 1 << 27
+
+
 def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: torch.device, tc_ok: bool,
                   with_adjoint: bool, widths: Sequence[int] = (4, 5, 6), stored: bool = False):
     """(plan, per-block tensor-core flags, chosen width, cost table) for a segment: the
@@ -248,9 +252,14 @@ def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: to
         costs = {"dense": {str(k): (1.0 + 0.25 * k, 2.0 + 0.5 * k) for k in range(1, 7)},
                  "tc": (1.0, 2.0, 1.5) if tc_ok else None, "rows": 0}
     best = None
+    # on large states (a pass of >= 1 GiB) a width-32 beam is tried too for 6-wire blocks:
+    # it plans once per circuit structure (about 1 s for 400 gates, memoised) and finds a
+    # block or two fewer per 400 gates, each worth a full forward and reverse pass
+    wide = (bsz << n) >= WIDE_BEAM_MIN_AMPS and len(wire_lists) <= fusion.BEAM_MAX_GATES
     for k in widths:
         k = max(1, min(k, n, 6))
-        for look, beam in ((0, 0), (8, 0), (8, 4)):
+        variants = ((0, 0), (8, 0), (8, 4)) + (((8, WIDE_BEAM),) if wide and k == 6 else ())
+        for look, beam in variants:
             plan = fusion.plan_cached(wire_lists, k, look, beam)
             cost, flags = plan_cost(plan, costs, tc_ok, with_adjoint, stored)
             if best is None or cost < best[0]:
