@@ -619,7 +619,7 @@ def run_ours(args):
             e0.record(stream)
             for _ in range(args.steps):
                 th.grad = None
-                step(th)
+                ev_main, _ = step(th)
             e1.record(stream)
             torch.cuda.synchronize()
     finally:
@@ -643,9 +643,11 @@ def run_ours(args):
 
     _lib.check_status(dev)
     if args.method == "fused" and not args.quick and not args.no_plain:
+        g_main, ev_main = th.grad.detach().clone(), ev_main.detach().clone()
         # ---------------- the same fused step with the in-place reverse sweep (O(1) extra
         # states), and the plain method: with staged low-qubit runs (its default) and
         # strictly gate by gate
+        variant_out = {}
         for variant, key in (("fused_in_place", "fused_adjoint_in_place"), ("plain", "plain_method"),
                              ("plain_gate_by_gate", "plain_gate_by_gate")):
             for _ in range(2):
@@ -658,9 +660,10 @@ def run_ours(args):
             e0.record(stream)
             for _ in range(args.steps):
                 th.grad = None
-                step(th, variant)
+                ev_v, _ = step(th, variant)
             e1.record(stream)
             torch.cuda.synchronize()
+            variant_out[key] = (th.grad.detach().clone(), ev_v.detach().clone())
             ms_plain = R.max_over_ranks(e0.elapsed_time(e1), dev)
             v_plain = R.job_throughput(bsz * args.steps, world, ms_plain / 1e3)
             line[key] = {"value": v_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
@@ -670,6 +673,16 @@ def run_ours(args):
         line["fused_speedup_vs_plain_staged"] = value / line["plain_method"]["value"]
         line["fused_adjoint_in_place"]["speedup_vs_plain"] = \
             line["fused_adjoint_in_place"]["value"] / line["plain_gate_by_gate"]["value"]
+        # the timed step's outputs against the plain gate-by-gate adjoint sweep on the same
+        # angles (complex64 throughout; the complex128 central-difference check of the same
+        # workload is a test, since it takes minutes)
+        g_ref, ev_ref = variant_out["plain_gate_by_gate"]
+        line["max_err"] = {"reference": "plain gate-by-gate adjoint sweep, same angles",
+                           "grad_max_abs": float(g_ref.abs().max()),
+                           "grad": float((g_main - g_ref).abs().max()),
+                           "expval": float((ev_main - ev_ref).abs().max()),
+                           "grad_fused_in_place": float((variant_out["fused_adjoint_in_place"][0] - g_ref).abs().max()),
+                           "grad_plain_staged": float((variant_out["plain_method"][0] - g_ref).abs().max())}
     if not args.quick:
         # ---------------- end to end through the public API with host buffers
         pin_theta = torch.from_numpy(theta_host).pin_memory()
@@ -916,6 +929,13 @@ def roofline(args, dev, stored=True, live=None):
         t = timeit(fn)
         gbs = nbytes / t / 1e9
         res[name] = {"us": t * 1e6, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak}
+    # CZ touches a quarter of the amplitudes; where one of its wires is among the two lowest
+    # address bits, every touched 32-byte sector is only partly used (DRAM moves whole
+    # sectors): the same pass on the bytes of the sectors it touches
+    sec = np.mean([1.0 if max(bb) < 2 else (0.5 if min(bb) < 2 else 0.25)
+                   for bb in ([n - 1 - w for w in pairs[i]] for i in range(reps))])
+    res["cz_fwd"]["sector_bytes"] = int(2 * S * sec)
+    res["cz_fwd"]["frac_sector_bytes"] = 2 * S * sec / (res["cz_fwd"]["us"] / 1e6) / 1e9 / peak
     for name in ("expval8", "apply_sum8"):
         res[name]["passes"] = _lib.expval_passes(xs, n) if name == "expval8" else len(_lib.coset_groups(xs, n))
         # shared-memory reads of the coset passes: own pair + one partner pair per string

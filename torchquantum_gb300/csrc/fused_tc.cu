@@ -318,6 +318,9 @@ __device__ __forceinline__ int64_t tile_base(const TcParams& p, int64_t t, bool 
 #define TQK_TC_PREFETCH 1
 #endif
 constexpr int kPrefetchTiles = TQK_TC_PREFETCH;
+#ifndef TQK_TC_EARLY_LOAD
+#define TQK_TC_EARLY_LOAD 1
+#endif
 
 // Registers r whose amplitude starts a 128-byte line (16 amplitudes).  Address bits 0-3
 // are always tile dimensions (target bits or among the lowest non-target bits) and are
@@ -337,12 +340,15 @@ __device__ __forceinline__ void prefetch_lines(const TcParams& p, const float2* 
     if ((mask >> r) & 1u) asm volatile("prefetch.global.L2 [%0];" ::"l"(src + p.reg_off[r]));
 }
 
-// Producer: load the thread's 32 amplitudes of tile t, split them into bf16 hi/lo and
-// store its four 16-byte chunks (K = 64p + 8g + e) into the A image.
-__device__ __forceinline__ void produce_tile(const TcParams& p, const float2* src, uint8_t* abuf, int row0, int g0) {
-  float2 a[32];
+// Producer: the thread's 32 amplitudes of a tile (load_tile), split into bf16 hi/lo and
+// stored as its four 16-byte chunks (K = 64p + 8g + e) of the A image (store_tile).
+__device__ __forceinline__ void load_tile(const TcParams& p, const float2* src, float2 (&a)[32]) {
 #pragma unroll
   for (int r = 0; r < 32; ++r) a[r] = src[p.reg_off[r]];
+}
+
+__device__ __forceinline__ void store_tile(const float2 (&a)[32], const TcParams& p, uint8_t* abuf, int row0,
+                                           int g0) {
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const int row = row0 + p.c_row[c], g = g0 + p.c_g[c];
@@ -493,8 +499,18 @@ __global__ void __launch_bounds__(kThreadsWS, 1) k_tc(const TcParams p) {
       const int buf = static_cast<int>(k % kABufs);
       if (kPrefetchTiles > 0 && k + kPrefetchTiles < ntiles)
         prefetch_lines(p, base + tile_base(p, t_begin + k + kPrefetchTiles, ADJ) + toff, pf_mask);
+      // the tile's loads are issued before the wait for its buffer, so their latency
+      // overlaps the MMA that still reads the buffer (tiles are disjoint: nothing this
+      // kernel writes is read here)
+      float2 a[32];
+#if TQK_TC_EARLY_LOAD
+      load_tile(p, base + tile_base(p, t_begin + k, ADJ) + toff, a);
+#endif
       if (k >= kABufs && !wait_or_abort(&sy->a_empty[buf], static_cast<uint32_t>((k / kABufs - 1) & 1), sy)) break;
-      produce_tile(p, base + tile_base(p, t_begin + k, ADJ) + toff, abufs + buf * 2 * kImgBytes, row0, g0);
+#if !TQK_TC_EARLY_LOAD
+      load_tile(p, base + tile_base(p, t_begin + k, ADJ) + toff, a);
+#endif
+      store_tile(a, p, abufs + buf * 2 * kImgBytes, row0, g0);
       fence_proxy_async();
       mbar_arrive(&sy->a_full[buf]);
     }
