@@ -136,15 +136,33 @@ class Segment:
         # ---- native gate operands (one launch)
         natives = [r for r in records if isinstance(r, NativeGate)]
         self.natives = natives
-        sizes = [operand_size(g.type_id) * g.batch for g in natives]
-        total = sum(sizes)
+        # operands laid out by shape: the natives of one operand shape are consecutive, so
+        # their views come from one view + unbind per shape instead of per-gate slicing
+        shapes = [_operand_shape(g, operand_size(g.type_id)) for g in natives]
+        by_shape: Dict[tuple, List[int]] = {}
+        for i, shp in enumerate(shapes):
+            by_shape.setdefault(shp, []).append(i)
+        offsets = [0] * len(natives)
+        total = 0
+        for shp, idx in by_shape.items():
+            numel = int(np.prod(shp))
+            for i in idx:
+                offsets[i] = total
+                total += numel
         self.op128 = torch.empty(max(total, 1), dtype=torch.complex128, device=dev)
         self.op64 = torch.empty(max(total, 1), dtype=torch.complex64, device=dev)
-        self.gate_offsets = []
+        views64, views128 = [None] * len(natives), [None] * len(natives)
+        for shp, idx in by_shape.items():
+            a, cnt = offsets[idx[0]], len(idx)
+            size = cnt * int(np.prod(shp))
+            for i, v64, v128 in zip(idx, self.op64[a:a + size].view(cnt, *shp).unbind(0),
+                                    self.op128[a:a + size].view(cnt, *shp).unbind(0)):
+                views64[i], views128[i] = v64, v128
+        self.gate_offsets = offsets
         descs = []
-        off = 0
         self._keep = []
-        for g, sz in zip(natives, sizes):
+        p64, p128 = self.op64.data_ptr(), self.op128.data_ptr()
+        for g, off in zip(natives, offsets):
             p = g.params
             d = GateDesc()
             d.type, d.inverse, d.batch, d.nparam = g.type_id, int(g.inverse), g.batch, g.nparam
@@ -152,11 +170,9 @@ class Segment:
             d.p_row_stride = p.stride(0) if g.batch > 1 else 0
             d.p_col_stride = p.stride(1)
             d.p_is_double = int(p.dtype == torch.float64)
-            d.op128 = self.op128.data_ptr() + 16 * off
-            d.op64 = self.op64.data_ptr() + 8 * off
-            self.gate_offsets.append(off)
+            d.op128 = p128 + 16 * off
+            d.op64 = p64 + 8 * off
             descs.append(d)
-            off += sz
         self.gate_descs = descs
         if descs:
             table, host = _to_device_table(descs, dev)
@@ -167,13 +183,10 @@ class Segment:
         gi = 0
         for r in records:
             if isinstance(r, NativeGate):
-                o = self.gate_offsets[gi]
-                sz = operand_size(r.type_id)
-                shape = _operand_shape(r, sz)
                 op = engine.TapeOp(r.kind, r.wires, controls=r.wires[:r.nctrl], targets=r.wires[r.nctrl:],
-                                   operand=self.op64[o:o + sz * r.batch].view(shape))
+                                   operand=views64[gi])
                 op.native = r
-                op.op128 = self.op128[o:o + sz * r.batch].view(shape)
+                op.op128 = views128[gi]
                 gi += 1
             else:
                 op = r
@@ -516,8 +529,15 @@ class Segment:
         # operand cotangents -> parameter gradients
         grads = []
         if self.natives and self.bases:
-            gbufs = {k: torch.zeros_like(b, dtype=torch.float64) for k, (b, _) in self.bases.items()}
+            # one float64 buffer for every base tensor's gradient (each base's part laid out
+            # like the base's own storage), one conversion back to the bases' dtype
+            bases = [b for b, _ in self.bases.values()]
+            spans = [max(0, sum((sz - 1) * st for sz, st in zip(b.shape, b.stride()))) + 1 for b in bases]
+            starts = np.cumsum([0] + spans[:-1]).tolist()
+            flat = torch.zeros(max(sum(spans), 1), dtype=torch.float64, device=dev)
+            start_of = {k: st for k, st in zip(self.bases.keys(), starts)}
             descs = []
+            fp = flat.data_ptr()
             for g, d, off in zip(self.natives, self.gate_descs, self.gate_offsets):
                 if not g.params.requires_grad:
                     continue
@@ -526,14 +546,18 @@ class Segment:
                 nd.op128 = None
                 nd.op64 = None
                 nd.op_grad = opg.data_ptr() + 16 * off
-                nd.grad = gbufs[id(base)].data_ptr() + 8 * eoff
+                nd.grad = fp + 8 * (start_of[id(base)] + eoff)
                 descs.append(nd)
             if descs:
                 table, host = _to_device_table(descs, dev)
                 _lib.param_grads(table, len(descs), dev)
                 self._keep_pg = [table, host]
-            for key, (base, _) in self.bases.items():
-                grads.append(gbufs[key].to(base.dtype))
+            dtypes = {b.dtype for b in bases}
+            conv = flat.to(bases[0].dtype) if len(dtypes) == 1 else None
+            for b, st in zip(bases, starts):
+                src = conv if conv is not None else flat
+                gb = src.as_strided(b.shape, b.stride(), st)
+                grads.append(gb if conv is not None else gb.to(b.dtype))
         else:
             grads += [None] * len(self.bases)
         for op in self.generic_sources:
