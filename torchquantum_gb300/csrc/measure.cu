@@ -389,6 +389,46 @@ __device__ __forceinline__ void coset_issue(const CosetParams& p, int64_t item, 
   cp_async_arrive(&full[st]);
 }
 
+// Backward seed, one string over a thread's output pairs of a staged coset: pair k is
+// q0 + k * kCosetThreads (local index u = 2q), its partner pair (q ^ x4) in the stage.  The
+// sign (-1)^popcount(u & gam) splits into the thread's part (bits of 2 q0, folded into cft)
+// and the part from k * 2 kCosetThreads, the same for every thread; SW: x odd (the partner
+// pair is in swapped order); ODD: odd number of Y factors.
+constexpr int kSeedPairs = (1 << kCosetTileBits) / 2 / kCosetThreads;
+
+template <bool SW, bool ODD, bool FULL>
+__device__ __forceinline__ void seed_string(float2 (&o)[kSeedPairs][2], uint32_t b4, uint32_t q0, uint32_t npairs,
+                                            uint32_t x4, uint32_t gam, float cft) {
+  const uint32_t g1 = gam & 1u;
+  // FULL (tiles of 2^13 amplitudes): every thread has all its pairs, so the loads of all
+  // of them can be issued before the first product
+  float4 w[kSeedPairs];
+#pragma unroll
+  for (int k = 0; k < kSeedPairs; ++k) {
+    const uint32_t q = q0 + static_cast<uint32_t>(k) * kCosetThreads;
+    w[k] = (FULL || q < npairs) ? coset_stage4[b4 + (q ^ x4)] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int k = 0; k < kSeedPairs; ++k) {
+    const uint32_t q = q0 + static_cast<uint32_t>(k) * kCosetThreads;
+    if (!FULL && q >= npairs) break;  // tiles of fewer than 2^13 amplitudes
+    const uint32_t up = static_cast<uint32_t>(__popc((static_cast<uint32_t>(k) * 2u * kCosetThreads) & gam));
+    const float c0 = flip_if_odd(cft, up), c1 = flip_if_odd(cft, up + g1);
+    const float2 b0 = SW ? hi2(w[k]) : lo2(w[k]), b1 = SW ? lo2(w[k]) : hi2(w[k]);
+    if (ODD) {
+      o[k][0].x = fmaf(-c0, b0.y, o[k][0].x);
+      o[k][0].y = fmaf(c0, b0.x, o[k][0].y);
+      o[k][1].x = fmaf(-c1, b1.y, o[k][1].x);
+      o[k][1].y = fmaf(c1, b1.x, o[k][1].y);
+    } else {
+      o[k][0].x = fmaf(c0, b0.x, o[k][0].x);
+      o[k][0].y = fmaf(c0, b0.y, o[k][0].y);
+      o[k][1].x = fmaf(c1, b1.x, o[k][1].x);
+      o[k][1].y = fmaf(c1, b1.y, o[k][1].y);
+    }
+  }
+}
+
 template <bool SEED, int NS>
 __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p) {
   __shared__ __align__(8) uint64_t full[kCosetStages];
@@ -438,12 +478,9 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
     const int64_t b = item / p.cosets;
     const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
     uint32_t rho[NS];
-    float cf[NS];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-      rho[s] = s < p.ns ? ((static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u) : 0u;
-      cf[s] = (SEED && s < p.ns) ? __ldg(p.coef + b * p.m + p.col[s]) : 0.f;
-    }
+    for (int s = 0; s < NS; ++s)
+      rho[s] = (!SEED && s < p.ns) ? ((static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u) : 0u;
     bool ok = *vquit == 0;
     if (ok && !bulk::mbar_wait(&full[st], static_cast<uint32_t>(it / kCosetStages) & 1u)) {
       ok = false;
@@ -457,34 +494,40 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
 #pragma unroll
     for (int s = 0; s < NS; ++s) acc[s] = 0.f;
     if (ok && SEED) {
-      // strings s >= ns are padding (partner = the pair itself, weight 0): every
-      // string's partner load is issued before any arithmetic, with no branch between
-      for (uint32_t q = threadIdx.x; q < (tile >> 1); q += kCosetThreads) {
-        const uint32_t u = q << 1;
-        float4 w[NS];
+      // string by string over the thread's output pairs (outputs in registers), then one
+      // store per pair; each string's orientation and Y parity are fixed for its loop
+      const uint32_t npairs = tile >> 1, q0 = threadIdx.x;
+      float2 o[kSeedPairs][2];
 #pragma unroll
-        for (int s = 0; s < NS; ++s) w[s] = coset_stage4[b4 + ((u ^ xs[s]) >> 1)];
-        float2 o0 = make_float2(0.f, 0.f), o1 = o0;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-          const bool sw = (xs[s] & 1u) != 0;
-          const float2 b0 = sw ? hi2(w[s]) : lo2(w[s]), b1 = sw ? lo2(w[s]) : hi2(w[s]);
-          const uint32_t pb = static_cast<uint32_t>(__popc(u & gam[s])) + rho[s];
-          const float c0 = flip_if_odd(cf[s], pb), c1 = flip_if_odd(c0, gam[s] & 1u);
-          if (odd[s]) {
-            o0.x = fmaf(-c0, b0.y, o0.x);
-            o0.y = fmaf(c0, b0.x, o0.y);
-            o1.x = fmaf(-c1, b1.y, o1.x);
-            o1.y = fmaf(c1, b1.x, o1.y);
-          } else {
-            o0.x = fmaf(c0, b0.x, o0.x);
-            o0.y = fmaf(c0, b0.y, o0.y);
-            o1.x = fmaf(c1, b1.x, o1.x);
-            o1.y = fmaf(c1, b1.y, o1.y);
-          }
+      for (int k = 0; k < kSeedPairs; ++k) o[k][0] = o[k][1] = make_float2(0.f, 0.f);
+#pragma unroll 1
+      for (int s = 0; s < p.ns; ++s) {
+        const uint32_t x = p.xs[s], gam_s = p.gam[s];
+        const uint32_t rho_s = (static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u;
+        const float cft = flip_if_odd(__ldg(p.coef + b * p.m + p.col[s]),
+                                      static_cast<uint32_t>(__popc((q0 << 1) & gam_s)) + rho_s);
+        const uint32_t x4 = x >> 1;
+        const int variant = ((x & 1u) ? 2 : 0) + (p.odd[s] ? 1 : 0);
+        if (npairs == static_cast<uint32_t>(kSeedPairs * kCosetThreads)) {
+          if (variant == 3) seed_string<true, true, true>(o, b4, q0, npairs, x4, gam_s, cft);
+          else if (variant == 2) seed_string<true, false, true>(o, b4, q0, npairs, x4, gam_s, cft);
+          else if (variant == 1) seed_string<false, true, true>(o, b4, q0, npairs, x4, gam_s, cft);
+          else seed_string<false, false, true>(o, b4, q0, npairs, x4, gam_s, cft);
+        } else {
+          if (variant == 3) seed_string<true, true, false>(o, b4, q0, npairs, x4, gam_s, cft);
+          else if (variant == 2) seed_string<true, false, false>(o, b4, q0, npairs, x4, gam_s, cft);
+          else if (variant == 1) seed_string<false, true, false>(o, b4, q0, npairs, x4, gam_s, cft);
+          else seed_string<false, false, false>(o, b4, q0, npairs, x4, gam_s, cft);
         }
+      }
+#pragma unroll
+      for (int k = 0; k < kSeedPairs; ++k) {
+        const uint32_t q = q0 + static_cast<uint32_t>(k) * kCosetThreads;
+        if (q >= npairs) break;
+        const uint32_t u = q << 1;
         float2* dst = p.out + (static_cast<uint64_t>(b) << p.n) +
                       (static_cast<uint64_t>(rep ^ slot_hi[u >> p.c]) << p.c) + (u & lmask);
+        float2 o0 = o[k][0], o1 = o[k][1];
         if (p.accumulate) {
           const float4 old = ld4(dst);
           o0.x += old.x;
