@@ -436,6 +436,8 @@ class Segment:
                 row += b.block_batch
         cross_jobs, recs, keep, stored_at = [], [], [], {}
         zero_block = None
+        # a native gate's cotangent slot: the place of its operand in op128, inside opg
+        dopg = opg.data_ptr() - self.op128.data_ptr() if opg is not None else 0
         for op in self.exec_ops:  # forward order; the runner walks it backwards
             if isinstance(op, StagedRun):
                 slots = []
@@ -443,7 +445,7 @@ class Segment:
                     slot = None
                     if need_grads:
                         if hasattr(m, "native") and m.native.params.requires_grad:
-                            slot = _as_real(opg, m.op128, self.op128)
+                            slot = m.op128.data_ptr() + dopg
                         elif id(m) in gslots:
                             slot = torch.view_as_real(gslots[id(m)]).view(-1)
                     slots.append(slot)
@@ -478,7 +480,7 @@ class Segment:
             slot = None
             if need_grads:
                 if hasattr(op, "native") and op.native.params.requires_grad:
-                    slot = _as_real(opg, op.op128, self.op128)
+                    slot = op.op128.data_ptr() + dopg
                 elif id(op) in gslots:
                     slot = torch.view_as_real(gslots[id(op)]).view(-1)
             recs.append(_plain_record(op, slot))
@@ -571,7 +573,7 @@ _PLAIN_KIND = {engine.KIND_DENSE: _lib.X_DENSE, engine.KIND_CTRL: _lib.X_CTRL, e
 
 def _exec(kind: int, wires, nctrl: int = 0, ctrl_val: int = 1, batch: int = 1, operand=None, uncompute=None,
           image=None, image_h=None, u=None, grad=None, mr=None) -> "_lib.ExecOp":
-    """One ``tqk_exec_op`` record (tensors by their device address)."""
+    """One ``tqk_exec_op`` record (tensors, or device addresses as ints)."""
     r = _lib.ExecOp()
     r.kind, r.nw, r.nctrl, r.ctrl_val, r.batch = kind, len(wires), nctrl, ctrl_val, batch
     if len(wires) > len(r.wires):
@@ -581,7 +583,7 @@ def _exec(kind: int, wires, nctrl: int = 0, ctrl_val: int = 1, batch: int = 1, o
     for name, t in (("operand", operand), ("uncompute", uncompute), ("image", image), ("image_h", image_h),
                     ("u", u), ("grad", grad), ("mr", mr)):
         if t is not None:
-            setattr(r, name, t.data_ptr())
+            setattr(r, name, t if isinstance(t, int) else t.data_ptr())
     return r
 
 
@@ -663,7 +665,7 @@ class StagedRun:
             else:
                 d.batch = 1
             g = grads[i] if grads is not None else None
-            d.grad = g.data_ptr() if g is not None else None
+            d.grad = None if g is None else (g if isinstance(g, int) else g.data_ptr())
             out.append(d)
         return out
 
