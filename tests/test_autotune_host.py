@@ -52,13 +52,14 @@ def test_choose_fusion_picks_cheapest_candidate(monkeypatch):
     assert k == 6 and all(flags[i] for i, (_, idx) in enumerate(plan) if len(idx) > 1)
     costs = _fake_costs(1.0, 2.0, 5.0)
     cands = [F.plan_cached(wl, kk, la, bm) for kk in (4, 5, 6) for la, bm in ((0, 0), (8, 0), (8, 4))]
-    # 16 x 2^24 amplitudes: the width-32 beam is a candidate for 6-wire blocks as well
-    wide = F.plan_cached(wl, 6, 8, A.WIDE_BEAM)
-    _check_legal(wl, wide, 6)
-    best = min(A.plan_cost(c, costs, True, True)[0] for c in cands + [wide])
+    # 16 x 2^24 amplitudes: the wide beams are candidates for 6-wire blocks as well
+    wide = [F.plan_cached(wl, 6, la, bm) for la, bm in A.WIDE_BEAMS]
+    for w in wide:
+        _check_legal(wl, w, 6)
+        assert len(w) <= len(F.plan_cached(wl, 6, 8, 4))
+    best = min(A.plan_cost(c, costs, True, True)[0] for c in cands + wide)
     assert A.plan_cost(plan, costs, True, True)[0] == best
     assert best <= A.plan_cost(F.plan_blocks(wl, 6), costs, True, True)[0]
-    assert len(wide) <= len(F.plan_cached(wl, 6, 8, 4))
     # a small state (16 x 2^20 amplitudes) keeps the three cheaper candidates only
     plan_s, _, _, _ = A.choose_fusion(wl, 20, 16, None, True, True)
     assert any(plan_s is F.plan_cached(wl, kk, la, bm) for kk in (4, 5, 6) for la, bm in ((0, 0), (8, 0), (8, 4)))

@@ -232,7 +232,8 @@ def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool,
     return total, tc_flags
 
 
-WIDE_BEAM = 32
+# (lookahead, beam width) of the wide beams tried for 6-wire blocks on large states
+WIDE_BEAMS = ((8, 32), (16, 128))
 WIDE_BEAM_MIN_AMPS = 1 << 27
 
 
@@ -252,13 +253,14 @@ def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: to
         costs = {"dense": {str(k): (1.0 + 0.25 * k, 2.0 + 0.5 * k) for k in range(1, 7)},
                  "tc": (1.0, 2.0, 1.5) if tc_ok else None, "rows": 0}
     best = None
-    # on large states (a pass of >= 1 GiB) a width-32 beam is tried too for 6-wire blocks:
-    # it plans once per circuit structure (about 1 s for 400 gates, memoised) and finds a
-    # block or two fewer per 400 gates, each worth a full forward and reverse pass
+    # on large states (a pass of >= 1 GiB) wide beams are tried too for 6-wire blocks
+    # (width 32, and width 128 with a 16-gate front): they plan once per circuit structure
+    # (about 1 s and 4-6 s for 400 gates, memoised) and find one to three blocks fewer per
+    # 400 gates, each worth a full forward and reverse pass
     wide = (bsz << n) >= WIDE_BEAM_MIN_AMPS and len(wire_lists) <= fusion.BEAM_MAX_GATES
     for k in widths:
         k = max(1, min(k, n, 6))
-        variants = ((0, 0), (8, 0), (8, 4)) + (((8, WIDE_BEAM),) if wide and k == 6 else ())
+        variants = ((0, 0), (8, 0), (8, 4)) + (WIDE_BEAMS if wide and k == 6 else ())
         for look, beam in variants:
             plan = fusion.plan_cached(wire_lists, k, look, beam)
             cost, flags = plan_cost(plan, costs, tc_ok, with_adjoint, stored)

@@ -645,8 +645,28 @@ class StagedRun:
         self.wires = sorted({w for o in ops for w in o.wires})
 
     def descs(self, grads=None):
+        """The run's ``tqk_staged_op`` records; ``grads``: per-op cotangent slots (tensor,
+        device address or None) for the reverse pass.  The records without slots are built
+        once per run (operands do not move) and copied when slots are set."""
+        base = getattr(self, "_descs", None)
+        if base is None:
+            base = self._build_descs()
+            self._descs = base
+        if grads is None:
+            return base
         out = []
-        for i, o in enumerate(self.ops):
+        for d, g in zip(base, grads):
+            if g is None:
+                out.append(d)
+                continue
+            e = _lib.StagedOp.from_buffer_copy(d)
+            e.grad = g if isinstance(g, int) else g.data_ptr()
+            out.append(e)
+        return out
+
+    def _build_descs(self):
+        out = []
+        for o in self.ops:
             d = _lib.StagedOp()
             if o.kind == engine.KIND_X:
                 ws, d.kind, d.ctrl_val = o.controls + o.targets, _lib.S_X, o.ctrl_val
@@ -664,8 +684,7 @@ class StagedRun:
                 d.batch = int(o.operand.shape[0])
             else:
                 d.batch = 1
-            g = grads[i] if grads is not None else None
-            d.grad = None if g is None else (g if isinstance(g, int) else g.data_ptr())
+            d.grad = None
             out.append(d)
         return out
 
