@@ -44,6 +44,28 @@ def test_plan_cost_picks_cheaper_kernel():
     assert flags == [False, False, False]
 
 
+def test_lone_dense_gate_may_run_as_tensor_core_block():
+    """A gate alone in its block keeps its own kernel unless it is a dense / controlled gate
+    and a tensor-core block costs less than its dense pass with a cotangent; structured
+    lone gates are costed with the measured light pass."""
+    plan = [([0, 1, 2, 3, 4, 5], [0, 1, 2]), ([1, 2], [3]), ([7], [4]), ([0] * 30, [5])]
+    costs = {"dense": {str(k): (1.0, 4.0) for k in range(1, 7)}, "tc": (0.7, 1.4, 1.1), "rows": 1}
+    c, flags = A.plan_cost(plan, costs, True, True, stored=True)
+    assert flags == [True, False, False, False] and abs(c - (1.8 + 3 * 5.0)) < 1e-12
+    D, L, O = A.LONE_DENSE, A.LONE_LIGHT, A.LONE_OTHER
+    lone = [D, D, D, D, L, O]
+    c, flags = A.plan_cost(plan, costs, True, True, stored=True, lone_kind=lone)
+    # gate 3 (dense, 2 wires) runs as a block; gate 4 (light) keeps its kernel, costed as a
+    # dense pass while no light cost was measured; the 30-wire barrier op never is a block
+    assert flags == [True, True, False, False] and abs(c - (1.8 + 1.8 + 5.0 + 5.0)) < 1e-12
+    costs["light"] = (0.4, 0.8)
+    c, flags = A.plan_cost(plan, costs, True, True, stored=True, lone_kind=lone)
+    assert flags == [True, True, False, False] and abs(c - (1.8 + 1.8 + 1.2 + 5.0)) < 1e-12
+    # without tensor cores the dense lone gate keeps its own kernel
+    c, flags = A.plan_cost(plan, costs, False, True, stored=True, lone_kind=lone)
+    assert flags == [False] * 4 and abs(c - (5.0 + 5.0 + 1.2 + 5.0)) < 1e-12
+
+
 def test_choose_fusion_picks_cheapest_candidate(monkeypatch):
     gates, _ = W.random_circuit(24, 200, seed=0)
     wl = [g["wires"] for g in gates]

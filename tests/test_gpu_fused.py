@@ -254,7 +254,7 @@ def test_autotuned_fusion_vs_oracle(tmp_path, monkeypatch):
     ref = O.run(n, bsz, W.oracle_gates(gates, theta))
     assert np.abs(res["fused"][0] - ref).max() < 1e-5
     assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-5
-    assert any(k.startswith("fusion2|") for k in A._MEM)
+    assert any(k.startswith("fusion3|") for k in A._MEM)
     A.clear()
 
 

@@ -153,12 +153,13 @@ SCRATCH_AMPS = 1 << 27   # cost probes run on at most 2^27 amplitudes (1 GiB) pe
 
 def pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool) -> dict:
     """Measured milliseconds per pass over a [bsz, 2^n] state: ``dense[k] = (fwd, adj)``
-    for the CUDA-core dense k-wire kernels (k = 1..min(6, n)) and ``tc = (fwd, adj,
-    adj_stored)`` for the tensor-core 6-wire block kernel (if ``tc_ok``; adj_stored: the
-    reverse step that reads the block's stored input).  Probes use min(bsz, rows that
-    fit 2^27 amplitudes) rows and are scaled to bsz (the kernels stream rows
-    independently)."""
-    key = f"fusion2|{gpu_key(dev)}|n{n}|b{bsz}|tc{int(tc_ok)}"
+    for the CUDA-core dense k-wire kernels (k = 1..min(6, n)), ``light = (fwd, adj)`` for a
+    structured two-wire gate without a cotangent (CNOT; its reverse step moves psi and
+    lam) and ``tc = (fwd, adj, adj_stored)`` for the tensor-core 6-wire block kernel (if
+    ``tc_ok``; adj_stored: the reverse step that reads the block's stored input).  Probes
+    use min(bsz, rows that fit 2^27 amplitudes) rows and are scaled to bsz (the kernels
+    stream rows independently)."""
+    key = f"fusion3|{gpu_key(dev)}|n{n}|b{bsz}|tc{int(tc_ok)}"
     hit = lookup(key)
     if hit is not None:
         return hit
@@ -188,6 +189,11 @@ def _pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool, key: str) -> d
             f += _time_ms(lambda: _lib.apply_matrix(psi, n, wires, u, rows), dev)
             a += _time_ms(lambda: _lib.adjoint_matrix(psi, lam, n, wires, u, rows, grad), dev)
         out["dense"][str(k)] = (f / 2 * scale, a / 2 * scale)
+    if n >= 2:
+        f = 0.0
+        for c, t in ((0, 1), (n - 2, n - 1)):
+            f += _time_ms(lambda: _lib.apply_mcx(psi, n, [c], 1, t), dev)
+        out["light"] = (f / 2 * scale, f * scale)
     if tc_ok and n >= 6:
         z = rng.normal(size=(rows, 64, 64)) + 1j * rng.normal(size=(rows, 64, 64))
         u = torch.tensor(np.linalg.qr(z)[0], dtype=torch.complex128, device=dev)
@@ -206,26 +212,43 @@ def _pass_costs(n: int, bsz: int, dev: torch.device, tc_ok: bool, key: str) -> d
     return out
 
 
-def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool,
-              stored: bool = False) -> Tuple[float, List[bool]]:
+LONE_OTHER, LONE_DENSE, LONE_LIGHT = 0, 1, 2
+
+
+def plan_cost(plan, costs: dict, tc_ok: bool, with_adjoint: bool, stored: bool = False,
+              lone_kind: Optional[Sequence[int]] = None) -> Tuple[float, List[bool]]:
     """(cost in ms, per-block use of the tensor-core kernel) of a fusion plan; ``stored``:
-    tensor-core blocks keep their inputs, so their reverse step is the stored-input one."""
+    tensor-core blocks keep their inputs, so their reverse step is the stored-input one.
+    A gate alone in its block runs on its own kernel, costed as a dense pass of its width,
+    unless ``lone_kind[i]`` says otherwise: LONE_DENSE (a dense or controlled gate, whose
+    own kernel is a dense pass with a cotangent) may run as a tensor-core block when that
+    costs less; LONE_LIGHT (controlled-X, swap, phase, diagonal: structured kernels without
+    a cotangent) is costed as the measured ``light`` pass."""
     total = 0.0
     tc_flags = []
+    tcc = costs.get("tc") if tc_ok else None
+    ct = float("inf")
+    if tcc:
+        adj = tcc[2] if stored and len(tcc) > 2 else tcc[1]
+        ct = tcc[0] + (adj if with_adjoint else 0.0)
     for bwires, idxs in plan:
         k = len(bwires)
-        if len(idxs) == 1:  # a lone gate runs on its own kernel (about a dense pass of its width)
-            c = costs["dense"].get(str(min(k, 6)))
-            total += (c[0] + (c[1] if with_adjoint else 0.0)) if c else 0.0
+        dense = costs["dense"].get(str(min(k, 6)))
+        cd = (dense[0] + (dense[1] if with_adjoint else 0.0)) if dense else float("inf")
+        if len(idxs) == 1:  # a lone gate: its own kernel (about a dense pass of its width)
+            kind = lone_kind[idxs[0]] if lone_kind is not None else LONE_OTHER
+            light = costs.get("light")
+            if kind == LONE_DENSE and k <= 6 and ct < cd:
+                total += ct
+                tc_flags.append(True)
+                continue
+            if kind == LONE_LIGHT and light:
+                cd = light[0] + (light[1] if with_adjoint else 0.0)
+            total += cd if dense else 0.0
             tc_flags.append(False)
             continue
-        dense = costs["dense"].get(str(k))
-        cd = dense[0] + (dense[1] if with_adjoint else 0.0) if dense else float("inf")
-        ct = float("inf")
-        if tc_ok and costs.get("tc"):
-            tcc = costs["tc"]
-            adj = tcc[2] if stored and len(tcc) > 2 else tcc[1]
-            ct = tcc[0] + (adj if with_adjoint else 0.0)
+        if k > 6:
+            cd = float("inf")
         use_tc = ct < cd
         total += min(ct, cd)
         tc_flags.append(use_tc)
@@ -238,10 +261,12 @@ WIDE_BEAM_MIN_AMPS = 1 << 27
 
 
 def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: torch.device, tc_ok: bool,
-                  with_adjoint: bool, widths: Sequence[int] = (4, 5, 6), stored: bool = False):
+                  with_adjoint: bool, widths: Sequence[int] = (4, 5, 6), stored: bool = False,
+                  lone_kind: Optional[Sequence[int]] = None):
     """(plan, per-block tensor-core flags, chosen width, cost table) for a segment: the
     cheapest of the candidate plans under the measured per-pass costs (``stored``: the
-    tensor-core blocks are expected to keep their inputs for the backward)."""
+    tensor-core blocks are expected to keep their inputs for the backward; ``lone_kind``:
+    see ``plan_cost``)."""
     from . import fusion
 
     try:
@@ -263,7 +288,7 @@ def choose_fusion(wire_lists: Sequence[Sequence[int]], n: int, bsz: int, dev: to
         variants = ((0, 0), (8, 0), (8, 4)) + (WIDE_BEAMS if wide and k == 6 else ())
         for look, beam in variants:
             plan = fusion.plan_cached(wire_lists, k, look, beam)
-            cost, flags = plan_cost(plan, costs, tc_ok, with_adjoint, stored)
+            cost, flags = plan_cost(plan, costs, tc_ok, with_adjoint, stored, lone_kind)
             if best is None or cost < best[0]:
                 best = (cost, plan, flags, k)
     return best[1], best[2], best[3], costs
