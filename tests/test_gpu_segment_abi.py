@@ -54,12 +54,14 @@ def _replay(sg, n, bsz):
         if isinstance(op, program.StagedRun):
             recs.append(program._staged_record(op, op.descs(), keep))
         elif getattr(op, "members", None) is not None and op.tc:
+            if i == 0:  # the first block acts on |0...0>: U[:, 0] written in place, nothing kept
+                program._zero_input_apply(state, op, n)
+                continue
             r = program._exec(_lib.X_BLOCK_TC, op.wires, batch=op.block_batch, image=op.image)
-            if i > 0:  # the first block acts on |0...0> and keeps nothing
-                out = torch.empty_like(state)
-                r.out = out.data_ptr()
-                stored.append((op, cur))
-                cur = out
+            out = torch.empty_like(state)
+            r.out = out.data_ptr()
+            stored.append((op, cur))
+            cur = out
             recs.append(r)
         elif getattr(op, "members", None) is not None:
             recs.append(program._exec(_lib.X_BLOCK_DENSE, op.wires, batch=op.block_batch, operand=op.operand))

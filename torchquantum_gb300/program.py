@@ -205,18 +205,28 @@ class Segment:
                 with_adj = any(isinstance(r, NativeGate) and r.params.requires_grad for r in records) or \
                     any(not isinstance(r, NativeGate) and r.needs_grad for r in records)
                 stored = with_adj and getattr(qdev, "checkpoint", "auto") is not False
-                plan, tc_flags, k, _ = autotune.choose_fusion(wl, n, self.bsz, dev, tc_ok, with_adj, stored=stored)
+                # how a gate left alone by a plan runs: a dense or controlled gate may still
+                # run as a tensor-core block (its own kernel is a dense pass with a
+                # cotangent, and on large states a 6-wire block's forward + reverse step
+                # costs less); structured gates keep their light kernels
+                lone_kind = [autotune.LONE_OTHER if not fusable(op) else
+                             autotune.LONE_DENSE if op.kind in (engine.KIND_DENSE, engine.KIND_CTRL) else
+                             autotune.LONE_LIGHT for op in ops]
+                plan, tc_flags, k, _ = autotune.choose_fusion(wl, n, self.bsz, dev, tc_ok, with_adj, stored=stored,
+                                                              lone_kind=lone_kind)
+                lone_tc = [len(idxs) == 1 and tc for (_, idxs), tc in zip(plan, tc_flags)]
                 if backend == "tc":
                     tc_flags = [tc_ok for _ in plan]
             else:
                 k = max(1, min(6 if fw == "auto" else int(fw), n, 6))
                 plan = fusion.plan_cached(wl, k, 8, 4)
                 tc_flags = [fusion.use_tensor_cores(qdev, len(bw)) for bw, _ in plan]
+                lone_tc = [False] * len(plan)
             self.fuse_width = k
             exec_ops = []
-            for (bwires, idxs), tc in zip(plan, tc_flags):
+            for (bwires, idxs), tc, lone in zip(plan, tc_flags, lone_tc):
                 members = [ops[i] for i in idxs]
-                if len(members) == 1:  # a lone gate is cheapest on its own kernel
+                if len(members) == 1 and not lone:  # a lone gate on its own kernel
                     exec_ops.append(members[0])
                     continue
                 exec_ops.append(self._make_block(qdev, members, bwires, tc))
@@ -356,13 +366,17 @@ class Segment:
                 if not op.tc:
                     recs.append(_exec(_lib.X_BLOCK_DENSE, op.wires, batch=op.block_batch, operand=op.operand))
                     continue
+                if zero_input and i == 0:
+                    # a first block on |0...0>: its output is column 0 of U at the block's 64
+                    # patterns (every other amplitude stays 0), written directly instead of a
+                    # pass over the state; its reverse step needs neither its input nor the
+                    # cotangent before it (nothing precedes it), so nothing is kept
+                    op.zero_input = True
+                    _zero_input_apply(cur, op, self.n)
+                    continue
                 r = _exec(_lib.X_BLOCK_TC, op.wires, batch=op.block_batch, image=op.image)
                 out = None
-                if zero_input and i == 0:
-                    # a first block on |0...0>: its reverse step needs neither its input nor
-                    # the cotangent before it (nothing precedes it), so nothing is kept
-                    op.zero_input = True
-                elif store_inputs:
+                if store_inputs:
                     out = _new_state(cur)
                     if out is None:  # out of memory: the remaining blocks run in place
                         store_inputs = False
@@ -607,16 +621,35 @@ def _staged_record(run, descs, keep: list) -> "_lib.ExecOp":
     return r
 
 
+def _zero_input_index(blk, n: int, device) -> torch.Tensor:
+    """Amplitude offsets of a 6-wire block's 64 patterns with every other bit clear
+    (wires[0] is the pattern's most significant bit), on the device; built once per block."""
+    idx = getattr(blk, "_zero_idx", None)
+    if idx is None:
+        offs = [sum(1 << (n - 1 - w) for i, w in enumerate(blk.wires) if (j >> (5 - i)) & 1) for j in range(64)]
+        # a pinned staging copy: a copy from pageable memory would block the stream (and
+        # with it the host's run-ahead into the next step)
+        host = torch.tensor(offs, dtype=torch.long).pin_memory()
+        idx = host.to(device, non_blocking=True)
+        blk._zero_idx_host = host  # alive until the copy has run
+        blk._zero_idx = idx
+    return idx
+
+
+def _zero_input_apply(buf: torch.Tensor, blk, n: int) -> None:
+    """A tensor-core block applied to |0...0> in every row of ``buf``: its output is U[:, 0]
+    (complex64) at the 64 pattern offsets, zero elsewhere (pattern 0 is offset 0, so the
+    initial amplitude 1 is overwritten)."""
+    col = blk.u128[:, :, 0].to(torch.complex64)  # [batch, 64]
+    if col.shape[0] != buf.shape[0]:
+        col = col.expand(buf.shape[0], 64)
+    buf.index_copy_(1, _zero_input_index(blk, n, buf.device), col.contiguous())
+
+
 def _add_zero_input_cotangent(lam: torch.Tensor, blk, slot: torch.Tensor, n: int) -> None:
     """gu[b][j][0] += lam[b, offset of pattern j] for a block applied to |0...0> (wires[0] is
     the pattern's most significant bit; the sum over rows when one U serves every row)."""
-    offs = [sum(1 << (n - 1 - w) for i, w in enumerate(blk.wires) if (j >> (5 - i)) & 1) for j in range(64)]
-    # a pinned staging copy: a copy from pageable memory would block the stream (and with
-    # it the host's run-ahead into the next step)
-    host = torch.tensor(offs, dtype=torch.long).pin_memory()
-    idx = host.to(lam.device, non_blocking=True)
-    blk._zero_idx_host = host  # alive until the copy has run
-    vals = lam.index_select(1, idx).to(torch.complex128)  # [bsz, 64]
+    vals = lam.index_select(1, _zero_input_index(blk, n, lam.device)).to(torch.complex128)  # [bsz, 64]
     g = torch.view_as_complex(slot.view(-1, 2)).view(blk.block_batch, 64, 64)
     if blk.block_batch == 1:
         g[0, :, 0] += vals.sum(0)
