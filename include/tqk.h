@@ -214,6 +214,13 @@ int tqk_fused_apply(void* state, int64_t bsz, int n, const int32_t* wires, const
 int tqk_fused_apply_to(const void* state_in, void* state_out, int64_t bsz, int n, const int32_t* wires,
                        const void* image, int64_t u_batch, int* status, void* stream);
 
+/* A fused block applied to |0...0>: `state` holds exactly |0...0> in every row; row b's
+ * amplitude at the block's pattern j (wires[0] the pattern's most significant bit, every
+ * other bit clear) becomes U_b[j][0] rounded to complex64 (u: complex128 [u_batch][64][64]),
+ * which is U |0...0> without a pass over the state.  The block's reverse step is then
+ * skipped: its cotangent is lam conj(e_0)^T, lam read at the same 64 offsets. */
+int tqk_fused_zero_input(void* state, int64_t bsz, int n, const int32_t* wires, const void* u, int64_t u_batch,
+                         void* stream);
 /* Adjoint step of a fused block on the tensor cores: psi <- U^H psi, lam <- U^H lam
  * (image_h = tqk_fused_prepare of U^H on the same wires), and, if mr_out != NULL, the real cross term
  * mr_out[g][2j+p][2j'+q] += sum over columns of Re/Im parts lam_{j,p} * psi_{j',q}
@@ -287,7 +294,11 @@ int tqk_gate_operands(const tqk_gate_desc* gates, int ngates, void* stream);
 /* grad[...] += d loss / d param for every gate with grad != NULL, from op_grad. */
 int tqk_param_grads(const tqk_gate_desc* gates, int ngates, void* stream);
 /* U = G_m ... G_1 per (block, batch row) in float64; replaces upstream static mode's
- * block unitary construction (graph/graphs.py:712-792). */
+ * block unitary construction (graph/graphs.py:712-792).  The tables are device memory and
+ * are not read on the host: a block with k outside 1..6, or an op outside its limits
+ * (1..6 wires, positions below k, dense / controlled parts of 1 or 2 targets, operand rows
+ * of at least the entries its kind reads), is skipped by the kernel (U not written / the
+ * op not applied), never indexed out of bounds. */
 int tqk_block_build(const tqk_block_desc* blocks, int nblocks, int max_batch, const tqk_block_op* ops,
                     void* stream);
 /* From dL/dU (desc.gu) and U (desc.u): every op's operand cotangent, atomically added
@@ -437,7 +448,9 @@ enum {
   TQK_X_SWAP = 5,        /* controlled swap of wires[nctrl], wires[nctrl + 1] */
   TQK_X_STAGED = 6,      /* staged run: `staged[0..nstaged)` in one shared-memory pass */
   TQK_X_BLOCK_TC = 7,    /* fused 6-wire block on the tensor cores: image / image_h */
-  TQK_X_BLOCK_DENSE = 8  /* fused block on the CUDA cores: operand = U (complex64) */
+  TQK_X_BLOCK_DENSE = 8, /* fused block on the CUDA cores: operand = U (complex64) */
+  TQK_X_BLOCK_ZERO = 9   /* fused 6-wire block applied to |0...0> (tqk_fused_zero_input, u = U):
+                            forward only; in the reverse table it must carry skip_reverse */
 };
 typedef struct {
   int32_t kind;            /* TQK_X_* */

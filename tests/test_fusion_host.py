@@ -71,3 +71,31 @@ def test_block_unitary_matches_oracle_product():
                        params=None if g["params"] is None else g["params"][b:b + 1]) for g in ogates]
             cols = O.run(k, 1 << k, og, state=eye)  # row j = U e_j
             np.testing.assert_allclose(u[b], cols.T, atol=1e-12)
+
+
+def test_ops_blocks_cannot_hold_stay_alone_on_small_states():
+    """An op the block kernels cannot hold (a 3-wire dense matrix, an op with an explicit
+    uncompute) is a planner barrier: on a 4-wire state, where all wires fit one 6-wire
+    block, every planner still leaves it alone and moves no gate across it."""
+    from torchquantum_gb300 import program as P
+
+    n = 4
+
+    def dense(wires):
+        d = 1 << len(wires)
+        return engine.TapeOp(engine.KIND_DENSE, wires, operand=torch.eye(d, dtype=torch.complex64)[None])
+
+    wide = dense([0, 1, 2])
+    nonunitary = dense([3])
+    nonunitary.uncompute = torch.eye(2, dtype=torch.complex64)[None]
+    ops = [dense([0]), dense([1]), wide, dense([2]), dense([3]), nonunitary, dense([0]), dense([1, 2])]
+    assert not P.fusable(wide) and not P.fusable(nonunitary) and P.fusable(ops[0])
+    wl = P.planner_wires(ops, n)
+    assert len(wl[2]) > 6 and len(wl[5]) > 6
+    for plan in (fusion.plan_blocks(wl, 6), fusion.plan_blocks(wl, 6, 8), fusion.plan_beam(wl, 6, 4, 8)):
+        where = {i: b for b, (_, idxs) in enumerate(plan) for i in idxs}
+        for barrier in (2, 5):
+            assert plan[where[barrier]][1] == [barrier]
+            # no gate after the barrier sits in a block before it, and none before it after
+            assert all(where[i] < where[barrier] for i in range(barrier))
+            assert all(where[i] > where[barrier] for i in range(barrier + 1, len(ops)))

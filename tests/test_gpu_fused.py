@@ -258,6 +258,50 @@ def test_autotuned_fusion_vs_oracle(tmp_path, monkeypatch):
     A.clear()
 
 
+@pytest.mark.parametrize("checkpoint", ["auto", False])
+def test_lone_gates_as_tensor_core_blocks(monkeypatch, checkpoint):
+    """A plan that leaves every gate alone, with the tensor-core flag set on each (what the
+    autotuner does for a lone dense gate when a padded 6-wire block costs less than the
+    gate's own pass): every fusable gate runs as its own tensor-core block (the others on
+    their own kernels), the first one on |0...0> written directly.  States, expvals and
+    gradients match the oracle and the plain method."""
+    import torchquantum_gb300 as tq
+    from torchquantum_gb300 import autotune as A
+
+    def every_gate_alone(wl, n, bsz, dev, tc_ok, with_adj, widths=(4, 5, 6), stored=False, lone_kind=None):
+        assert lone_kind is not None and len(lone_kind) == len(wl)
+        plan = [(list(w), [i]) for i, w in enumerate(wl)]
+        return plan, [True] * len(plan), 6, None
+
+    rng = np.random.default_rng(41)
+    n, bsz = 14, 2
+    gates = [g for g in _circuit(rng, n, bsz, 30) if len(g["wires"]) <= 2]
+    paulis = ["".join(rng.choice(list("IXYZ"), size=n)) for _ in range(3)]
+    res = {}
+    for method in ("plain", "fused"):
+        if method == "fused":
+            monkeypatch.setattr(A, "choose_fusion", every_gate_alone)
+        q, leaves = _run(n, bsz, gates, method, "auto")
+        q.checkpoint = checkpoint
+        ev = tq.expval_joint_analytical_batch(q, paulis)
+        ev.sum().backward()
+        res[method] = (q.get_states_1d().detach().cpu().numpy(), ev.detach().cpu().numpy(),
+                       [lf.grad.cpu().numpy() for lf in leaves])
+        if method == "fused":
+            from torchquantum_gb300 import program as P
+
+            seg = q._tape[0]
+            blocks = [op for op in seg.exec_ops if getattr(op, "members", None) is not None]
+            assert all(op.tc and len(op.members) == 1 and len(op.wires) == 6 for op in blocks)
+            assert sum(1 for op in seg.records if P.fusable(op)) == len(blocks) > 0
+            if getattr(seg.exec_ops[0], "members", None) is not None:
+                assert getattr(seg.exec_ops[0], "zero_input", False)
+    assert np.abs(res["fused"][0] - O.run(n, bsz, gates)).max() < 1e-5
+    assert np.abs(res["fused"][1] - res["plain"][1]).max() < 1e-5
+    for gp, gf in zip(res["plain"][2], res["fused"][2]):
+        assert np.abs(gf - gp).max() < 1e-5
+
+
 def test_adjoint_image_and_cross_grad_kernels():
     """tqk_fused_prepare_adjoint(U) is byte-identical to tqk_fused_prepare(U^H), and
     tqk_fused_cross_grad adds M U (M from the real cross term) into a float64 cotangent

@@ -55,7 +55,7 @@ def _replay(sg, n, bsz):
             recs.append(program._staged_record(op, op.descs(), keep))
         elif getattr(op, "members", None) is not None and op.tc:
             if i == 0:  # the first block acts on |0...0>: U[:, 0] written in place, nothing kept
-                program._zero_input_apply(state, op, n)
+                recs.append(program._exec(_lib.X_BLOCK_ZERO, op.wires, batch=op.block_batch, u=op.u128))
                 continue
             r = program._exec(_lib.X_BLOCK_TC, op.wires, batch=op.block_batch, image=op.image)
             out = torch.empty_like(state)

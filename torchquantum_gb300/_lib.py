@@ -74,6 +74,7 @@ _SIGS = {
     "tqk_fused_adjoint": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
     "tqk_fused_apply_to": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp]),
     "tqk_fused_adjoint_stored": (_int, [_vp, _vp, _i64, _int, _i32p, _vp, _i64, _vp, _vp, _vp]),
+    "tqk_fused_zero_input": (_int, [_vp, _i64, _int, _i32p, _vp, _i64, _vp]),
     "tqk_pauli_expval_noalloc_capacity": (_i64, []),
     "tqk_pauli_expval_noalloc": (_int, [_vp, _i64, _int, _u64p, _u64p, _int, _vp, _vp]),
     "tqk_segment_forward": (_int, [_vp, _i64, _int, _vp, _int, _vp, _vp, _vp, EXEC_HOOK, _vp, _vp]),
@@ -359,7 +360,7 @@ class ExecOp(ctypes.Structure):
 
 
 assert ctypes.sizeof(ExecOp) == 184
-X_DENSE, X_CTRL, X_MCX, X_PHASE, X_DIAG, X_SWAP, X_STAGED, X_BLOCK_TC, X_BLOCK_DENSE = range(9)
+X_DENSE, X_CTRL, X_MCX, X_PHASE, X_DIAG, X_SWAP, X_STAGED, X_BLOCK_TC, X_BLOCK_DENSE, X_BLOCK_ZERO = range(10)
 # Optional Python callables (exec record, after) the runners call around each op's
 # launches, per direction (bench.py installs one to time the dominant kernel's launches
 # inside a step).
@@ -481,6 +482,13 @@ def fused_apply_to(src, dst, n, wires, image, u_batch):
     """dst = U src for a fused block (src unchanged)."""
     _check(load().tqk_fused_apply_to(src.data_ptr(), dst.data_ptr(), src.shape[0], n, _i32(wires), image.data_ptr(),
                                      u_batch, status_word(src.device).data_ptr(), _stream(src)))
+
+
+def fused_zero_input(state, n, wires, u128):
+    """A fused block applied to |0...0> (``state`` holds exactly that): U[:, :, 0] written
+    at the block's 64 patterns."""
+    _check(load().tqk_fused_zero_input(state.data_ptr(), state.shape[0], n, _i32(wires), u128.data_ptr(),
+                                       int(u128.shape[0]), _stream(state)))
 
 
 def fused_adjoint_stored(psi_in, lam, n, wires, image_h, u_batch, mr_out):

@@ -856,6 +856,51 @@ extern "C" int tqk_fused_cross_add_many(const tqk_cross_job* jobs, int njobs, in
   return launch_status("tqk_fused_cross_add_many");
 }
 
+namespace tqk {
+namespace tc {
+
+// Amplitude offsets of a 6-wire block's 64 patterns with every other bit clear.
+struct PatternOffsets {
+  uint64_t off[64];
+};
+
+// A block applied to |0...0>: row b's amplitude at pattern j becomes U_b[j][0] (the rest of
+// the row is zero already).  One thread per pattern, one CTA per row.
+__global__ void __launch_bounds__(64) k_zero_input(float2* state, int n, const double2* u, int64_t u_batch,
+                                                   const __grid_constant__ PatternOffsets po) {
+  const int64_t b = blockIdx.x;
+  const int j = threadIdx.x;
+  const double2 v = u[((u_batch > 1 ? b : 0) * 64 + j) * 64];
+  state[(b << n) + po.off[j]] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+}
+
+}  // namespace tc
+}  // namespace tqk
+
+extern "C" int tqk_fused_zero_input(void* state, int64_t bsz, int n, const int32_t* wires, const void* u,
+                                    int64_t u_batch, void* stream) {
+  using namespace tqk;
+  const char* what = "tqk_fused_zero_input";
+  int rc = check_state(state, bsz, n, what);
+  if (rc) return rc;
+  if ((rc = check_batch(u_batch, bsz, what))) return rc;
+  if (u == nullptr) return fail(TQK_BAD_POINTER, "%s: null block unitary", what);
+  if (bsz > 2147483647ll) return fail(TQK_BAD_SHAPE, "%s: bsz %lld", what, (long long)bsz);
+  int bits[6];
+  uint64_t used = 0;
+  if ((rc = wires_to_bits(n, wires, 6, bits, &used, what))) return rc;
+  tc::PatternOffsets po;
+  for (int j = 0; j < 64; ++j) {
+    uint64_t o = 0;
+    for (int i = 0; i < 6; ++i)
+      if ((j >> (5 - i)) & 1) o |= 1ull << bits[i];
+    po.off[j] = o;
+  }
+  tc::k_zero_input<<<static_cast<unsigned>(bsz), 64, 0, as_stream(stream)>>>(
+      static_cast<float2*>(state), n, static_cast<const double2*>(u), u_batch, po);
+  return launch_status(what);
+}
+
 namespace {
 
 // One free dimension of a tile and what it adds to an amplitude offset, the tile row

@@ -383,17 +383,39 @@ __device__ void apply_op_rows(C* U, int D, const tqk_block_op& op, const double2
   }
 }
 
+// Descriptor limits the block kernels rely on (shared memory holds a 64 x 64 block; an op
+// touches at most 6 wires, a dense part at most 2 targets): a block or op outside them is
+// skipped, never indexed (the host checks them before upload).
+__device__ __forceinline__ bool block_ok(const tqk_block_desc& bl) { return bl.k >= 1 && bl.k <= 6 && bl.num_ops >= 0; }
+
+__device__ __forceinline__ bool op_ok(const tqk_block_op& op, int k) {
+  if (op.nw < 1 || op.nw > 6 || op.nctrl < 0 || op.nctrl > op.nw) return false;
+  for (int j = 0; j < op.nw; ++j)
+    if (op.pos[j] < 0 || op.pos[j] >= k) return false;
+  const int kt = op.nw - op.nctrl;
+  switch (op.kind) {
+    case TQK_K_DENSE:
+    case TQK_K_CTRL: return kt >= 1 && kt <= 2 && op.op_size >= (1 << kt) * (1 << kt);
+    case TQK_K_X: return kt == 1;
+    case TQK_K_SWAP: return kt == 2;
+    case TQK_K_PHASE: return op.op_size >= 1;
+    case TQK_K_DIAG: return op.op_size >= (1 << op.nw);
+    default: return false;
+  }
+}
+
 __global__ void k_block_build(const tqk_block_desc* blocks, const tqk_block_op* ops) {
   extern __shared__ double2 smem_u[];
   C2* U = reinterpret_cast<C2*>(smem_u);
   const tqk_block_desc bl = blocks[blockIdx.x];
   const int64_t b = blockIdx.y;
-  if (b >= bl.batch) return;
+  if (b >= bl.batch || !block_ok(bl)) return;
   const int D = 1 << bl.k;
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) U[e] = mk((e / D) == (e % D) ? 1.0 : 0.0, 0.0);
   __syncthreads();
   for (int i = 0; i < bl.num_ops; ++i) {
     const tqk_block_op op = ops[bl.first_op + i];
+    if (!op_ok(op, bl.k)) continue;  // uniform for the CTA
     const double2* opnd = static_cast<const double2*>(op.operand) + (op.batch > 1 ? b : 0) * op.op_size;
     apply_op_rows(U, D, op, opnd, false);
     __syncthreads();
@@ -627,7 +649,7 @@ __global__ void k_block_unbuild(const tqk_block_desc* blocks, const tqk_block_op
   extern __shared__ double2 smem_u[];
   const tqk_block_desc bl = blocks[blockIdx.x];
   const int64_t b = blockIdx.y;
-  if (b >= bl.batch || bl.gu == nullptr) return;
+  if (b >= bl.batch || bl.gu == nullptr || !block_ok(bl)) return;
   const int D = 1 << bl.k;
   F2* W = reinterpret_cast<F2*>(smem_u);
   F2* X = W + D * D;
@@ -640,6 +662,7 @@ __global__ void k_block_unbuild(const tqk_block_desc* blocks, const tqk_block_op
   __syncthreads();
   for (int i = bl.num_ops - 1; i >= 0; --i) {
     const tqk_block_op op = ops[bl.first_op + i];
+    if (!op_ok(op, bl.k)) continue;  // uniform for the CTA
     const double2* opnd = static_cast<const double2*>(op.operand) + (op.batch > 1 ? b : 0) * op.op_size;
     apply_op_rows(W, D, op, opnd, true);  // W <- G^H W = product of the ops before op
     __syncthreads();

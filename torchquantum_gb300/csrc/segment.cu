@@ -52,6 +52,10 @@ int check_op(const tqk_exec_op& op, int i, const char* what) {
         return fail(TQK_BAD_POINTER, "%s: op %d: a block cotangent needs mr (and u without a stored input)", what,
                     i);
       return TQK_OK;
+    case TQK_X_BLOCK_ZERO:
+      if (op.nw != 6 || op.u == nullptr)
+        return fail(TQK_BAD_SHAPE, "%s: op %d: a zero-input block has 6 wires and its U", what, i);
+      return TQK_OK;
     case TQK_X_MCX:
       if (op.nw != op.nctrl + 1) return fail(TQK_BAD_SHAPE, "%s: op %d: MCX has one target", what, i);
       return TQK_OK;
@@ -120,6 +124,9 @@ extern "C" int tqk_segment_forward(void* state, int64_t bsz, int n, const tqk_ex
           rc = tqk_fused_apply(cur, bsz, n, w, op.image, op.batch, status, stream);
         }
         break;
+      case TQK_X_BLOCK_ZERO:
+        rc = tqk_fused_zero_input(cur, bsz, n, w, op.u, op.batch, stream);
+        break;
     }
     if (rc) return rc;
     if (hook) hook(i, op.kind, 1, user);
@@ -144,6 +151,9 @@ extern "C" int tqk_segment_backward(const void* psi_end, void* lam, void* work, 
     if ((rc = check_op(ops[i], i, what))) return rc;
   for (int i = 1; i < nops; ++i)
     if (ops[i].skip_reverse) return fail(TQK_BAD_SHAPE, "%s: only op 0 may skip the reverse sweep", what);
+  for (int i = 0; i < nops; ++i)
+    if (ops[i].kind == TQK_X_BLOCK_ZERO && !ops[i].skip_reverse)
+      return fail(TQK_BAD_SHAPE, "%s: op %d: a zero-input block has no reverse step (set skip_reverse)", what, i);
   int64_t count = 0;
   cudaStream_t st = as_stream(stream);
   Cursor psi{psi_end, work, static_cast<size_t>(bsz) * (static_cast<size_t>(8) << n), false, st, &count};

@@ -195,7 +195,7 @@ class Segment:
         # ---- plan
         self.blocks = []
         if method == "fused":
-            wl = [op.wires if fusable(op) else list(range(n)) for op in ops]
+            wl = planner_wires(ops, n)
             fw = qdev.fuse_wires
             backend = getattr(qdev, "fused_backend", "auto")
             tc_ok = backend != "cuda" and n >= fusion.TC_MIN_WIRES
@@ -226,7 +226,7 @@ class Segment:
             exec_ops = []
             for (bwires, idxs), tc, lone in zip(plan, tc_flags, lone_tc):
                 members = [ops[i] for i in idxs]
-                if len(members) == 1 and not lone:  # a lone gate on its own kernel
+                if len(members) == 1 and not (lone and fusable(members[0])):  # a lone gate on its own kernel
                     exec_ops.append(members[0])
                     continue
                 exec_ops.append(self._make_block(qdev, members, bwires, tc))
@@ -247,6 +247,8 @@ class Segment:
     def _make_block(self, qdev, members, bwires, tc):
         from . import fusion
 
+        if len(bwires) > 6 or not all(fusable(m) for m in members):
+            raise _lib.TQKError(1, f"a fused block holds at most 6 wires of fusable ops (got {len(bwires)} wires)")
         if tc:
             bwires = fusion._pad_wires(bwires, self.n)
         k = len(bwires)
@@ -372,7 +374,7 @@ class Segment:
                     # pass over the state; its reverse step needs neither its input nor the
                     # cotangent before it (nothing precedes it), so nothing is kept
                     op.zero_input = True
-                    _zero_input_apply(cur, op, self.n)
+                    recs.append(_exec(_lib.X_BLOCK_ZERO, op.wires, batch=op.block_batch, u=op.u128))
                     continue
                 r = _exec(_lib.X_BLOCK_TC, op.wires, batch=op.block_batch, image=op.image)
                 out = None
@@ -636,16 +638,6 @@ def _zero_input_index(blk, n: int, device) -> torch.Tensor:
     return idx
 
 
-def _zero_input_apply(buf: torch.Tensor, blk, n: int) -> None:
-    """A tensor-core block applied to |0...0> in every row of ``buf``: its output is U[:, 0]
-    (complex64) at the 64 pattern offsets, zero elsewhere (pattern 0 is offset 0, so the
-    initial amplitude 1 is overwritten)."""
-    col = blk.u128[:, :, 0].to(torch.complex64)  # [batch, 64]
-    if col.shape[0] != buf.shape[0]:
-        col = col.expand(buf.shape[0], 64)
-    buf.index_copy_(1, _zero_input_index(blk, n, buf.device), col.contiguous())
-
-
 def _add_zero_input_cotangent(lam: torch.Tensor, blk, slot: torch.Tensor, n: int) -> None:
     """gu[b][j][0] += lam[b, offset of pattern j] for a block applied to |0...0> (wires[0] is
     the pattern's most significant bit; the sum over rows when one U serves every row)."""
@@ -796,6 +788,15 @@ def _generic128(m) -> torch.Tensor:
     t = engine.kernel_operand(t.to(torch.complex128))
     m._op128_keep = t
     return t
+
+
+def planner_wires(ops, n: int) -> List[List[int]]:
+    """Wire lists the fusion planners see: an op's wires, or for an op the block kernels
+    cannot hold (``fusable`` false) a barrier -- every wire (nothing moves across it) plus
+    7 placeholder wires, wider than any block, so every planner leaves it alone (also when
+    n <= 6, where all n wires would fit in one block)."""
+    barrier = list(range(n)) + [-1 - i for i in range(7)]
+    return [list(op.wires) if fusable(op) else barrier for op in ops]
 
 
 def fusable(op) -> bool:
