@@ -463,7 +463,8 @@ typedef struct {
   const void* uncompute;   /* DENSE / CTRL: exact inverse for psi (non-unitary gates), or NULL */
   const void* image;       /* BLOCK_TC forward image (tqk_fused_prepare of U) */
   const void* image_h;     /* BLOCK_TC reverse image (of U^H) */
-  const void* u;           /* BLOCK_TC: U, complex128 [batch][64][64] (in-place reverse step's M U) */
+  const void* u;           /* BLOCK_TC: U, complex128 [batch][64][64] (in-place reverse step's M U);
+                              BLOCK_ZERO: the same U, whose column 0 the op writes */
   void* out;               /* BLOCK_TC forward: the block's output buffer (its input is then kept
                               as the stored input), or NULL to apply in place */
   const void* stored;      /* BLOCK_TC reverse: the block's stored input, or NULL (uncompute) */
