@@ -342,9 +342,13 @@ __device__ __forceinline__ void prefetch_lines(const TcParams& p, const float2* 
 
 // Producer: the thread's 32 amplitudes of a tile (load_tile), split into bf16 hi/lo and
 // stored as its four 16-byte chunks (K = 64p + 8g + e) of the A image (store_tile).
+// The loads take the read-only (non-coherent) path: every 128-byte line belongs to one tile
+// (see line_owner_mask), is read once by that tile's producers, and is written (by the
+// epilogue, in place or lam) only after the tile's MMAs consumed it, so no line is read
+// again after a write within the launch.
 __device__ __forceinline__ void load_tile(const TcParams& p, const float2* src, float2 (&a)[32]) {
 #pragma unroll
-  for (int r = 0; r < 32; ++r) a[r] = src[p.reg_off[r]];
+  for (int r = 0; r < 32; ++r) a[r] = __ldg(src + p.reg_off[r]);
 }
 
 __device__ __forceinline__ void store_tile(const float2 (&a)[32], const TcParams& p, uint8_t* abuf, int row0,
