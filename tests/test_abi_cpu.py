@@ -119,3 +119,27 @@ def test_segment_entry_points_marshal_without_launching(lib):
     two[1].skip_reverse = 1
     rc = lib.tqk_segment_backward(16, 32, None, 1, 4, two, 2, 16, None, None, hook, None, None)
     assert rc == 2 and b"only op 0" in lib.tqk_last_error() and called == []
+
+
+def test_zero_input_block_op_is_checked_on_the_host(lib):
+    """A TQK_X_BLOCK_ZERO op needs 6 wires and its U, and in a reverse table it must carry
+    skip_reverse (it has no reverse step); tqk_fused_zero_input rejects bad wires and
+    batches before any launch."""
+    import ctypes
+
+    ops = (_lib.ExecOp * 1)()
+    ops[0].kind, ops[0].nw = _lib.X_BLOCK_ZERO, 6
+    for j in range(6):
+        ops[0].wires[j] = j
+    final = ctypes.c_void_p()
+    rc = lib.tqk_segment_forward(16, 1, 8, ops, 1, 16, ctypes.byref(final), None, _lib.EXEC_HOOK(), None, None)
+    assert rc == 2 and b"zero-input block" in lib.tqk_last_error()  # no U
+    ops[0].u = 64
+    rc = lib.tqk_segment_backward(16, 32, None, 1, 8, ops, 1, 16, None, None, _lib.EXEC_HOOK(), None, None)
+    assert rc == 2 and b"skip_reverse" in lib.tqk_last_error()
+    w = (ctypes.c_int32 * 6)(0, 1, 2, 3, 4, 4)
+    rc = lib.tqk_fused_zero_input(16, 1, 8, w, 64, 1, None)
+    assert rc != 0 and b"used twice" in lib.tqk_last_error()
+    w = (ctypes.c_int32 * 6)(0, 1, 2, 3, 4, 5)
+    rc = lib.tqk_fused_zero_input(16, 4, 8, w, 64, 3, None)
+    assert rc != 0
