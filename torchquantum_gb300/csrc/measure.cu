@@ -477,10 +477,6 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
     }
     const int64_t b = item / p.cosets;
     const uint32_t rep = coset_rep(static_cast<uint32_t>(item - b * p.cosets), p);
-    uint32_t rho[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-      rho[s] = (!SEED && s < p.ns) ? ((static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u) : 0u;
     bool ok = *vquit == 0;
     if (ok && !bulk::mbar_wait(&full[st], static_cast<uint32_t>(it / kCosetStages) & 1u)) {
       ok = false;
@@ -490,9 +486,6 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
       }
     }
     const uint32_t b4 = static_cast<uint32_t>(st) * (tile >> 1);  // stage start, float4 units
-    float acc[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) acc[s] = 0.f;
     if (ok && SEED) {
       // string by string over the thread's output pairs (outputs in registers), then one
       // store per pair; each string's orientation and Y parity are fixed for its loop
@@ -544,40 +537,42 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
       // amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the side whose bit
       // hb (the highest of xs) is clear -- enumerated directly by inserting a zero at hb --
       // and counted twice (P is Hermitian: both sides contribute the same real part).
-      uint32_t first[NS + 1];
-      first[0] = 0;
+      uint32_t total = 0;
 #pragma unroll
-      for (int s = 0; s < NS; ++s)
-        first[s + 1] = first[s] + (kind[s] == 3u ? 0u : (kind[s] == 2u ? tile >> 2 : tile >> 1));
-      const uint32_t per = ((first[NS] + kCosetWarps - 1) / kCosetWarps + 31u) & ~31u;
-      const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(first[NS], w0 + per);
+      for (int s = 0; s < NS; ++s) total += kind[s] == 3u ? 0u : (kind[s] == 2u ? tile >> 2 : tile >> 1);
+      const uint32_t per = ((total + kCosetWarps - 1) / kCosetWarps + 31u) & ~31u;
+      const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(total, w0 + per);
+      // the warp's row of red: zero, then the sums of the strings its segment touches (one
+      // string body in the code, looped at run time, instead of one per string)
+      if (lane < NS) red[it & 1][warp][lane] = 0.f;
+      __syncwarp();
+      uint32_t f0 = 0;
+#pragma unroll 1
+      for (int s = 0; s < p.ns && f0 < w1; ++s) {
+        const uint32_t ks = p.kind[s];
+        const uint32_t f1 = f0 + (ks == 3u ? 0u : (ks == 2u ? tile >> 2 : tile >> 1));
+        const uint32_t lo = max(f0, w0), hi = min(f1, w1);
+        if (lo < hi) {  // uniform for the warp
+          const uint32_t j0 = lo - f0 + lane, j1 = hi - f0;
+          const uint32_t xs_s = p.xs[s], gam_s = p.gam[s], hb_s = p.hb[s], odd_s = p.odd[s];
+          const uint32_t rho_s = (static_cast<uint32_t>(__popc(rep & p.zh[s])) ^ p.fl[s]) & 1u;
+          float a;
+          if (ks == 0u) a = coset_diag_sum(b4, j0, j1, gam_s, rho_s);
+          else if (ks == 1u) a = 2.f * coset_x1_sum(b4, j0, j1, odd_s != 0u, gam_s, rho_s);
+          else if (xs_s & 1u)
+            a = 2.f * (odd_s ? coset_string_sum<true, true>(b4, j0, j1, hb_s, xs_s, gam_s, rho_s)
+                             : coset_string_sum<true, false>(b4, j0, j1, hb_s, xs_s, gam_s, rho_s));
+          else
+            a = 2.f * (odd_s ? coset_string_sum<false, true>(b4, j0, j1, hb_s, xs_s, gam_s, rho_s)
+                             : coset_string_sum<false, false>(b4, j0, j1, hb_s, xs_s, gam_s, rho_s));
 #pragma unroll
-      for (int s = 0; s < NS; ++s) {
-        const uint32_t lo = max(first[s], w0), hi = min(first[s + 1], w1);
-        if (lo >= hi) continue;  // uniform for the warp
-        const uint32_t j0 = lo - first[s] + lane, j1 = hi - first[s];
-        float a;
-        if (kind[s] == 0u) a = coset_diag_sum(b4, j0, j1, gam[s], rho[s]);
-        else if (kind[s] == 1u) a = 2.f * coset_x1_sum(b4, j0, j1, odd[s] != 0u, gam[s], rho[s]);
-        else if (xs[s] & 1u)
-          a = 2.f * (odd[s] ? coset_string_sum<true, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
-                            : coset_string_sum<true, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
-        else
-          a = 2.f * (odd[s] ? coset_string_sum<false, true>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s])
-                            : coset_string_sum<false, false>(b4, j0, j1, hb[s], xs[s], gam[s], rho[s]));
-        acc[s] = a;
+          for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+          if (lane == 0) red[it & 1][warp][s] = a;
+        }
+        f0 = f1;
       }
-    }
-    if (!SEED) {
-      // CTA sum of each string's accumulators: warps in float32, the warps' sums in
-      // float64 in a fixed order; red is double-buffered by item parity
-#pragma unroll
-      for (int s = 0; s < NS; ++s)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
-      if (lane == 0)
-#pragma unroll
-        for (int s = 0; s < NS; ++s) red[it & 1][warp][s] = acc[s];
+    } else if (!SEED) {
+      if (lane < NS) red[it & 1][warp][lane] = 0.f;  // a stage that never arrived: its partials are NaN below
     }
     __syncthreads();  // the stage is read: the next iteration may refill it
     if (!SEED && warp == 0 && lane < p.ns) {
