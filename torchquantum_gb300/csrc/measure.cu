@@ -331,7 +331,7 @@ __device__ __forceinline__ float coset_string_sum(uint32_t b4, uint32_t j0, uint
   const uint32_t g1 = gam & 1u;
   const uint32_t x4 = x >> 1;  // partner pair index = (u >> 1) ^ (x >> 1)
   float a = 0.f;
-#pragma unroll 2
+#pragma unroll 4
   for (uint32_t j = j0; j < j1; j += 32) {
     // pair index of u: j with a zero inserted at bit h - 1 (u = 2 x pair index, h >= 1)
     const uint32_t pu = ((j >> (h - 1)) << h) | (j & (lo >> 1));
