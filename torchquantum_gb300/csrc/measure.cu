@@ -455,15 +455,10 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
   int64_t issued = 0;  // pipeline iterations whose loads this CTA issued
   for (; issued < kCosetStages - 1 && blockIdx.x + issued * gridDim.x < total; ++issued)
     coset_issue(p, blockIdx.x + issued * gridDim.x, static_cast<int>(issued), slot_hi, full);
-  uint32_t xs[NS], gam[NS], odd[NS], kind[NS], hb[NS];
-#pragma unroll
-  for (int s = 0; s < NS; ++s) {
-    xs[s] = s < p.ns ? p.xs[s] : 0u;
-    gam[s] = s < p.ns ? p.gam[s] : 0u;
-    odd[s] = s < p.ns ? p.odd[s] : 0u;
-    kind[s] = s < p.ns ? p.kind[s] : 3u;
-    hb[s] = s < p.ns ? p.hb[s] : 0u;
-  }
+  // expvals: pair visits of all strings in a coset (tile / 4 per string, tile / 2 for x = 0
+  // or 1; strings past ns are padding)
+  uint32_t visits = 0;
+  for (int s = 0; s < p.ns; ++s) visits += p.kind[s] == 3u ? 0u : (p.kind[s] == 2u ? tile >> 2 : tile >> 1);
   const uint32_t lmask = (1u << p.c) - 1u;
   int it = 0;
   for (int64_t item = blockIdx.x; item < total; item += gridDim.x, ++it) {
@@ -537,11 +532,8 @@ __global__ void __launch_bounds__(kCosetThreads, 1) k_coset(const CosetParams p)
       // amplitude pairs (u, u + 1) / ((u ^ xs) & ~1) is visited once, from the side whose bit
       // hb (the highest of xs) is clear -- enumerated directly by inserting a zero at hb --
       // and counted twice (P is Hermitian: both sides contribute the same real part).
-      uint32_t total = 0;
-#pragma unroll
-      for (int s = 0; s < NS; ++s) total += kind[s] == 3u ? 0u : (kind[s] == 2u ? tile >> 2 : tile >> 1);
-      const uint32_t per = ((total + kCosetWarps - 1) / kCosetWarps + 31u) & ~31u;
-      const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(total, w0 + per);
+      const uint32_t per = ((visits + kCosetWarps - 1) / kCosetWarps + 31u) & ~31u;
+      const uint32_t w0 = static_cast<uint32_t>(warp) * per, w1 = min(visits, w0 + per);
       // the warp's row of red: zero, then the sums of the strings its segment touches (one
       // string body in the code, looped at run time, instead of one per string)
       if (lane < NS) red[it & 1][warp][lane] = 0.f;
